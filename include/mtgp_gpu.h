@@ -1,0 +1,332 @@
+/*
+ * mtgp_gpu.h -- C ABI of the GB300 MTGP generator.
+ *
+ * Drop-in GPU replacement for the MTGP reference C API (MersenneTwister-Lab/MTGP,
+ * v1.1.2).  Every entry point below names the reference function it replaces.
+ * The generated sequences are bit-identical to the reference's
+ * mtgp32-fast.c / mtgp64-fast.c for the same parameter set, seed and offset,
+ * floats included.
+ *
+ * Conventions
+ *   - Plain C types only: pointers, sizes, ints.  CUDA streams are passed as
+ *     `void *` (a cudaStream_t; NULL = legacy default stream).
+ *   - Every function returns an int status (MTGP_OK == 0, negative on error);
+ *     no C++ exception crosses this boundary.  The reference returns -1 on
+ *     allocation failure (mtgp32-fast.c:49-51) and asserts on malformed jump
+ *     strings (mtgp32-fast-jump.c:62); here both are status codes.
+ *     mtgp_gpu_last_error() returns a per-thread message for the last failure.
+ *   - Output buffers are caller-owned DEVICE memory unless a name says _host.
+ *   - A handle is single-owner, like the reference's mtgp32_fast_t: calls on one
+ *     handle must not race; different handles are independent.
+ *   - Fills are asynchronous on the given stream; the handle's device state is
+ *     advanced in stream order, so successive fills on one stream continue the
+ *     sequence exactly like successive genrand_* calls.
+ *
+ * The parameter and state structs have the reference's layout
+ * (mtgp32-fast.h:47-88, mtgp64-fast.h:46-87), so the reference's parameter
+ * tables (mtgp32-param-fast.c, mtgp64-param-fast.c, ...) link unchanged.  If a
+ * translation unit also includes the reference's mtgp32-fast.h / mtgp64-fast.h,
+ * include those first: this header then uses their definitions.
+ */
+#ifndef MTGP_GPU_H
+#define MTGP_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__cplusplus)
+extern "C" {
+#endif
+
+/* ---- reference-layout types (mtgp32-fast.h:47-88) ------------------------ */
+#if !defined(MTGP32_FAST_H)
+#define MTGP_GPU_DEFINES_MTGP32_TYPES 1
+typedef struct MTGP32_PARAMS_FAST_T {
+    int mexp;                   /* Mersenne exponent                       */
+    int pos;                    /* pick-up position                        */
+    int sh1;                    /* shift 1                                 */
+    int sh2;                    /* shift 2                                 */
+    uint32_t tbl[16];           /* recursion table                         */
+    uint32_t tmp_tbl[16];       /* tempering table                         */
+    uint32_t flt_tmp_tbl[16];   /* tempering + [1,2) float packing table   */
+    uint32_t mask;              /* state-space mask of the oldest word     */
+    unsigned char poly_sha1[21];
+} mtgp32_params_fast_t;
+
+typedef struct MTGP32_STATUS_FAST_T {
+    int idx;
+    int size;
+    int large_size;
+    int large_mask;
+    uint32_t array[];
+} mtgp32_status_fast_t;
+
+typedef struct MTGP32_FAST_T {
+    mtgp32_params_fast_t params;
+    mtgp32_status_fast_t *status;
+} mtgp32_fast_t;
+#endif
+
+/* ---- reference-layout types (mtgp64-fast.h:46-87) ------------------------ */
+#if !defined(MTGP64_FAST_H)
+#define MTGP_GPU_DEFINES_MTGP64_TYPES 1
+typedef struct MTGP64_PARAMS_FAST_T {
+    int mexp;
+    int pos;
+    int sh1;
+    int sh2;
+    uint64_t tbl[16];
+    uint64_t tmp_tbl[16];
+    uint64_t dbl_tmp_tbl[16];
+    uint64_t mask;
+    unsigned char poly_sha1[21];
+} mtgp64_params_fast_t;
+
+typedef struct MTGP64_STATUS_FAST_T {
+    int idx;
+    int size;
+    int large_size;
+    int large_mask;
+    uint64_t array[];
+} mtgp64_status_fast_t;
+
+typedef struct MTGP64_FAST_T {
+    mtgp64_params_fast_t params;
+    mtgp64_status_fast_t *status;
+} mtgp64_fast_t;
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define MTGP_OK               0
+#define MTGP_ERR_ALLOC      (-1)  /* host or device allocation failed (ref: -1)  */
+#define MTGP_ERR_INVALID    (-2)  /* NULL handle/pointer, bad size or parameter  */
+#define MTGP_ERR_UNSUPPORTED (-3) /* parameter set shape not supported          */
+#define MTGP_ERR_BAD_JUMP   (-4)  /* malformed jump string / polynomial         */
+#define MTGP_ERR_CUDA       (-5)  /* CUDA runtime error (message has details)   */
+#define MTGP_ERR_TIMEOUT    (-6)  /* a bounded device-side wait gave up         */
+#define MTGP_ERR_BUDGET     (-7)  /* request exceeds the device-memory budget   */
+#define MTGP_ERR_BUSY       (-8)  /* no free slot; retry later                  */
+
+/* Output kinds; the numbering is shared by all fill/batch entry points. */
+#define MTGP_KIND_UINT       0   /* genrand_uint32 / genrand_uint64          */
+#define MTGP_KIND_CLOSE1_OPEN2 1 /* [1,2)  genrand_close1_open2              */
+#define MTGP_KIND_CLOSE_OPEN 2   /* [0,1)  genrand_close_open                */
+#define MTGP_KIND_OPEN_CLOSE 3   /* (0,1]  genrand_open_close                */
+#define MTGP_KIND_OPEN_OPEN  4   /* (0,1)  genrand_open_open                 */
+
+/* Message describing the calling thread's last failed call ("" if none). */
+const char *mtgp_gpu_last_error(void);
+/* Library version string. */
+const char *mtgp_gpu_version(void);
+
+/* ========================================================================= */
+/* Single generator (replaces mtgp32_fast_t usage)                            */
+/* ========================================================================= */
+typedef struct mtgp32_gpu mtgp32_gpu_t;
+typedef struct mtgp64_gpu mtgp64_gpu_t;
+
+/* Replaces mtgp32_init (mtgp32-fast.c:94-104) + mtgp32_init_state (:119-137).
+ * Allocates the device-resident state; the seeding is done on the host with
+ * the reference's exact arithmetic. */
+int mtgp32_gpu_init(mtgp32_gpu_t **out, const mtgp32_params_fast_t *para,
+                    uint32_t seed);
+/* Replaces mtgp32_init_by_array (mtgp32-fast.c:151-235). */
+int mtgp32_gpu_init_by_array(mtgp32_gpu_t **out,
+                             const mtgp32_params_fast_t *para,
+                             const uint32_t *array, int length);
+/* Replaces mtgp32_init_by_str (mtgp32-fast.c:250-334). */
+int mtgp32_gpu_init_by_str(mtgp32_gpu_t **out,
+                           const mtgp32_params_fast_t *para, const char *str);
+/* Replaces mtgp32_free (mtgp32-fast.c:342-344).  Synchronises the handle's
+ * internal stream before freeing.  NULL is a no-op. */
+void mtgp32_gpu_free(mtgp32_gpu_t *h);
+
+/* n successive mtgp32_genrand_uint32 (mtgp32-fast.h:252-267) into dev_out. */
+int mtgp32_gpu_fill_uint32(mtgp32_gpu_t *h, uint32_t *dev_out, size_t n,
+                           void *stream);
+/* n successive mtgp32_genrand_close1_open2 (mtgp32-fast.h:278-293). */
+int mtgp32_gpu_fill_close1_open2(mtgp32_gpu_t *h, float *dev_out, size_t n,
+                                 void *stream);
+/* n successive mtgp32_genrand_close_open (mtgp32-fast.h:304-306). */
+int mtgp32_gpu_fill_close_open(mtgp32_gpu_t *h, float *dev_out, size_t n,
+                               void *stream);
+/* n successive mtgp32_genrand_open_close (mtgp32-fast.h:317-319). */
+int mtgp32_gpu_fill_open_close(mtgp32_gpu_t *h, float *dev_out, size_t n,
+                               void *stream);
+/* n successive mtgp32_genrand_open_open (mtgp32-fast.h:330-346). */
+int mtgp32_gpu_fill_open_open(mtgp32_gpu_t *h, float *dev_out, size_t n,
+                              void *stream);
+/* Generic form of the five fills above; kind is an MTGP_KIND_* value. */
+int mtgp32_gpu_fill(mtgp32_gpu_t *h, int kind, void *dev_out, size_t n,
+                    void *stream);
+/* Advance the state by n steps without writing output. */
+int mtgp32_gpu_skip(mtgp32_gpu_t *h, uint64_t n, void *stream);
+
+/* Replaces mtgp32_fast_jump (mtgp32-fast-jump.c:51-79): jump_string is the
+ * polynomial in the reference's hex form (digit k holds coefficients 4k..4k+3,
+ * least significant bit first).  Runs on the GPU. */
+int mtgp32_gpu_fast_jump(mtgp32_gpu_t *h, const char *jump_string,
+                         void *stream);
+/* Same jump with the polynomial in the reference's uint32-array form
+ * (mtgp-calc-jump.hpp:67-91: bit j of word i is the coefficient of
+ * X^(32i+j)), as stored in the jump tables (mtgp32-jump-table.h). */
+int mtgp32_gpu_jump_array(mtgp32_gpu_t *h, const uint32_t *poly, int nwords,
+                          void *stream);
+/* Jump ahead by `steps` outputs (any 128-bit count, given as lo/hi words).
+ * Uses the characteristic polynomial of the handle's parameter set
+ * (computed once per set on the host by Berlekamp-Massey) and an
+ * X^steps mod chi polynomial built on the host. */
+int mtgp32_gpu_jump_steps(mtgp32_gpu_t *h, uint64_t steps_lo,
+                          uint64_t steps_hi, void *stream);
+
+/* Copy the device state into a reference struct whose status was allocated
+ * by the reference (mtgp32_init) for the same parameter set; afterwards the
+ * reference's genrand_* functions continue the sequence exactly.
+ * Synchronous.  State mapping follows mtgp32-fast.h:165-183. */
+int mtgp32_gpu_export(mtgp32_gpu_t *h, mtgp32_fast_t *dst);
+/* Load the state (and parameters) of a reference struct into the handle. */
+int mtgp32_gpu_import(mtgp32_gpu_t *h, const mtgp32_fast_t *src);
+/* Live state window, oldest word first (size words), to / from host memory. */
+int mtgp32_gpu_get_window_host(mtgp32_gpu_t *h, uint32_t *win, int size);
+int mtgp32_gpu_set_window_host(mtgp32_gpu_t *h, const uint32_t *win, int size);
+
+/* 64-bit twins: mtgp64-fast.c:99-142,156-339, mtgp64-fast.h:262-356,
+ * mtgp64-fast-jump.c:51-79. */
+int mtgp64_gpu_init(mtgp64_gpu_t **out, const mtgp64_params_fast_t *para,
+                    uint64_t seed);
+int mtgp64_gpu_init_by_array(mtgp64_gpu_t **out,
+                             const mtgp64_params_fast_t *para,
+                             const uint64_t *array, int length);
+int mtgp64_gpu_init_by_str(mtgp64_gpu_t **out,
+                           const mtgp64_params_fast_t *para, const char *str);
+void mtgp64_gpu_free(mtgp64_gpu_t *h);
+int mtgp64_gpu_fill_uint64(mtgp64_gpu_t *h, uint64_t *dev_out, size_t n,
+                           void *stream);
+int mtgp64_gpu_fill_close1_open2(mtgp64_gpu_t *h, double *dev_out, size_t n,
+                                 void *stream);
+int mtgp64_gpu_fill_close_open(mtgp64_gpu_t *h, double *dev_out, size_t n,
+                               void *stream);
+int mtgp64_gpu_fill_open_close(mtgp64_gpu_t *h, double *dev_out, size_t n,
+                               void *stream);
+int mtgp64_gpu_fill_open_open(mtgp64_gpu_t *h, double *dev_out, size_t n,
+                              void *stream);
+int mtgp64_gpu_fill(mtgp64_gpu_t *h, int kind, void *dev_out, size_t n,
+                    void *stream);
+int mtgp64_gpu_skip(mtgp64_gpu_t *h, uint64_t n, void *stream);
+int mtgp64_gpu_fast_jump(mtgp64_gpu_t *h, const char *jump_string,
+                         void *stream);
+int mtgp64_gpu_jump_array(mtgp64_gpu_t *h, const uint32_t *poly, int nwords,
+                          void *stream);
+int mtgp64_gpu_jump_steps(mtgp64_gpu_t *h, uint64_t steps_lo,
+                          uint64_t steps_hi, void *stream);
+int mtgp64_gpu_export(mtgp64_gpu_t *h, mtgp64_fast_t *dst);
+int mtgp64_gpu_import(mtgp64_gpu_t *h, const mtgp64_fast_t *src);
+int mtgp64_gpu_get_window_host(mtgp64_gpu_t *h, uint64_t *win, int size);
+int mtgp64_gpu_set_window_host(mtgp64_gpu_t *h, const uint64_t *win,
+                               int size);
+
+/* ========================================================================= */
+/* Pools: many device-resident streams (bank, batched and serving paths)      */
+/* ========================================================================= */
+/* A pool holds `count` streams of one Mersenne exponent.  Stream i uses
+ * parameter set params[param_idx ? param_idx[i] : i] and its window stays in
+ * HBM between calls.  The reference has no counterpart object; its CUDA
+ * samples keep the same data in mtgp32_kernel_status_t arrays
+ * (cuda-sample/mtgp32-cuda.cu:43-45) and launch one CTA per generator. */
+typedef struct mtgp32_gpu_pool mtgp32_gpu_pool_t;
+typedef struct mtgp64_gpu_pool mtgp64_gpu_pool_t;
+
+/* One unit of batched work: continue stream `stream` by `count` values of
+ * `kind` (MTGP_KIND_*, or -1 = advance without output), written at byte
+ * offset `out_offset` of the output buffer (a multiple of the value size).
+ * Items naming the same stream are applied in array order. */
+typedef struct mtgp_work_item {
+    uint32_t stream;
+    int32_t kind;
+    uint64_t count;
+    uint64_t out_offset;
+} mtgp_work_item_t;
+
+/* A prepared batch: descriptors uploaded once, launched many times. */
+typedef struct mtgp_gpu_plan mtgp_gpu_plan_t;
+
+/* Seeded pool: stream i = mtgp32_init(params[pidx[i]], seeds[i]). */
+int mtgp32_gpu_pool_create(mtgp32_gpu_pool_t **out,
+                           const mtgp32_params_fast_t *params, int nparams,
+                           const int *param_idx, const uint32_t *seeds,
+                           int count);
+/* Substream pool: stream j = (para, seed) jumped ahead by j * step, where
+ * jump_table row k (nwords words each) is X^(4^k * step) mod chi, the layout
+ * of the reference's jump tables (cuda-sample/mtgp32-jump-table.h:6-13).
+ * count <= 4^rows.  The jumps run on the GPU (mirrors
+ * cuda-sample/mtgp32-jump-kernel.cuh:383-423). */
+int mtgp32_gpu_pool_create_substreams(mtgp32_gpu_pool_t **out,
+                                      const mtgp32_params_fast_t *para,
+                                      uint32_t seed, int count,
+                                      const uint32_t *jump_table, int rows,
+                                      int nwords, void *stream);
+void mtgp32_gpu_pool_free(mtgp32_gpu_pool_t *p);
+int mtgp32_gpu_pool_size(const mtgp32_gpu_pool_t *p);
+/* Plain path, one launch for the whole pool (one CTA per stream): every
+ * stream produces n_per_stream values at dev_out + i * n_per_stream. */
+int mtgp32_gpu_pool_fill(mtgp32_gpu_pool_t *p, int kind, void *dev_out,
+                         size_t n_per_stream, void *stream);
+/* Plain path for one stream (one launch, one CTA). */
+int mtgp32_gpu_pool_fill_stream(mtgp32_gpu_pool_t *p, int s, int kind,
+                                void *dev_out, size_t n, void *stream);
+/* Batched path: all items in one persistent launch. */
+int mtgp32_gpu_pool_submit(mtgp32_gpu_pool_t *p, const mtgp_work_item_t *items,
+                           int nitems, void *dev_out, void *stream);
+int mtgp32_gpu_pool_plan(mtgp32_gpu_pool_t *p, const mtgp_work_item_t *items,
+                         int nitems, mtgp_gpu_plan_t **plan);
+/* Jump stream s by a polynomial (uint32-array form). */
+int mtgp32_gpu_pool_jump_array(mtgp32_gpu_pool_t *p, int s,
+                               const uint32_t *poly, int nwords, void *stream);
+/* All windows, count * size words, stream-major (synchronous). */
+int mtgp32_gpu_pool_get_windows_host(mtgp32_gpu_pool_t *p, uint32_t *win,
+                                     size_t nwords);
+int mtgp32_gpu_pool_set_windows_host(mtgp32_gpu_pool_t *p,
+                                     const uint32_t *win, size_t nwords);
+int mtgp32_gpu_pool_export(mtgp32_gpu_pool_t *p, int s, mtgp32_fast_t *dst);
+
+int mtgp64_gpu_pool_create(mtgp64_gpu_pool_t **out,
+                           const mtgp64_params_fast_t *params, int nparams,
+                           const int *param_idx, const uint64_t *seeds,
+                           int count);
+int mtgp64_gpu_pool_create_substreams(mtgp64_gpu_pool_t **out,
+                                      const mtgp64_params_fast_t *para,
+                                      uint64_t seed, int count,
+                                      const uint32_t *jump_table, int rows,
+                                      int nwords, void *stream);
+void mtgp64_gpu_pool_free(mtgp64_gpu_pool_t *p);
+int mtgp64_gpu_pool_size(const mtgp64_gpu_pool_t *p);
+int mtgp64_gpu_pool_fill(mtgp64_gpu_pool_t *p, int kind, void *dev_out,
+                         size_t n_per_stream, void *stream);
+int mtgp64_gpu_pool_fill_stream(mtgp64_gpu_pool_t *p, int s, int kind,
+                                void *dev_out, size_t n, void *stream);
+int mtgp64_gpu_pool_submit(mtgp64_gpu_pool_t *p, const mtgp_work_item_t *items,
+                           int nitems, void *dev_out, void *stream);
+int mtgp64_gpu_pool_plan(mtgp64_gpu_pool_t *p, const mtgp_work_item_t *items,
+                         int nitems, mtgp_gpu_plan_t **plan);
+int mtgp64_gpu_pool_jump_array(mtgp64_gpu_pool_t *p, int s,
+                               const uint32_t *poly, int nwords, void *stream);
+int mtgp64_gpu_pool_get_windows_host(mtgp64_gpu_pool_t *p, uint64_t *win,
+                                     size_t nwords);
+int mtgp64_gpu_pool_set_windows_host(mtgp64_gpu_pool_t *p,
+                                     const uint64_t *win, size_t nwords);
+int mtgp64_gpu_pool_export(mtgp64_gpu_pool_t *p, int s, mtgp64_fast_t *dst);
+
+/* Launch a prepared batch (one persistent kernel).  Capturable. */
+int mtgp_gpu_plan_launch(mtgp_gpu_plan_t *plan, void *dev_out, void *stream);
+/* Same launch through a CUDA graph, captured on first use for this
+ * dev_out and replayed afterwards. */
+int mtgp_gpu_plan_graph_launch(mtgp_gpu_plan_t *plan, void *dev_out,
+                               void *stream);
+/* Bytes of output the plan writes (max over items of offset + size). */
+uint64_t mtgp_gpu_plan_output_bytes(const mtgp_gpu_plan_t *plan);
+void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
+
+#if defined(__cplusplus)
+}
+#endif
+#endif /* MTGP_GPU_H */

@@ -1,0 +1,264 @@
+"""Python mirror of the reference C API, on the GPU.
+
+Names and argument meanings follow the reference (mtgp32-fast.h:108-130,
+mtgp64-fast.h:107-129, mtgp32-fast-jump.h:25): a generator is created from a
+parameter set and a seed (or a seed array / string), fills return the same
+values as successive genrand_* calls, and fast_jump takes the reference's
+hex jump string.  Device memory and streams come from PyTorch; everything
+else goes through the C ABI of libmtgp_gb300.so.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from ._lib import WorkItem, check, lib
+from .params import MTGP32Params, MTGP64Params
+
+KIND_UINT, KIND_CLOSE1_OPEN2, KIND_CLOSE_OPEN, KIND_OPEN_CLOSE, KIND_OPEN_OPEN = range(5)
+KINDS = {"uint": 0, "close1_open2": 1, "close_open": 2, "open_close": 3, "open_open": 4}
+
+
+def _stream(stream):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _dtype(bits, kind):
+    if bits == 32:
+        return torch.int32 if kind == 0 else torch.float32
+    return torch.int64 if kind == 0 else torch.float64
+
+
+class _Gen:
+    bits = 32
+
+    def __init__(self, params, seed=None, array=None, string=None):
+        L = lib()
+        self._L = L
+        self.pre = "mtgp%d_gpu_" % self.bits
+        self.params = params
+        h = ctypes.c_void_p()
+        if string is not None:
+            if isinstance(string, str):
+                string = string.encode("latin-1")
+            check(getattr(L, self.pre + "init_by_str")(ctypes.byref(h), ctypes.byref(params), string))
+        elif array is not None:
+            a = np.ascontiguousarray(array, dtype=np.uint32 if self.bits == 32 else np.uint64)
+            check(getattr(L, self.pre + "init_by_array")(
+                ctypes.byref(h), ctypes.byref(params), a.ctypes.data_as(ctypes.c_void_p), len(a)))
+        else:
+            check(getattr(L, self.pre + "init")(ctypes.byref(h), ctypes.byref(params),
+                                                0 if seed is None else seed))
+        self.h = h
+        self.size = params.mexp // self.bits + 1
+
+    def close(self):
+        if self.h:
+            getattr(self._L, self.pre + "free")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fill_into(self, kind, out, n=None, stream=None):
+        """Write n values of `kind` into the CUDA tensor `out` (in order)."""
+        n = out.numel() if n is None else n
+        assert out.is_cuda and out.is_contiguous() and out.element_size() * 8 == self.bits
+        check(getattr(self._L, self.pre + "fill")(self.h, kind, ctypes.c_void_p(out.data_ptr()),
+                                                  n, _stream(stream)))
+        return out
+
+    def fill(self, kind, n, device="cuda", stream=None):
+        out = torch.empty(n, dtype=_dtype(self.bits, kind), device=device)
+        return self.fill_into(kind, out, n, stream)
+
+    def skip(self, n, stream=None):
+        check(getattr(self._L, self.pre + "skip")(self.h, n, _stream(stream)))
+
+    def fast_jump(self, jump_string, stream=None):
+        check(getattr(self._L, self.pre + "fast_jump")(self.h, jump_string.encode(), _stream(stream)))
+
+    def jump_array(self, words, stream=None):
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        check(getattr(self._L, self.pre + "jump_array")(self.h, w.ctypes.data_as(ctypes.c_void_p),
+                                                        len(w), _stream(stream)))
+
+    def jump_steps(self, steps, stream=None):
+        check(getattr(self._L, self.pre + "jump_steps")(self.h, steps & (2**64 - 1), steps >> 64,
+                                                        _stream(stream)))
+
+    def window(self):
+        w = np.empty(self.size, dtype=np.uint32 if self.bits == 32 else np.uint64)
+        check(getattr(self._L, self.pre + "get_window_host")(self.h, w.ctypes.data_as(ctypes.c_void_p),
+                                                             self.size))
+        return w
+
+    def set_window(self, win):
+        w = np.ascontiguousarray(win, dtype=np.uint32 if self.bits == 32 else np.uint64)
+        check(getattr(self._L, self.pre + "set_window_host")(self.h, w.ctypes.data_as(ctypes.c_void_p),
+                                                             len(w)))
+
+
+class MTGP32(_Gen):
+    """GPU twin of mtgp32_fast_t (mtgp32-fast.h:86-89)."""
+    bits = 32
+
+    def fill_uint32(self, n, **kw):
+        return self.fill(0, n, **kw)
+
+    def fill_close1_open2(self, n, **kw):
+        return self.fill(1, n, **kw)
+
+    def fill_close_open(self, n, **kw):
+        return self.fill(2, n, **kw)
+
+    def fill_open_close(self, n, **kw):
+        return self.fill(3, n, **kw)
+
+    def fill_open_open(self, n, **kw):
+        return self.fill(4, n, **kw)
+
+
+class MTGP64(_Gen):
+    """GPU twin of mtgp64_fast_t (mtgp64-fast.h:85-88)."""
+    bits = 64
+
+    def fill_uint64(self, n, **kw):
+        return self.fill(0, n, **kw)
+
+    def fill_close1_open2(self, n, **kw):
+        return self.fill(1, n, **kw)
+
+    def fill_close_open(self, n, **kw):
+        return self.fill(2, n, **kw)
+
+    def fill_open_close(self, n, **kw):
+        return self.fill(3, n, **kw)
+
+    def fill_open_open(self, n, **kw):
+        return self.fill(4, n, **kw)
+
+
+class Plan:
+    """A prepared batch (mtgp_gpu_plan_t)."""
+
+    def __init__(self, handle, pool):
+        self.h = handle
+        self.pool = pool  # keep the pool alive
+
+    @property
+    def output_bytes(self):
+        return lib().mtgp_gpu_plan_output_bytes(self.h)
+
+    def launch(self, out, stream=None):
+        check(lib().mtgp_gpu_plan_launch(self.h, ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+
+    def graph_launch(self, out, stream=None):
+        check(lib().mtgp_gpu_plan_graph_launch(self.h, ctypes.c_void_p(out.data_ptr()),
+                                               _stream(stream)))
+
+    def close(self):
+        if self.h:
+            lib().mtgp_gpu_plan_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def work_items(streams, kinds, counts, offsets):
+    n = len(streams)
+    arr = (WorkItem * n)()
+    for k in range(n):
+        arr[k].stream = int(streams[k])
+        arr[k].kind = int(kinds[k])
+        arr[k].count = int(counts[k])
+        arr[k].out_offset = int(offsets[k])
+    return arr
+
+
+class Pool:
+    """Many device-resident streams (mtgp32_gpu_pool_t / mtgp64_gpu_pool_t)."""
+
+    def __init__(self, bits, handle, size_words):
+        self.bits = bits
+        self.pre = "mtgp%d_gpu_pool_" % bits
+        self.h = handle
+        self.size = size_words
+        self.count = getattr(lib(), self.pre + "size")(handle)
+
+    @classmethod
+    def create(cls, params_list, seeds, param_idx=None):
+        bits = 32 if isinstance(params_list[0], MTGP32Params) else 64
+        P = MTGP32Params if bits == 32 else MTGP64Params
+        arr = (P * len(params_list))(*params_list)
+        sd = np.ascontiguousarray(seeds, dtype=np.uint32 if bits == 32 else np.uint64)
+        pidx = None if param_idx is None else np.ascontiguousarray(param_idx, dtype=np.int32)
+        h = ctypes.c_void_p()
+        check(getattr(lib(), "mtgp%d_gpu_pool_create" % bits)(
+            ctypes.byref(h), arr, len(params_list),
+            None if pidx is None else pidx.ctypes.data_as(ctypes.c_void_p),
+            sd.ctypes.data_as(ctypes.c_void_p), len(sd)))
+        return cls(bits, h, params_list[0].mexp // bits + 1)
+
+    @classmethod
+    def substreams(cls, params, seed, count, table, stream=None):
+        bits = 32 if isinstance(params, MTGP32Params) else 64
+        t = np.ascontiguousarray(table, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        check(getattr(lib(), "mtgp%d_gpu_pool_create_substreams" % bits)(
+            ctypes.byref(h), ctypes.byref(params), seed, count,
+            t.ctypes.data_as(ctypes.c_void_p), t.shape[0], t.shape[1], _stream(stream)))
+        return cls(bits, h, params.mexp // bits + 1)
+
+    def close(self):
+        if self.h:
+            getattr(lib(), self.pre + "free")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fill(self, kind, out, n_per_stream, stream=None):
+        check(getattr(lib(), self.pre + "fill")(self.h, kind, ctypes.c_void_p(out.data_ptr()),
+                                                n_per_stream, _stream(stream)))
+
+    def fill_stream(self, s, kind, out, n, stream=None, byte_offset=0):
+        check(getattr(lib(), self.pre + "fill_stream")(
+            self.h, s, kind, ctypes.c_void_p(out.data_ptr() + byte_offset), n, _stream(stream)))
+
+    def plan(self, items):
+        ph = ctypes.c_void_p()
+        check(getattr(lib(), self.pre + "plan")(self.h, items, len(items), ctypes.byref(ph)))
+        return Plan(ph, self)
+
+    def submit(self, items, out, stream=None):
+        check(getattr(lib(), self.pre + "submit")(self.h, items, len(items),
+                                                  ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+
+    def jump_array(self, s, words, stream=None):
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        check(getattr(lib(), self.pre + "jump_array")(self.h, s, w.ctypes.data_as(ctypes.c_void_p),
+                                                      len(w), _stream(stream)))
+
+    def windows(self):
+        w = np.empty(self.count * self.size, dtype=np.uint32 if self.bits == 32 else np.uint64)
+        check(getattr(lib(), self.pre + "get_windows_host")(self.h, w.ctypes.data_as(ctypes.c_void_p),
+                                                            w.size))
+        return w.reshape(self.count, self.size)
+
+    def set_windows(self, win):
+        w = np.ascontiguousarray(win, dtype=np.uint32 if self.bits == 32 else np.uint64).ravel()
+        check(getattr(lib(), self.pre + "set_windows_host")(self.h, w.ctypes.data_as(ctypes.c_void_p),
+                                                            w.size))

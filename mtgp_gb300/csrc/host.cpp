@@ -1,0 +1,965 @@
+// host.cpp -- the C ABI of include/mtgp_gpu.h.
+//
+// Host side of the GB300 MTGP generator: parameter validation, seeding (the
+// reference's exact integer arithmetic, done once per stream on the host as
+// the reference's CUDA samples do, cuda-sample/mtgp32-cuda.cu:304-330),
+// device memory for parameters and state windows, and the launches of the
+// generation, jump and batched kernels.  Everything that produces random
+// numbers runs on the GPU; there is no CPU generation path.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "batch.h"
+#include "gf2.h"
+#include "internal.h"
+
+namespace mtgp {
+
+void toDev(const mtgp32_params_fast_t &p, DevParams32 *d) {
+    std::memset(d, 0, sizeof *d);
+    d->pos = p.pos;
+    d->sh1 = p.sh1;
+    d->sh2 = p.sh2;
+    d->mask = p.mask;
+    std::memcpy(d->tbl, p.tbl, sizeof d->tbl);
+    std::memcpy(d->tmp, p.tmp_tbl, sizeof d->tmp);
+    std::memcpy(d->flt, p.flt_tmp_tbl, sizeof d->flt);
+}
+
+void toDev(const mtgp64_params_fast_t &p, DevParams64 *d) {
+    std::memset(d, 0, sizeof *d);
+    d->pos = p.pos;
+    d->sh1 = p.sh1;
+    d->sh2 = p.sh2;
+    d->mask = p.mask;
+    std::memcpy(d->tbl, p.tbl, sizeof d->tbl);
+    std::memcpy(d->tmp, p.tmp_tbl, sizeof d->tmp);
+    std::memcpy(d->dbl, p.dbl_tmp_tbl, sizeof d->dbl);
+}
+
+}  // namespace mtgp
+
+using namespace mtgp;
+
+namespace {
+
+thread_local std::string g_err;
+
+int setErr(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int cudaErr(cudaError_t e, const char *what) {
+    return setErr(MTGP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cudaErr(e_, what); \
+    } while (0)
+
+inline cudaStream_t S(void *s) { return static_cast<cudaStream_t>(s); }
+
+// ------------------------------------------------------------------------
+// Seeding (host).  Same integer arithmetic as the reference.
+// ------------------------------------------------------------------------
+
+// mtgp32-fast.c:119-137
+void seed32(const mtgp32_params_fast_t &p, uint32_t seed, uint32_t *a) {
+    const int size = p.mexp / 32 + 1;
+    const uint32_t hidden = p.tbl[4] ^ (p.tbl[8] << 16);
+    uint32_t b = hidden;
+    b += b >> 16;
+    b += b >> 8;
+    std::fill(a, a + size, (b & 0xffu) * 0x01010101u);
+    a[0] = seed;
+    a[1] = hidden;
+    for (int i = 1; i < size; i++) a[i] ^= 1812433253u * (a[i - 1] ^ (a[i - 1] >> 30)) + (uint32_t)i;
+}
+
+// mtgp64-fast.c:124-142
+void seed64(const mtgp64_params_fast_t &p, uint64_t seed, uint64_t *a) {
+    const int size = p.mexp / 64 + 1;
+    const uint64_t hidden = p.tbl[4] ^ (p.tbl[8] << 16);
+    uint64_t b = hidden >> 32;
+    b += b >> 16;
+    b += b >> 8;
+    std::fill(a, a + size, (b & 0xffu) * 0x0101010101010101ULL);
+    a[0] = seed;
+    a[1] = hidden;
+    for (int i = 1; i < size; i++)
+        a[i] ^= 6364136223846793005ULL * (a[i - 1] ^ (a[i - 1] >> 62)) + (uint64_t)i;
+}
+
+// Key-schedule seeding shared by init_by_array and init_by_str
+// (mtgp32-fast.c:151-235 / 250-334, mtgp64-fast.c:156-239 / 255-339).
+// `keyAt(j)` returns key word j as the reference adds it: array words
+// directly, string bytes as signed char (the reference's behaviour on
+// x86-64), so results do not depend on the host's char signedness.
+template <typename W, class Key>
+void keyed(W *a, int size, W hidden, int len, Key keyAt, W mul1, W mul2, int shr) {
+    const int lag = size >= 623 ? 11 : size >= 68 ? 7 : size >= 39 ? 5 : 3;
+    const int mid = (size - lag) / 2;
+    W b = (sizeof(W) == 8) ? (hidden >> 32) : hidden;
+    b += b >> 16;
+    b += b >> 8;
+    std::fill(a, a + size, (W)((b & 0xffu) * (W)0x0101010101010101ULL));
+    a[0] = hidden;
+    auto f1 = [&](W x) { return (W)((x ^ (x >> shr)) * mul1); };
+    auto f2 = [&](W x) { return (W)((x ^ (x >> shr)) * mul2); };
+    int total = (len + 1 > size) ? len + 1 : size;
+    W r = f1(a[0] ^ a[mid] ^ a[size - 1]);
+    a[mid] += r;
+    r += (W)len;
+    a[(mid + lag) % size] += r;
+    a[0] = r;
+    total--;
+    int i = 1, j = 0;
+    for (; j < total && j < len; j++) {
+        W t = f1(a[i] ^ a[(i + mid) % size] ^ a[(i + size - 1) % size]);
+        a[(i + mid) % size] += t;
+        t += keyAt(j, i);
+        a[(i + mid + lag) % size] += t;
+        a[i] = t;
+        i = (i + 1) % size;
+    }
+    for (; j < total; j++) {
+        W t = f1(a[i] ^ a[(i + mid) % size] ^ a[(i + size - 1) % size]);
+        a[(i + mid) % size] += t;
+        t += (W)i;
+        a[(i + mid + lag) % size] += t;
+        a[i] = t;
+        i = (i + 1) % size;
+    }
+    for (j = 0; j < size; j++) {
+        W t = f2(a[i] + a[(i + mid) % size] + a[(i + size - 1) % size]);
+        a[(i + mid) % size] ^= t;
+        t -= (W)i;
+        a[(i + mid + lag) % size] ^= t;
+        a[i] = t;
+        i = (i + 1) % size;
+    }
+    if (a[size - 1] == 0) a[size - 1] = (W)0x4d544750u;
+}
+
+// ------------------------------------------------------------------------
+// Traits of the two word sizes.
+// ------------------------------------------------------------------------
+struct T32 {
+    using W = uint32_t;
+    using HP = mtgp32_params_fast_t;
+    using DP = DevParams32;
+    using Fast = mtgp32_fast_t;
+    static constexpr int kBits = 32;
+    static bool shape(int mexp, Shape *s) { return shape32(mexp, s); }
+    static cudaError_t gen(int mexp, int kind, const DP *p, const int *pi, W *st, int ng,
+                           void *out, uint64_t n, uint64_t os, cudaStream_t s) {
+        return launchGen32(mexp, kind, p, pi, st, ng, out, n, os, s);
+    }
+    static cudaError_t jump(int mexp, const DP *p, W *st, const JumpDesc *d, int nd, int nw,
+                            cudaStream_t s) {
+        return launchJump32(mexp, p, st, d, nd, nw, s);
+    }
+    static cudaError_t batch(int mexp, const DP *p, W *st, const BatchTask *t, int nt,
+                             const BatchItem *i, void *out, unsigned *c, int g, cudaStream_t s) {
+        return launchBatch32(mexp, p, st, t, nt, i, out, c, g, s);
+    }
+    static void seed(const HP &p, W s, W *a) { seed32(p, s, a); }
+    static void byArray(const HP &p, const W *key, int len, W *a) {
+        keyed<W>(a, p.mexp / 32 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
+                 [&](int j, int i) { return (W)(key[j] + (W)i); }, 1664525u, 1566083941u, 27);
+    }
+    static void byStr(const HP &p, const char *s, int len, W *a) {
+        keyed<W>(a, p.mexp / 32 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
+                 [&](int j, int i) { return (W)((int)(signed char)s[j] + i); }, 1664525u,
+                 1566083941u, 27);
+    }
+};
+
+struct T64 {
+    using W = uint64_t;
+    using HP = mtgp64_params_fast_t;
+    using DP = DevParams64;
+    using Fast = mtgp64_fast_t;
+    static constexpr int kBits = 64;
+    static bool shape(int mexp, Shape *s) { return shape64(mexp, s); }
+    static cudaError_t gen(int mexp, int kind, const DP *p, const int *pi, W *st, int ng,
+                           void *out, uint64_t n, uint64_t os, cudaStream_t s) {
+        return launchGen64(mexp, kind, p, pi, st, ng, out, n, os, s);
+    }
+    static cudaError_t jump(int mexp, const DP *p, W *st, const JumpDesc *d, int nd, int nw,
+                            cudaStream_t s) {
+        return launchJump64(mexp, p, st, d, nd, nw, s);
+    }
+    static cudaError_t batch(int mexp, const DP *p, W *st, const BatchTask *t, int nt,
+                             const BatchItem *i, void *out, unsigned *c, int g, cudaStream_t s) {
+        return launchBatch64(mexp, p, st, t, nt, i, out, c, g, s);
+    }
+    static void seed(const HP &p, W s, W *a) { seed64(p, s, a); }
+    static void byArray(const HP &p, const W *key, int len, W *a) {
+        keyed<W>(a, p.mexp / 64 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
+                 [&](int j, int i) { return (W)(key[j] + (W)i); }, 2173292883993ULL,
+                 58885565329898161ULL, 59);
+    }
+    static void byStr(const HP &p, const char *s, int len, W *a) {
+        keyed<W>(a, p.mexp / 64 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
+                 [&](int j, int i) { return (W)(int64_t)((int)(signed char)s[j] + i); },
+                 2173292883993ULL, 58885565329898161ULL, 59);
+    }
+};
+
+template <class T>
+int checkParams(const typename T::HP &p, Shape *sh) {
+    if (!T::shape(p.mexp, sh))
+        return setErr(MTGP_ERR_UNSUPPORTED, "mtgp%d: Mersenne exponent %d not supported", T::kBits,
+                      p.mexp);
+    if (p.pos < 1 || p.pos > sh->n - sh->tn)
+        return setErr(MTGP_ERR_UNSUPPORTED,
+                      "mtgp%d: pos %d outside [1, %d] (needs size - pos >= %d lanes)", T::kBits,
+                      p.pos, sh->n - sh->tn, sh->tn);
+    if (p.sh1 < 0 || p.sh1 >= 32 || p.sh2 < 0 || p.sh2 >= 32)
+        return setErr(MTGP_ERR_INVALID, "mtgp%d: shift out of range", T::kBits);
+    return MTGP_OK;
+}
+
+// ------------------------------------------------------------------------
+// Pool: `count` device-resident streams of one Mersenne exponent.
+// ------------------------------------------------------------------------
+template <class T>
+struct Pool {
+    using W = typename T::W;
+    Shape sh{};
+    int count = 0, nparams = 0, stride = 0, size = 0;
+    std::vector<typename T::HP> hparams;
+    std::vector<int> hpidx;
+    typename T::DP *d_params = nullptr;
+    int *d_pidx = nullptr;
+    W *d_states = nullptr;
+    uint32_t *d_poly = nullptr;
+    size_t poly_cap = 0;
+    JumpDesc *d_desc = nullptr;
+    size_t desc_cap = 0;
+    std::vector<gf2::Poly> chi;   // characteristic polynomial per parameter set
+    std::vector<int> chideg;
+
+    ~Pool() {
+        cudaFree(d_params);
+        cudaFree(d_pidx);
+        cudaFree(d_states);
+        cudaFree(d_poly);
+        cudaFree(d_desc);
+    }
+
+    int init(const typename T::HP *params, int np, const int *pidx, int n) {
+        if (!params || np <= 0 || n <= 0) return setErr(MTGP_ERR_INVALID, "empty pool");
+        int rc = checkParams<T>(params[0], &sh);
+        if (rc) return rc;
+        for (int k = 1; k < np; k++) {
+            Shape s2;
+            rc = checkParams<T>(params[k], &s2);
+            if (rc) return rc;
+            if (s2.mexp != sh.mexp)
+                return setErr(MTGP_ERR_INVALID, "pool parameter sets mix exponents %d and %d",
+                              sh.mexp, s2.mexp);
+        }
+        count = n;
+        nparams = np;
+        size = sh.n;
+        stride = stateStride(sh.n);
+        hparams.assign(params, params + np);
+        hpidx.resize(n);
+        for (int i = 0; i < n; i++) {
+            int k = pidx ? pidx[i] : (np == n ? i : 0);
+            if (k < 0 || k >= np) return setErr(MTGP_ERR_INVALID, "param_idx[%d] = %d out of range", i, k);
+            hpidx[i] = k;
+        }
+        std::vector<typename T::DP> dp(np);
+        for (int k = 0; k < np; k++) toDev(params[k], &dp[k]);
+        CK(cudaMalloc(&d_params, sizeof(typename T::DP) * np), "cudaMalloc(params)");
+        CK(cudaMalloc(&d_pidx, sizeof(int) * n), "cudaMalloc(pidx)");
+        CK(cudaMalloc(&d_states, sizeof(W) * (size_t)stride * n), "cudaMalloc(states)");
+        CK(cudaMemcpy(d_params, dp.data(), sizeof(typename T::DP) * np, cudaMemcpyHostToDevice),
+           "upload params");
+        CK(cudaMemcpy(d_pidx, hpidx.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "upload pidx");
+        CK(cudaMemset(d_states, 0, sizeof(W) * (size_t)stride * n), "clear states");
+        chi.assign(np, gf2::Poly());
+        chideg.assign(np, -1);
+        return MTGP_OK;
+    }
+
+    int setWindows(const W *win, size_t nwords) {
+        if (!win || nwords < (size_t)count * size)
+            return setErr(MTGP_ERR_INVALID, "window buffer too small");
+        CK(cudaDeviceSynchronize(), "synchronize");
+        CK(cudaMemcpy2D(d_states, sizeof(W) * stride, win, sizeof(W) * size, sizeof(W) * size,
+                        count, cudaMemcpyHostToDevice),
+           "upload windows");
+        return MTGP_OK;
+    }
+
+    int getWindows(W *win, size_t nwords) {
+        if (!win || nwords < (size_t)count * size)
+            return setErr(MTGP_ERR_INVALID, "window buffer too small");
+        CK(cudaDeviceSynchronize(), "synchronize");
+        CK(cudaMemcpy2D(win, sizeof(W) * size, d_states, sizeof(W) * stride, sizeof(W) * size,
+                        count, cudaMemcpyDeviceToHost),
+           "download windows");
+        return MTGP_OK;
+    }
+
+    int seedAll(const W *seeds) {
+        std::vector<W> win((size_t)count * size);
+        for (int i = 0; i < count; i++) T::seed(hparams[hpidx[i]], seeds[i], &win[(size_t)i * size]);
+        return setWindows(win.data(), win.size());
+    }
+
+    static int checkKind(int kind) {
+        if (kind < 0 || kind > 4) return setErr(MTGP_ERR_INVALID, "unknown output kind %d", kind);
+        return MTGP_OK;
+    }
+
+    int checkOut(const void *out, size_t n) {
+        if (n == 0) return MTGP_OK;
+        if (!out) return setErr(MTGP_ERR_INVALID, "null output pointer");
+        if (reinterpret_cast<uintptr_t>(out) % sizeof(W))
+            return setErr(MTGP_ERR_INVALID, "output pointer not %zu-byte aligned", sizeof(W));
+        return MTGP_OK;
+    }
+
+    int fillAll(int kind, void *out, size_t n, void *s) {
+        int rc = checkKind(kind);
+        if (!rc) rc = checkOut(out, n);
+        if (rc) return rc;
+        CK(T::gen(sh.mexp, kind, d_params, d_pidx, d_states, count, out, n, n, S(s)), "generate");
+        return MTGP_OK;
+    }
+
+    int fillOne(int i, int kind, void *out, size_t n, void *s) {
+        if (i < 0 || i >= count) return setErr(MTGP_ERR_INVALID, "stream %d out of range", i);
+        int rc = kind == -1 ? MTGP_OK : checkKind(kind);
+        if (!rc && kind >= 0) rc = checkOut(out, n);
+        if (rc) return rc;
+        CK(T::gen(sh.mexp, kind, d_params, d_pidx + i, d_states + (size_t)i * stride, 1, out, n, n,
+                  S(s)),
+           "generate");
+        return MTGP_OK;
+    }
+
+    int maxPolyWords() const { return 2 * (sh.mexp / 32 + 1); }
+
+    int ensureScratch(size_t words, size_t descs) {
+        if (words > poly_cap) {
+            cudaFree(d_poly);
+            d_poly = nullptr;
+            CK(cudaMalloc(&d_poly, sizeof(uint32_t) * words), "cudaMalloc(poly)");
+            poly_cap = words;
+        }
+        if (descs > desc_cap) {
+            cudaFree(d_desc);
+            d_desc = nullptr;
+            CK(cudaMalloc(&d_desc, sizeof(JumpDesc) * descs), "cudaMalloc(jump descriptors)");
+            desc_cap = descs;
+        }
+        return MTGP_OK;
+    }
+
+    // Jump stream i by one polynomial (uint32-array form).
+    int jumpArray(int i, const uint32_t *poly, int nwords, void *s) {
+        if (i < 0 || i >= count) return setErr(MTGP_ERR_INVALID, "stream %d out of range", i);
+        if (!poly || nwords <= 0) return setErr(MTGP_ERR_BAD_JUMP, "empty jump polynomial");
+        while (nwords > 1 && poly[nwords - 1] == 0) nwords--;
+        if (nwords > maxPolyWords())
+            return setErr(MTGP_ERR_BAD_JUMP, "jump polynomial of %d words exceeds %d", nwords,
+                          maxPolyWords());
+        int rc = ensureScratch((size_t)nwords, 1);
+        if (rc) return rc;
+        // The scratch buffers are reused: order this call after earlier ones.
+        CK(cudaStreamSynchronize(S(s)), "synchronize");
+        CK(cudaMemcpy(d_poly, poly, sizeof(uint32_t) * nwords, cudaMemcpyHostToDevice),
+           "upload polynomial");
+        JumpDesc d{};
+        d.poly[0] = d_poly;
+        d.nchain = 1;
+        d.pidx = hpidx[i];
+        d.src = d.dst = (uint64_t)i * stride;
+        CK(cudaMemcpy(d_desc, &d, sizeof d, cudaMemcpyHostToDevice), "upload descriptor");
+        CK(T::jump(sh.mexp, d_params, d_states, d_desc, 1, nwords, S(s)), "jump");
+        return MTGP_OK;
+    }
+
+    int fastJump(int i, const char *hex, void *s) {
+        if (!hex) return setErr(MTGP_ERR_BAD_JUMP, "null jump string");
+        gf2::Poly p;
+        int ncoef = 0;
+        if (!gf2::fromHex(hex, &p, &ncoef))
+            return setErr(MTGP_ERR_BAD_JUMP, "jump string has a non-hex character");
+        int nw = std::max(1, (ncoef + 31) / 32);
+        std::vector<uint32_t> w = gf2::toWords32(p, nw);
+        return jumpArray(i, w.data(), nw, s);
+    }
+
+    // Characteristic polynomial of parameter set k: Berlekamp-Massey over
+    // the LSBs of 2*mexp outputs (mtgp32-calc-poly.cpp:36-45), which are
+    // generated on the GPU from a throw-away stream.
+    int characteristic(int k) {
+        if (chideg[k] >= 0) return MTGP_OK;
+        Pool<T> tmp;
+        int rc = tmp.init(&hparams[k], 1, nullptr, 1);
+        if (rc) return rc;
+        W one = 1;
+        rc = tmp.seedAll(&one);
+        if (rc) return rc;
+        const size_t n = 2 * (size_t)sh.mexp;
+        W *d_out = nullptr;
+        CK(cudaMalloc(&d_out, sizeof(W) * n), "cudaMalloc(bm)");
+        rc = tmp.fillAll(0, d_out, n, nullptr);
+        std::vector<W> h(n);
+        cudaError_t e = cudaMemcpy(h.data(), d_out, sizeof(W) * n, cudaMemcpyDeviceToHost);
+        cudaFree(d_out);
+        if (rc) return rc;
+        if (e != cudaSuccess) return cudaErr(e, "download bm sequence");
+        std::vector<uint8_t> bits(n);
+        for (size_t j = 0; j < n; j++) bits[j] = (uint8_t)(h[j] & 1u);
+        gf2::Poly c;
+        int d = gf2::minpoly(bits, &c);
+        if (d != sh.mexp)
+            return setErr(MTGP_ERR_UNSUPPORTED, "characteristic polynomial has degree %d, not %d", d,
+                          sh.mexp);
+        chi[k] = c;
+        chideg[k] = d;
+        return MTGP_OK;
+    }
+
+    int jumpSteps(int i, uint64_t lo, uint64_t hi, void *s) {
+        if (i < 0 || i >= count) return setErr(MTGP_ERR_INVALID, "stream %d out of range", i);
+        if (lo == 0 && hi == 0) return MTGP_OK;
+        int k = hpidx[i];
+        int rc = characteristic(k);
+        if (rc) return rc;
+        std::vector<uint32_t> e = {(uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi,
+                                   (uint32_t)(hi >> 32)};
+        gf2::Poly p = gf2::powxmod(e, chi[k], chideg[k]);
+        int nw = chideg[k] / 32 + 1;
+        std::vector<uint32_t> w = gf2::toWords32(p, nw);
+        return jumpArray(i, w.data(), nw, s);
+    }
+
+    // Substream j = stream 0's window jumped by j * step (table rows as in
+    // cuda-sample/mtgp32-jump-kernel.cuh:383-401: bit b of j applies row
+    // b/2 once for even b, twice for odd b).
+    int substreams(const uint32_t *table, int rows, int nwords, void *s) {
+        if (!table || rows <= 0 || nwords <= 0 || nwords > maxPolyWords())
+            return setErr(MTGP_ERR_BAD_JUMP, "bad jump table");
+        if (rows < 16 && (uint64_t)count > (1ULL << (2 * rows)))
+            return setErr(MTGP_ERR_INVALID, "%d substreams need more than %d table rows", count,
+                          rows);
+        int rc = ensureScratch((size_t)rows * nwords, (size_t)count);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(S(s)), "synchronize");
+        CK(cudaMemcpy(d_poly, table, sizeof(uint32_t) * rows * nwords, cudaMemcpyHostToDevice),
+           "upload jump table");
+        std::vector<JumpDesc> descs;
+        descs.reserve(count);
+        for (int j = 1; j < count; j++) {
+            JumpDesc d{};
+            for (int b = 0; b < 31; b++) {
+                if (!((j >> b) & 1)) continue;
+                const uint32_t *row = d_poly + (size_t)(b / 2) * nwords;
+                d.poly[d.nchain++] = row;
+                if (b & 1) d.poly[d.nchain++] = row;
+            }
+            d.pidx = hpidx[j];
+            d.src = d.dst = (uint64_t)j * stride;
+            descs.push_back(d);
+        }
+        if (descs.empty()) return MTGP_OK;
+        CK(cudaMemcpy(d_desc, descs.data(), sizeof(JumpDesc) * descs.size(),
+                      cudaMemcpyHostToDevice),
+           "upload descriptors");
+        CK(T::jump(sh.mexp, d_params, d_states, d_desc, (int)descs.size(), nwords, S(s)), "jump");
+        return MTGP_OK;
+    }
+
+    int exportTo(int i, typename T::Fast *dst) {
+        if (i < 0 || i >= count) return setErr(MTGP_ERR_INVALID, "stream %d out of range", i);
+        if (!dst || !dst->status) return setErr(MTGP_ERR_INVALID, "destination has no status");
+        const typename T::HP &p = hparams[hpidx[i]];
+        int ls = 1;
+        while (ls <= size) ls <<= 1;
+        if (dst->status->size != size || dst->status->large_size != ls)
+            return setErr(MTGP_ERR_INVALID,
+                          "destination status has size %d / large_size %d, expected %d / %d",
+                          dst->status->size, dst->status->large_size, size, ls);
+        CK(cudaDeviceSynchronize(), "synchronize");
+        CK(cudaMemcpy(dst->status->array, d_states + (size_t)i * stride, sizeof(W) * size,
+                      cudaMemcpyDeviceToHost),
+           "download window");
+        dst->params = p;
+        dst->status->idx = size - 1;
+        dst->status->large_mask = ls - 1;
+        return MTGP_OK;
+    }
+};
+
+}  // namespace
+
+// ==========================================================================
+// Public structs
+// ==========================================================================
+struct mtgp32_gpu { Pool<T32> pool; };
+struct mtgp64_gpu { Pool<T64> pool; };
+struct mtgp32_gpu_pool { Pool<T32> pool; };
+struct mtgp64_gpu_pool { Pool<T64> pool; };
+
+struct mtgp_gpu_plan {
+    int bits = 32;
+    void *pool = nullptr;  // Pool<T32> or Pool<T64>
+    BatchTask *d_tasks = nullptr;
+    BatchItem *d_items = nullptr;
+    unsigned *d_counter = nullptr;
+    int ntasks = 0;
+    uint64_t out_bytes = 0;
+    int grid = 0;
+    cudaGraphExec_t exec = nullptr;
+    void *graph_out = nullptr;
+    ~mtgp_gpu_plan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaFree(d_tasks);
+        cudaFree(d_items);
+        cudaFree(d_counter);
+    }
+};
+
+namespace {
+
+template <class T>
+int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_plan **out) {
+    using W = typename T::W;
+    if (!out) return setErr(MTGP_ERR_INVALID, "null plan pointer");
+    *out = nullptr;
+    if (nitems < 0 || (nitems > 0 && !items)) return setErr(MTGP_ERR_INVALID, "bad item list");
+    // group by stream, keeping the caller's order within a stream
+    std::vector<std::vector<int>> by(P.count);
+    uint64_t out_bytes = 0;
+    for (int k = 0; k < nitems; k++) {
+        const mtgp_work_item_t &it = items[k];
+        if (it.stream >= (uint32_t)P.count)
+            return setErr(MTGP_ERR_INVALID, "item %d: stream %u out of range", k, it.stream);
+        if (it.kind < -1 || it.kind > 4)
+            return setErr(MTGP_ERR_INVALID, "item %d: unknown kind %d", k, it.kind);
+        if (it.kind >= 0 && it.out_offset % sizeof(W))
+            return setErr(MTGP_ERR_INVALID, "item %d: offset not a multiple of %zu", k, sizeof(W));
+        if (it.count == 0) continue;
+        by[it.stream].push_back(k);
+        if (it.kind >= 0) out_bytes = std::max(out_bytes, it.out_offset + it.count * sizeof(W));
+    }
+    struct Tk { int stream; uint64_t total; };
+    std::vector<Tk> order;
+    for (int s = 0; s < P.count; s++) {
+        if (by[s].empty()) continue;
+        uint64_t tot = 0;
+        for (int k : by[s]) tot += items[k].count;
+        order.push_back({s, tot});
+    }
+    // longest task first
+    std::stable_sort(order.begin(), order.end(), [](const Tk &a, const Tk &b) { return a.total > b.total; });
+    std::vector<BatchTask> tasks;
+    std::vector<BatchItem> bitems;
+    for (const Tk &t : order) {
+        BatchTask bt{};
+        bt.stream = t.stream;
+        bt.first = (int)bitems.size();
+        bt.nitems = (int)by[t.stream].size();
+        bt.pidx = P.hpidx[t.stream];
+        for (int k : by[t.stream]) {
+            BatchItem bi{};
+            bi.out_off = items[k].out_offset;
+            bi.count = items[k].count;
+            bi.kind = items[k].kind;
+            bitems.push_back(bi);
+        }
+        tasks.push_back(bt);
+    }
+    mtgp_gpu_plan *pl = new (std::nothrow) mtgp_gpu_plan();
+    if (!pl) return setErr(MTGP_ERR_ALLOC, "plan allocation");
+    pl->bits = T::kBits;
+    pl->pool = &P;
+    pl->ntasks = (int)tasks.size();
+    pl->out_bytes = out_bytes;
+    cudaError_t e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
+    if (e == cudaSuccess && !tasks.empty()) e = cudaMalloc(&pl->d_tasks, sizeof(BatchTask) * tasks.size());
+    if (e == cudaSuccess && !bitems.empty()) e = cudaMalloc(&pl->d_items, sizeof(BatchItem) * bitems.size());
+    if (e == cudaSuccess && !tasks.empty())
+        e = cudaMemcpy(pl->d_tasks, tasks.data(), sizeof(BatchTask) * tasks.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !bitems.empty())
+        e = cudaMemcpy(pl->d_items, bitems.data(), sizeof(BatchItem) * bitems.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        delete pl;
+        return cudaErr(e, "upload plan");
+    }
+    *out = pl;
+    return MTGP_OK;
+}
+
+template <class T>
+int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
+    Pool<T> &P = *static_cast<Pool<T> *>(pl->pool);
+    if (pl->ntasks == 0) return MTGP_OK;
+    if (pl->out_bytes && !out) return setErr(MTGP_ERR_INVALID, "null output pointer");
+    CK(T::batch(P.sh.mexp, P.d_params, P.d_states, pl->d_tasks, pl->ntasks, pl->d_items, out,
+                pl->d_counter, pl->grid, S(s)),
+       "batched launch");
+    return MTGP_OK;
+}
+
+int planLaunch(mtgp_gpu_plan *pl, void *out, void *s) {
+    return pl->bits == 32 ? launchPlan<T32>(pl, out, s) : launchPlan<T64>(pl, out, s);
+}
+
+template <class Obj>
+int newObj(Obj **out) {
+    if (!out) return setErr(MTGP_ERR_INVALID, "null output handle pointer");
+    *out = new (std::nothrow) Obj();
+    if (!*out) return setErr(MTGP_ERR_ALLOC, "host allocation failed");
+    return MTGP_OK;
+}
+
+template <class T, class Obj>
+int initSingle(Obj **out, const typename T::HP *para, const typename T::W *win) {
+    int rc = newObj(out);
+    if (rc) return rc;
+    if (!para) {
+        delete *out;
+        *out = nullptr;
+        return setErr(MTGP_ERR_INVALID, "null parameter set");
+    }
+    rc = (*out)->pool.init(para, 1, nullptr, 1);
+    if (!rc) rc = (*out)->pool.setWindows(win, (*out)->pool.size);
+    if (rc) {
+        delete *out;
+        *out = nullptr;
+    }
+    return rc;
+}
+
+template <class T, class Obj>
+int importSingle(Obj *h, const typename T::Fast *src) {
+    using W = typename T::W;
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    if (!src || !src->status) return setErr(MTGP_ERR_INVALID, "source has no status");
+    Shape sh;
+    int rc = checkParams<T>(src->params, &sh);
+    if (rc) return rc;
+    if (sh.mexp != h->pool.sh.mexp)
+        return setErr(MTGP_ERR_INVALID, "source exponent %d differs from handle's %d", sh.mexp,
+                      h->pool.sh.mexp);
+    const int size = h->pool.size;
+    int ls = src->status->large_size, idx = src->status->idx;
+    if (src->status->size != size || ls <= size || (ls & (ls - 1)))
+        return setErr(MTGP_ERR_INVALID, "source status has unexpected sizes");
+    std::vector<W> win(size);
+    for (int k = 0; k < size; k++) win[k] = src->status->array[(idx - size + 1 + k + ls) & (ls - 1)];
+    typename T::DP dp;
+    toDev(src->params, &dp);
+    CK(cudaDeviceSynchronize(), "synchronize");
+    CK(cudaMemcpy(h->pool.d_params, &dp, sizeof dp, cudaMemcpyHostToDevice), "upload params");
+    h->pool.hparams[0] = src->params;
+    h->pool.chideg[0] = -1;
+    return h->pool.setWindows(win.data(), win.size());
+}
+
+}  // namespace
+
+// ==========================================================================
+// C ABI
+// ==========================================================================
+extern "C" {
+
+const char *mtgp_gpu_last_error(void) { return g_err.c_str(); }
+const char *mtgp_gpu_version(void) { return "mtgp-gb300 0.1 (sm_103a)"; }
+
+// ---- single generator, 32-bit -------------------------------------------
+int mtgp32_gpu_init(mtgp32_gpu_t **out, const mtgp32_params_fast_t *para, uint32_t seed) {
+    if (!para) return setErr(MTGP_ERR_INVALID, "null parameter set");
+    Shape sh;
+    int rc = checkParams<T32>(*para, &sh);
+    if (rc) return rc;
+    std::vector<uint32_t> w(sh.n);
+    T32::seed(*para, seed, w.data());
+    return initSingle<T32>(out, para, w.data());
+}
+int mtgp32_gpu_init_by_array(mtgp32_gpu_t **out, const mtgp32_params_fast_t *para,
+                             const uint32_t *array, int length) {
+    if (!para || length < 0 || (length > 0 && !array))
+        return setErr(MTGP_ERR_INVALID, "bad seed array");
+    Shape sh;
+    int rc = checkParams<T32>(*para, &sh);
+    if (rc) return rc;
+    std::vector<uint32_t> w(sh.n);
+    T32::byArray(*para, array, length, w.data());
+    return initSingle<T32>(out, para, w.data());
+}
+int mtgp32_gpu_init_by_str(mtgp32_gpu_t **out, const mtgp32_params_fast_t *para, const char *str) {
+    if (!para || !str) return setErr(MTGP_ERR_INVALID, "bad seed string");
+    Shape sh;
+    int rc = checkParams<T32>(*para, &sh);
+    if (rc) return rc;
+    std::vector<uint32_t> w(sh.n);
+    T32::byStr(*para, str, (int)std::strlen(str), w.data());
+    return initSingle<T32>(out, para, w.data());
+}
+void mtgp32_gpu_free(mtgp32_gpu_t *h) {
+    if (!h) return;
+    cudaDeviceSynchronize();
+    delete h;
+}
+int mtgp32_gpu_fill(mtgp32_gpu_t *h, int kind, void *out, size_t n, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.fillAll(kind, out, n, s);
+}
+int mtgp32_gpu_fill_uint32(mtgp32_gpu_t *h, uint32_t *o, size_t n, void *s) { return mtgp32_gpu_fill(h, 0, o, n, s); }
+int mtgp32_gpu_fill_close1_open2(mtgp32_gpu_t *h, float *o, size_t n, void *s) { return mtgp32_gpu_fill(h, 1, o, n, s); }
+int mtgp32_gpu_fill_close_open(mtgp32_gpu_t *h, float *o, size_t n, void *s) { return mtgp32_gpu_fill(h, 2, o, n, s); }
+int mtgp32_gpu_fill_open_close(mtgp32_gpu_t *h, float *o, size_t n, void *s) { return mtgp32_gpu_fill(h, 3, o, n, s); }
+int mtgp32_gpu_fill_open_open(mtgp32_gpu_t *h, float *o, size_t n, void *s) { return mtgp32_gpu_fill(h, 4, o, n, s); }
+int mtgp32_gpu_skip(mtgp32_gpu_t *h, uint64_t n, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.fillOne(0, -1, nullptr, n, s);
+}
+int mtgp32_gpu_fast_jump(mtgp32_gpu_t *h, const char *js, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.fastJump(0, js, s);
+}
+int mtgp32_gpu_jump_array(mtgp32_gpu_t *h, const uint32_t *p, int nw, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.jumpArray(0, p, nw, s);
+}
+int mtgp32_gpu_jump_steps(mtgp32_gpu_t *h, uint64_t lo, uint64_t hi, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.jumpSteps(0, lo, hi, s);
+}
+int mtgp32_gpu_export(mtgp32_gpu_t *h, mtgp32_fast_t *dst) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.exportTo(0, dst);
+}
+int mtgp32_gpu_import(mtgp32_gpu_t *h, const mtgp32_fast_t *src) { return importSingle<T32>(h, src); }
+int mtgp32_gpu_get_window_host(mtgp32_gpu_t *h, uint32_t *w, int size) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.getWindows(w, size < 0 ? 0 : (size_t)size);
+}
+int mtgp32_gpu_set_window_host(mtgp32_gpu_t *h, const uint32_t *w, int size) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.setWindows(w, size < 0 ? 0 : (size_t)size);
+}
+
+// ---- single generator, 64-bit -------------------------------------------
+int mtgp64_gpu_init(mtgp64_gpu_t **out, const mtgp64_params_fast_t *para, uint64_t seed) {
+    if (!para) return setErr(MTGP_ERR_INVALID, "null parameter set");
+    Shape sh;
+    int rc = checkParams<T64>(*para, &sh);
+    if (rc) return rc;
+    std::vector<uint64_t> w(sh.n);
+    T64::seed(*para, seed, w.data());
+    return initSingle<T64>(out, para, w.data());
+}
+int mtgp64_gpu_init_by_array(mtgp64_gpu_t **out, const mtgp64_params_fast_t *para,
+                             const uint64_t *array, int length) {
+    if (!para || length < 0 || (length > 0 && !array))
+        return setErr(MTGP_ERR_INVALID, "bad seed array");
+    Shape sh;
+    int rc = checkParams<T64>(*para, &sh);
+    if (rc) return rc;
+    std::vector<uint64_t> w(sh.n);
+    T64::byArray(*para, array, length, w.data());
+    return initSingle<T64>(out, para, w.data());
+}
+int mtgp64_gpu_init_by_str(mtgp64_gpu_t **out, const mtgp64_params_fast_t *para, const char *str) {
+    if (!para || !str) return setErr(MTGP_ERR_INVALID, "bad seed string");
+    Shape sh;
+    int rc = checkParams<T64>(*para, &sh);
+    if (rc) return rc;
+    std::vector<uint64_t> w(sh.n);
+    T64::byStr(*para, str, (int)std::strlen(str), w.data());
+    return initSingle<T64>(out, para, w.data());
+}
+void mtgp64_gpu_free(mtgp64_gpu_t *h) {
+    if (!h) return;
+    cudaDeviceSynchronize();
+    delete h;
+}
+int mtgp64_gpu_fill(mtgp64_gpu_t *h, int kind, void *out, size_t n, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.fillAll(kind, out, n, s);
+}
+int mtgp64_gpu_fill_uint64(mtgp64_gpu_t *h, uint64_t *o, size_t n, void *s) { return mtgp64_gpu_fill(h, 0, o, n, s); }
+int mtgp64_gpu_fill_close1_open2(mtgp64_gpu_t *h, double *o, size_t n, void *s) { return mtgp64_gpu_fill(h, 1, o, n, s); }
+int mtgp64_gpu_fill_close_open(mtgp64_gpu_t *h, double *o, size_t n, void *s) { return mtgp64_gpu_fill(h, 2, o, n, s); }
+int mtgp64_gpu_fill_open_close(mtgp64_gpu_t *h, double *o, size_t n, void *s) { return mtgp64_gpu_fill(h, 3, o, n, s); }
+int mtgp64_gpu_fill_open_open(mtgp64_gpu_t *h, double *o, size_t n, void *s) { return mtgp64_gpu_fill(h, 4, o, n, s); }
+int mtgp64_gpu_skip(mtgp64_gpu_t *h, uint64_t n, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.fillOne(0, -1, nullptr, n, s);
+}
+int mtgp64_gpu_fast_jump(mtgp64_gpu_t *h, const char *js, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.fastJump(0, js, s);
+}
+int mtgp64_gpu_jump_array(mtgp64_gpu_t *h, const uint32_t *p, int nw, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.jumpArray(0, p, nw, s);
+}
+int mtgp64_gpu_jump_steps(mtgp64_gpu_t *h, uint64_t lo, uint64_t hi, void *s) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.jumpSteps(0, lo, hi, s);
+}
+int mtgp64_gpu_export(mtgp64_gpu_t *h, mtgp64_fast_t *dst) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.exportTo(0, dst);
+}
+int mtgp64_gpu_import(mtgp64_gpu_t *h, const mtgp64_fast_t *src) { return importSingle<T64>(h, src); }
+int mtgp64_gpu_get_window_host(mtgp64_gpu_t *h, uint64_t *w, int size) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.getWindows(w, size < 0 ? 0 : (size_t)size);
+}
+int mtgp64_gpu_set_window_host(mtgp64_gpu_t *h, const uint64_t *w, int size) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
+    return h->pool.setWindows(w, size < 0 ? 0 : (size_t)size);
+}
+
+// ---- pools ----------------------------------------------------------------
+#define POOL_API(B, W)                                                                           \
+    int mtgp##B##_gpu_pool_create(mtgp##B##_gpu_pool_t **out, const mtgp##B##_params_fast_t *p, \
+                                  int np, const int *pidx, const W *seeds, int count) {          \
+        if (!seeds) return setErr(MTGP_ERR_INVALID, "null seeds");                              \
+        int rc = newObj(out);                                                                    \
+        if (!rc) rc = (*out)->pool.init(p, np, pidx, count);                                     \
+        if (!rc) rc = (*out)->pool.seedAll(seeds);                                               \
+        if (rc && out && *out) {                                                                 \
+            delete *out;                                                                         \
+            *out = nullptr;                                                                      \
+        }                                                                                        \
+        return rc;                                                                               \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_create_substreams(mtgp##B##_gpu_pool_t **out,                         \
+                                             const mtgp##B##_params_fast_t *p, W seed,           \
+                                             int count, const uint32_t *table, int rows,         \
+                                             int nwords, void *s) {                              \
+        int rc = newObj(out);                                                                    \
+        if (!rc) rc = (*out)->pool.init(p, 1, nullptr, count);                                   \
+        if (!rc) {                                                                               \
+            std::vector<W> seeds((size_t)count, seed);                                           \
+            rc = (*out)->pool.seedAll(seeds.data());                                             \
+        }                                                                                        \
+        if (!rc) rc = (*out)->pool.substreams(table, rows, nwords, s);                           \
+        if (rc && out && *out) {                                                                 \
+            delete *out;                                                                         \
+            *out = nullptr;                                                                      \
+        }                                                                                        \
+        return rc;                                                                               \
+    }                                                                                            \
+    void mtgp##B##_gpu_pool_free(mtgp##B##_gpu_pool_t *p) {                                      \
+        if (!p) return;                                                                          \
+        cudaDeviceSynchronize();                                                                 \
+        delete p;                                                                                \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_size(const mtgp##B##_gpu_pool_t *p) { return p ? p->pool.count : 0; } \
+    int mtgp##B##_gpu_pool_fill(mtgp##B##_gpu_pool_t *p, int kind, void *out, size_t n,          \
+                                void *s) {                                                       \
+        if (!p) return setErr(MTGP_ERR_INVALID, "null pool");                                   \
+        return p->pool.fillAll(kind, out, n, s);                                                 \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_fill_stream(mtgp##B##_gpu_pool_t *p, int i, int kind, void *out,      \
+                                       size_t n, void *s) {                                      \
+        if (!p) return setErr(MTGP_ERR_INVALID, "null pool");                                   \
+        if (kind < 0 || kind > 4) return setErr(MTGP_ERR_INVALID, "unknown kind %d", kind);     \
+        return p->pool.fillOne(i, kind, out, n, s);                                              \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_plan(mtgp##B##_gpu_pool_t *p, const mtgp_work_item_t *items,          \
+                                int nitems, mtgp_gpu_plan_t **plan) {                            \
+        if (!p) return setErr(MTGP_ERR_INVALID, "null pool");                                   \
+        return makePlan(p->pool, items, nitems, plan);                                           \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_submit(mtgp##B##_gpu_pool_t *p, const mtgp_work_item_t *items,        \
+                                  int nitems, void *out, void *s) {                              \
+        mtgp_gpu_plan_t *pl = nullptr;                                                           \
+        int rc = mtgp##B##_gpu_pool_plan(p, items, nitems, &pl);                                 \
+        if (rc) return rc;                                                                       \
+        rc = planLaunch(pl, out, s);                                                             \
+        cudaError_t e = cudaStreamSynchronize(S(s));                                             \
+        delete pl;                                                                               \
+        if (!rc && e != cudaSuccess) rc = cudaErr(e, "batched launch");                          \
+        return rc;                                                                               \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_jump_array(mtgp##B##_gpu_pool_t *p, int i, const uint32_t *poly,      \
+                                      int nw, void *s) {                                         \
+        if (!p) return setErr(MTGP_ERR_INVALID, "null pool");                                   \
+        return p->pool.jumpArray(i, poly, nw, s);                                                \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_get_windows_host(mtgp##B##_gpu_pool_t *p, W *w, size_t n) {           \
+        if (!p) return setErr(MTGP_ERR_INVALID, "null pool");                                   \
+        return p->pool.getWindows(w, n);                                                         \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_set_windows_host(mtgp##B##_gpu_pool_t *p, const W *w, size_t n) {     \
+        if (!p) return setErr(MTGP_ERR_INVALID, "null pool");                                   \
+        return p->pool.setWindows(w, n);                                                         \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_export(mtgp##B##_gpu_pool_t *p, int i, mtgp##B##_fast_t *dst) {       \
+        if (!p) return setErr(MTGP_ERR_INVALID, "null pool");                                   \
+        return p->pool.exportTo(i, dst);                                                         \
+    }
+
+POOL_API(32, uint32_t)
+POOL_API(64, uint64_t)
+
+int mtgp_gpu_plan_launch(mtgp_gpu_plan_t *pl, void *out, void *s) {
+    if (!pl) return setErr(MTGP_ERR_INVALID, "null plan");
+    return planLaunch(pl, out, s);
+}
+
+int mtgp_gpu_plan_graph_launch(mtgp_gpu_plan_t *pl, void *out, void *s) {
+    if (!pl) return setErr(MTGP_ERR_INVALID, "null plan");
+    if (!s) return setErr(MTGP_ERR_INVALID, "graph launch needs a non-default stream");
+    if (!pl->exec || pl->graph_out != out) {
+        if (pl->exec) {
+            cudaGraphExecDestroy(pl->exec);
+            pl->exec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(S(s), cudaStreamCaptureModeThreadLocal), "begin capture");
+        int rc = planLaunch(pl, out, s);
+        cudaError_t e = cudaStreamEndCapture(S(s), &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return cudaErr(e, "end capture");
+        e = cudaGraphInstantiate(&pl->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cudaErr(e, "instantiate graph");
+        pl->graph_out = out;
+    }
+    CK(cudaGraphLaunch(pl->exec, S(s)), "graph launch");
+    return MTGP_OK;
+}
+
+uint64_t mtgp_gpu_plan_output_bytes(const mtgp_gpu_plan_t *pl) { return pl ? pl->out_bytes : 0; }
+
+void mtgp_gpu_plan_free(mtgp_gpu_plan_t *pl) {
+    if (!pl) return;
+    cudaDeviceSynchronize();
+    delete pl;
+}
+
+}  // extern "C"

@@ -1,0 +1,89 @@
+// internal.h -- declarations shared by the host (C-ABI) and kernel units.
+//
+// Device data layout (all in HBM):
+//   DevParams32 / DevParams64  one per parameter set: pos, shifts, mask and
+//                              the three 16-entry tables (recursion, temper,
+//                              float temper) of mtgp32-fast.h:47-58 /
+//                              mtgp64-fast.h:46-57.
+//   state window               one per generator: the live state, oldest word
+//                              first, `size` = mexp/w + 1 words, padded to a
+//                              stride of stateStride() words (a multiple of
+//                              32 words, so every window starts 128-byte
+//                              aligned).  Word k of the window is the
+//                              reference's array[(idx - size + 1 + k) &
+//                              large_mask] (mtgp32-fast.h:165-183).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mtgp_gpu.h"
+
+namespace mtgp {
+
+struct DevParams32 {
+    int pos, sh1, sh2;
+    uint32_t mask;
+    uint32_t tbl[16];
+    uint32_t tmp[16];
+    uint32_t flt[16];
+};
+
+struct DevParams64 {
+    int pos, sh1, sh2, pad_;
+    uint64_t mask;
+    uint64_t tbl[16];
+    uint64_t tmp[16];
+    uint64_t dbl[16];
+};
+
+// Shape of one supported Mersenne exponent: N live words, TN parallel lanes
+// (threads per generator; the reference guarantees size - pos > TN,
+// mtgp32-fast.h:96-106), RING = shared-memory ring length (power of two,
+// >= N + TN so one sub-step's reads and writes never alias).
+struct Shape {
+    int mexp, n, tn, ring;
+};
+
+bool shape32(int mexp, Shape *s);
+bool shape64(int mexp, Shape *s);
+__host__ __device__ constexpr int stateStride(int n) { return (n + 31) & ~31; }
+
+void toDev(const mtgp32_params_fast_t &p, DevParams32 *d);
+void toDev(const mtgp64_params_fast_t &p, DevParams64 *d);
+
+// ---- generation (gen_kernels.cu) ----------------------------------------
+// ngen generators, generator g uses params[pidx ? pidx[g] : g] (device
+// arrays), its window at states + g*stateStride(N), and writes n values of
+// `kind` at out + g*outStride elements.  kind < 0 = skip (no output).
+cudaError_t launchGen32(int mexp, int kind, const DevParams32 *params,
+                        const int *pidx, uint32_t *states, int ngen,
+                        void *out, uint64_t n, uint64_t outStride,
+                        cudaStream_t s);
+cudaError_t launchGen64(int mexp, int kind, const DevParams64 *params,
+                        const int *pidx, uint64_t *states, int ngen,
+                        void *out, uint64_t n, uint64_t outStride,
+                        cudaStream_t s);
+
+// ---- jump (jump_kernels.cu) ---------------------------------------------
+// One descriptor per jump.  The kernel reads the window at `src`, applies
+// the polynomial (uint32-array form, nwords words), and writes the jumped
+// window to `dst` (dst may equal src).  `polys` lists up to kMaxChain
+// polynomials applied in order (a chain); unused entries are null.
+constexpr int kMaxChain = 24;
+struct JumpDesc {
+    const uint32_t *poly[kMaxChain];
+    int nchain;
+    int pidx;          // parameter-set index
+    uint64_t src;      // element offset of the source window
+    uint64_t dst;      // element offset of the destination window
+};
+cudaError_t launchJump32(int mexp, const DevParams32 *params, uint32_t *states,
+                         const JumpDesc *descs, int ndesc, int nwords,
+                         cudaStream_t s);
+cudaError_t launchJump64(int mexp, const DevParams64 *params, uint64_t *states,
+                         const JumpDesc *descs, int ndesc, int nwords,
+                         cudaStream_t s);
+
+}  // namespace mtgp

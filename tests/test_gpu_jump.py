@@ -1,0 +1,114 @@
+"""GF(2) jump-ahead on the GPU vs the oracle (mtgp32-fast-jump.c:51-79)."""
+import numpy as np
+import pytest
+import torch
+
+from mtgp_gb300.params import jump_string, jump_table, load_table
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(32, "mtgp32_fast_11213"), (64, "mtgp64dc_fast_11213")]
+
+
+def _gen(bits, p, **kw):
+    from mtgp_gb300.api import MTGP32, MTGP64
+    return (MTGP32 if bits == 32 else MTGP64)(p, **kw)
+
+
+@pytest.mark.parametrize("bits,table", CASES)
+def test_fast_jump_string(gpu, orc, bits, table):
+    p = load_table(table)[0]
+    g = _gen(bits, p, seed=1234)
+    o = orc.gen(p, seed=1234)
+    g.fill(0, 777)
+    o.fill(0, 777)
+    g.fast_jump(jump_string(bits))
+    o.fast_jump(jump_string(bits))
+    assert np.array_equal(g.window(), o.window())
+    assert np.array_equal(g.fill(0, 4000).cpu().numpy().view(o.window().dtype), o.fill(0, 4000))
+
+
+@pytest.mark.parametrize("bits,table", CASES)
+def test_jump_table_rows(gpu, orc, bits, table):
+    p = load_table(table)[0]
+    tbl = jump_table(bits)
+    g = _gen(bits, p, seed=1)
+    o = orc.gen(p, seed=1)
+    for row in (5, 1, 3):
+        g.jump_array(tbl[row])
+        o.jump_words(tbl[row])
+        assert np.array_equal(g.window(), o.window()), row
+
+
+@pytest.mark.parametrize("bits,table,idx", [(32, "mtgp32_fast_23209", 2), (32, "mtgp32_fast_44497", 1),
+                                            (64, "mtgp64_fast_23209", 0), (64, "mtgp64_fast_44497", 3),
+                                            (64, "mtgp64_fast_110503", 0)])
+def test_jump_other_exponents(gpu, orc, bits, table, idx):
+    """Random polynomials on every exponent's kernel shape (output groups,
+    ring sizes, wide lanes)."""
+    p = load_table(table)[idx]
+    rng = np.random.default_rng(idx + bits)
+    nwords = p.mexp // 32 + 1
+    poly = rng.integers(0, 2 ** 32, nwords, dtype=np.uint64).astype(np.uint32)
+    poly[-1] &= (1 << (p.mexp % 32)) - 1
+    g = _gen(bits, p, seed=11)
+    o = orc.gen(p, seed=11)
+    g.jump_array(poly)
+    o.jump_words(poly)
+    assert np.array_equal(g.window(), o.window())
+
+
+def test_jump_small_polys(gpu, orc):
+    """Polynomials X^k for small k: jump == k steps (test-jump32.cpp:224-229)."""
+    for bits, table in CASES:
+        p = load_table(table)[0]
+        for k in (0, 1, 2, 31, 32, 33, 351, 1000):
+            poly = np.zeros(k // 32 + 1, dtype=np.uint32)
+            poly[k // 32] = 1 << (k % 32)
+            g = _gen(bits, p, seed=3)
+            o = orc.gen(p, seed=3)
+            g.jump_array(poly)
+            o.skip(k)
+            assert np.array_equal(g.window(), o.window()), (bits, k)
+
+
+@pytest.mark.parametrize("bits,table", CASES)
+def test_jump_steps_equals_skip(gpu, orc, bits, table):
+    """jump_steps builds X^s mod chi on the host (chi by Berlekamp-Massey over
+    GPU output) and jumps on the GPU."""
+    p = load_table(table)[0]
+    for steps in (1, 1000, 123457):
+        g = _gen(bits, p, seed=8)
+        o = orc.gen(p, seed=8)
+        g.jump_steps(steps)
+        o.skip(steps)
+        assert np.array_equal(g.window(), o.window()), steps
+
+
+def test_jump_steps_3_162_equals_table(gpu, orc):
+    p = load_table("mtgp32_fast_11213")[0]
+    g = _gen(32, p, seed=1234)
+    o = orc.gen(p, seed=1234)
+    g.jump_steps(3 ** 162)
+    o.fast_jump(jump_string(32))
+    assert np.array_equal(g.window(), o.window())
+
+
+@pytest.mark.parametrize("bits,table", CASES)
+def test_substreams(gpu, orc, bits, table):
+    """Substream j = seed state jumped by j * 3^162 on the GPU (the table
+    walk of cuda-sample/mtgp32-jump-kernel.cuh:383-401)."""
+    from mtgp_gb300.api import Pool
+    p = load_table(table)[0]
+    count = 70
+    pool = Pool.substreams(p, 1234, count, jump_table(bits))
+    win = pool.windows()
+    o = orc.gen(p, seed=1234)
+    js = jump_string(bits)
+    for j in range(count):
+        assert np.array_equal(win[j], o.window()), j
+        o.fast_jump(js)
+    # far substreams via the table rows directly
+    for j in (1023, 4095):
+        if j >= count:
+            continue
