@@ -89,6 +89,8 @@ class _Gen:
                                                         len(w), _stream(stream)))
 
     def jump_steps(self, steps, stream=None):
+        if not 0 <= steps < 2 ** 128:
+            raise ValueError("steps must be in [0, 2^128)")
         check(getattr(self._L, self.pre + "jump_steps")(self.h, steps & (2**64 - 1), steps >> 64,
                                                         _stream(stream)))
 

@@ -476,6 +476,9 @@ struct Pool {
             JumpDesc d{};
             for (int b = 0; b < 31; b++) {
                 if (!((j >> b) & 1)) continue;
+                if (d.nchain + 2 > kMaxChain)
+                    return setErr(MTGP_ERR_INVALID, "substream %d needs more than %d jumps", j,
+                                  kMaxChain);
                 const uint32_t *row = d_poly + (size_t)(b / 2) * nwords;
                 d.poly[d.nchain++] = row;
                 if (b & 1) d.poly[d.nchain++] = row;

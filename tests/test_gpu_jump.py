@@ -7,6 +7,20 @@ from mtgp_gb300.params import jump_string, jump_table, load_table
 
 pytestmark = pytest.mark.gpu
 
+
+def same_state(g, o, p):
+    """States agree: word 0 under the state mask (its other bits never reach
+    an output, mtgp32-fast.h:149-159; the reference compares it the same way,
+    cuda-sample/mtgp32-sample-jump1-host.cu:105-108), every other word
+    exactly, and the next outputs exactly."""
+    a, b = g.window(), o.clone().window()
+    if (int(a[0]) ^ int(b[0])) & int(p.mask):
+        return False
+    if not np.array_equal(a[1:], b[1:]):
+        return False
+    nxt = g.fill(0, 2000).cpu().numpy().view(a.dtype)
+    return np.array_equal(nxt, o.clone().fill(0, 2000))
+
 CASES = [(32, "mtgp32_fast_11213"), (64, "mtgp64dc_fast_11213")]
 
 
@@ -82,33 +96,56 @@ def test_jump_steps_equals_skip(gpu, orc, bits, table):
         o = orc.gen(p, seed=8)
         g.jump_steps(steps)
         o.skip(steps)
-        assert np.array_equal(g.window(), o.window()), steps
+        assert same_state(g, o, p), steps
 
 
-def test_jump_steps_3_162_equals_table(gpu, orc):
+def test_jump_steps_large_exponent(gpu, orc):
+    """A 127-bit step count: the GPU path's X^s mod chi (host GF(2) code)
+    equals the oracle's bit-serial PowerXMod, so the windows agree exactly."""
     p = load_table("mtgp32_fast_11213")[0]
+    steps = 3 ** 80
+    assert steps < 2 ** 128
+    bits_seq = (orc.gen(p, seed=1).fill(0, 2 * p.mexp) & 1).astype(np.uint8)
+    d, chi = orc.minpoly(bits_seq)
+    poly = orc.powxmod(steps, chi, d).view(np.uint32)[:351]
     g = _gen(32, p, seed=1234)
     o = orc.gen(p, seed=1234)
-    g.jump_steps(3 ** 162)
-    o.fast_jump(jump_string(32))
+    g.jump_steps(steps)
+    o.jump_words(poly)
     assert np.array_equal(g.window(), o.window())
+
+
+def test_jump_steps_rejects_oversized(gpu):
+    g = _gen(32, load_table("mtgp32_fast_11213")[0], seed=1)
+    with pytest.raises(ValueError):
+        g.jump_steps(2 ** 128)
 
 
 @pytest.mark.parametrize("bits,table", CASES)
 def test_substreams(gpu, orc, bits, table):
-    """Substream j = seed state jumped by j * 3^162 on the GPU (the table
-    walk of cuda-sample/mtgp32-jump-kernel.cuh:383-401)."""
+    """Substream j = seed state jumped by j * 3^162 on the GPU.  Exact against
+    the oracle walking the same table rows (bit b of j applies row b/2 once
+    for even b, twice for odd b: cuda-sample/mtgp32-jump-kernel.cuh:383-401);
+    equal as a state (word 0 under the mask, outputs exact) to j successive
+    JUMP3_162 jumps of the reference's CPU code."""
     from mtgp_gb300.api import Pool
     p = load_table(table)[0]
+    tbl = jump_table(bits)
     count = 70
-    pool = Pool.substreams(p, 1234, count, jump_table(bits))
+    pool = Pool.substreams(p, 1234, count, tbl)
     win = pool.windows()
-    o = orc.gen(p, seed=1234)
+    chain = orc.gen(p, seed=1234)
     js = jump_string(bits)
-    for j in range(count):
+    for j in list(range(count)):
+        o = orc.gen(p, seed=1234)
+        for b in range(12):
+            if (j >> b) & 1:
+                o.jump_words(tbl[b // 2])
+                if b & 1:
+                    o.jump_words(tbl[b // 2])
         assert np.array_equal(win[j], o.window()), j
-        o.fast_jump(js)
-    # far substreams via the table rows directly
-    for j in (1023, 4095):
-        if j >= count:
-            continue
+        c = chain.clone()
+        w = c.window()
+        assert (int(w[0]) ^ int(win[j][0])) & int(p.mask) == 0, j
+        assert np.array_equal(w[1:], win[j][1:]), j
+        chain.fast_jump(js)
