@@ -195,6 +195,10 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--substreams", type=int, default=N_SUB,
+                    help="substreams of the batched workload (profiling runs use fewer)")
+    ap.add_argument("--only", default="all", choices=["all", "batched", "bank"],
+                    help="profiling runs: time only one path, no e2e / plain / CPU legs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -219,7 +223,8 @@ def main():
     from mtgp_gb300.params import jump_table, load_table
 
     p = load_table("mtgp32_fast_11213")[0]
-    lens = lengths()
+    nsub = args.substreams
+    lens = lengths()[:nsub]
     offs = np.concatenate([[0], np.cumsum(lens)[:-1]]) * 4
     total_bytes = int(lens.sum()) * 4
     s = torch.cuda.Stream()
@@ -227,19 +232,24 @@ def main():
     # --- substream setup (GPU jumps), timed separately ---
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    pool = Pool.substreams(p, SEED + rank, N_SUB, jump_table(32), stream=s)
+    pool = Pool.substreams(p, SEED + rank, nsub, jump_table(32), stream=s)
     torch.cuda.synchronize()
     jump_ms = (time.perf_counter() - t0) * 1e3
     start_windows = pool.windows()
 
-    items = work_items(np.arange(N_SUB), np.zeros(N_SUB), lens, offs)
+    items = work_items(np.arange(nsub), np.zeros(nsub), lens, offs)
+    t0 = time.perf_counter()
     plan = pool.plan(items)
+    plan_ms = (time.perf_counter() - t0) * 1e3
+    plan_tasks, plan_chunk = plan.info()
     out = torch.empty(total_bytes // 4, dtype=torch.int32, device="cuda")
 
     # first step, kept for the CPU-baseline leg's bit-exact check
     plan.launch(out, s)
     s.synchronize()
     first_step = out[:int(lens[:256].sum())].cpu().numpy().view(np.uint32).copy()
+    if args.only == "bank":
+        args.steps = 0
 
     # --- batched, device-resident, CUDA graph ---
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -256,7 +266,7 @@ def main():
         s.synchronize()
         torch.cuda.synchronize()
         barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = max(ev0.elapsed_time(ev1) / max(args.steps, 1), 1e-6)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -264,9 +274,12 @@ def main():
     value = world * total_bytes / (ms * 1e-3) / 1e9
     launches = 2 * args.steps  # memset of the work counter + the persistent kernel
 
+    if args.only != "all":
+        args.plain_steps = 0
+        args.no_cpu = True
     # --- e2e: host items in, host output back, every step ---
+    e2e_steps = 0 if args.only != "all" else max(3, min(args.steps, 10))
     host_out = torch.empty(total_bytes // 4, dtype=torch.int32, pin_memory=True)
-    e2e_steps = max(3, min(args.steps, 10))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -274,7 +287,7 @@ def main():
             pool.submit(items, out, s)
             host_out.copy_(out, non_blocking=True)
         s.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = (time.perf_counter() - t0) / max(e2e_steps, 1)
     e2e = world * total_bytes / e2e_s / 1e9
 
     # --- plain: one launch (one CTA) per substream ---
@@ -283,13 +296,14 @@ def main():
         torch.cuda.synchronize()
         ev0.record(s)
         for _ in range(args.plain_steps):
-            for j in range(N_SUB):
+            for j in range(nsub):
                 pool.fill_stream(j, 0, out, int(lens[j]), stream=s, byte_offset=int(offs[j]))
         ev1.record(s)
         s.synchronize()
         plain_ms = ev0.elapsed_time(ev1) / args.plain_steps
 
     # --- bank: 128 parameter sets, 2^21 uint32 each, one CTA per set ---
+    bank_reps = 0 if args.only == "batched" else 5
     tbl = load_table("mtgp32_fast_11213")
     bank = Pool.create([tbl[i] for i in range(128)], np.arange(128) + 1234)
     nb = 1 << 21
@@ -298,15 +312,15 @@ def main():
         bank.fill(0, bout, nb, stream=s)
     s.synchronize()
     ev0.record(s)
-    for _ in range(5):
+    for _ in range(bank_reps):
         bank.fill(0, bout, nb, stream=s)
     ev1.record(s)
     s.synchronize()
-    bank_ms = ev0.elapsed_time(ev1) / 5
+    bank_ms = max(ev0.elapsed_time(ev1) / max(bank_reps, 1), 1e-6)
     bank_gbs = 128 * nb * 4 / (bank_ms * 1e-3) / 1e9
 
     hbm, peak_kind = peaks()
-    state_bytes = 2 * N_SUB * 351 * 4
+    state_bytes = 2 * nsub * 351 * 4
     achieved = (total_bytes + state_bytes) / (ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
@@ -338,12 +352,13 @@ def main():
             "pct_hbm": round(100 * value / world / hbm, 2),
             "plain": None if plain_ms is None else {
                 "value": round(world * total_bytes / (plain_ms * 1e-3) / 1e9, 3), "unit": "GB/s",
-                "ms_per_step": round(plain_ms, 2), "launches_per_step": N_SUB},
+                "ms_per_step": round(plain_ms, 2), "launches_per_step": nsub},
             "batched_over_plain": None if plain_ms is None else round(plain_ms / ms, 2),
             "bank": {"value": round(bank_gbs, 2), "unit": "GB/s", "ms": round(bank_ms, 3),
                      "workload": "128 sets x 2^21 uint32, seeds 1234+i, one CTA per set"},
-            "jump_setup": {"ms": round(jump_ms, 2), "us_per_substream": round(1e3 * jump_ms / N_SUB, 2)},
-            "e2e": {"value": round(e2e, 3), "unit": "GB/s", "h2d_bytes_per_step": 24 * N_SUB,
+            "jump_setup": {"ms": round(jump_ms, 2), "us_per_substream": round(1e3 * jump_ms / nsub, 2)},
+            "plan": {"tasks": plan_tasks, "split_chunk": plan_chunk, "build_ms": round(plan_ms, 1)},
+            "e2e": {"value": round(e2e, 3), "unit": "GB/s", "h2d_bytes_per_step": 24 * nsub,
                     "d2h_bytes_per_step": total_bytes},
             "roofline": roofline,
             "cpu_baseline": cpu,

@@ -324,6 +324,15 @@ int mtgp_gpu_plan_graph_launch(mtgp_gpu_plan_t *plan, void *dev_out,
                                void *stream);
 /* Bytes of output the plan writes (max over items of offset + size). */
 uint64_t mtgp_gpu_plan_output_bytes(const mtgp_gpu_plan_t *plan);
+/* Tasks of the launch after splitting, and the chunk length used to split
+ * long requests (0 = none split). */
+int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *plan, int64_t *tasks,
+                       int64_t *chunk);
+/* Process-wide tuning knobs for plans made afterwards (no reference
+ * counterpart; the autotuner and tests use them):
+ *   "split_chunk"  0 = automatic, < 0 = never split, > 0 = chunk length
+ *   "batch_grid"   0 = one CTA per resident slot, > 0 = that many CTAs  */
+int mtgp_gpu_set_tuning(const char *key, int64_t value);
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
 
 #if defined(__cplusplus)

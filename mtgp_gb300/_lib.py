@@ -38,6 +38,8 @@ SIGS = {
     "mtgp_gpu_plan_graph_launch": (c_int, [vp, vp, vp]),
     "mtgp_gpu_plan_output_bytes": (c_u64, [vp]),
     "mtgp_gpu_plan_free": (None, [vp]),
+    "mtgp_gpu_plan_info": (c_int, [vp, vp, vp]),
+    "mtgp_gpu_set_tuning": (c_int, [cp, ctypes.c_int64]),
 }
 for B, P, W in ((32, P32, c_u32), (64, P64, c_u64)):
     pre = "mtgp%d_gpu_" % B

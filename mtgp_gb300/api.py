@@ -157,6 +157,12 @@ class Plan:
     def output_bytes(self):
         return lib().mtgp_gpu_plan_output_bytes(self.h)
 
+    def info(self):
+        """(tasks after splitting, chunk length used for splitting or 0)."""
+        t, c = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().mtgp_gpu_plan_info(self.h, ctypes.byref(t), ctypes.byref(c)))
+        return t.value, c.value
+
     def launch(self, out, stream=None):
         check(lib().mtgp_gpu_plan_launch(self.h, ctypes.c_void_p(out.data_ptr()), _stream(stream)))
 
@@ -174,6 +180,12 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def set_tuning(key, value):
+    """Process-wide knobs for plans made afterwards: "split_chunk" (0 auto,
+    <0 never, >0 chunk length) and "batch_grid" (0 auto, >0 CTAs)."""
+    check(lib().mtgp_gpu_set_tuning(key.encode(), int(value)))
 
 
 def work_items(streams, kinds, counts, offsets):

@@ -18,14 +18,47 @@ struct BatchTask {
     int32_t first;     // first item (items of one task are consecutive)
     int32_t nitems;
     int32_t pidx;      // parameter-set index of the stream
+    // Chunk of a split request: the task starts from the stream's window
+    // jumped by this polynomial (uint32-array form); null = no jump.
+    const uint32_t *jpoly;
+    // Where the advanced window goes: kWbStream = back to the stream,
+    // kWbNone = nowhere (a chunk that is not the last), k >= 0 = staging
+    // slot k (the last chunk; copied to the stream after the launch, so no
+    // chunk can read a window that another chunk already advanced).
+    int32_t wb;
+    int32_t pad_;
 };
+constexpr int32_t kWbStream = -1;
+constexpr int32_t kWbNone = -2;
 
 // grid <= 0: size the grid to the resident-CTA capacity of the GPU.
-cudaError_t launchBatch32(int mexp, const DevParams32 *params, uint32_t *states,
-                          const BatchTask *tasks, int ntasks, const BatchItem *items,
-                          void *out, unsigned *counter, int grid, cudaStream_t s);
-cudaError_t launchBatch64(int mexp, const DevParams64 *params, uint64_t *states,
-                          const BatchTask *tasks, int ntasks, const BatchItem *items,
-                          void *out, unsigned *counter, int grid, cudaStream_t s);
+// mode: the output kind shared by every item (-1 = all skips), or -2 when
+// items mix kinds.
+// split: some tasks carry jpoly (kernel variant with the jump code).
+// stage / stage_streams / nstage: staged windows copied to their streams
+// after the launch (stage slot k -> stream stage_streams[k]).
+struct BatchLaunch {
+    int mexp, mode, grid;
+    bool split;
+    int nwords;                     // words of every jpoly
+    const BatchTask *tasks;
+    int ntasks;
+    const BatchItem *items;
+    void *out;
+    unsigned *counter;
+    void *stage;
+    const int32_t *stage_streams;
+    int nstage;
+};
+cudaError_t launchBatch32(const BatchLaunch &b, const DevParams32 *params, uint32_t *states,
+                          cudaStream_t s);
+cudaError_t launchBatch64(const BatchLaunch &b, const DevParams64 *params, uint64_t *states,
+                          cudaStream_t s);
+// Whether the batched kernel of this exponent can split long requests.
+bool batchSplits32(int mexp);
+bool batchSplits64(int mexp);
+// Number of CTAs of the batched kernel resident at once on the device.
+int batchResident32(int mexp);
+int batchResident64(int mexp);
 
 }  // namespace mtgp

@@ -6,24 +6,44 @@
 // order.  The grid is sized to the number of CTAs the GPU keeps resident;
 // each CTA takes the next task from a device counter (tasks are sorted
 // longest-first on the host, so the long ones start first), loads the
-// stream's window into its shared ring, runs the items, and writes the
-// advanced window back.  The arithmetic is the plain path's (run32/run64).
+// stream's window into shared memory, runs the items with the generation
+// core (mtgp_device.cuh), and writes the advanced window back.
+//
+// Long requests are split into chunks that run on different CTAs: chunk c
+// starts from the stream's window jumped ahead by its offset (X^off mod chi,
+// applied in the CTA with jump_device.cuh), and only the last chunk keeps
+// its final window, in a staging slot that a small kernel copies back after
+// the launch.
 #include "batch.h"
-#include "mtgp_device.cuh"
+#include "jump_device.cuh"
 
 namespace mtgp {
 
 namespace {
 
-template <int N, int TN, int RING>
-__global__ void __launch_bounds__(TN)
+// Jump geometry used inside the batched kernel (NT = the kernel's threads);
+// the jump's shared buffers alias the generation buffer.
+template <int N> struct SplitGeo32;
+template <> struct SplitGeo32<351> { using G = JGeo<351, 11, 256, 256, 2048>; };
+template <> struct SplitGeo32<726> { using G = JGeo<726, 23, 512, 512, 4096>; };
+template <int N> struct SplitGeo64;
+template <> struct SplitGeo64<176> { using G = JGeo<176, 7, 128, 128, 1024>; };
+template <> struct SplitGeo64<363> { using G = JGeo<363, 13, 256, 256, 2048>; };
+
+template <int N> constexpr bool kSplit32 = (N == 351 || N == 726);
+template <int N> constexpr bool kSplit64 = (N == 176 || N == 363);
+
+// MODE >= -1: every item has output kind MODE (-1 = skip); MODE == -2:
+// items of any kind (the kind is switched per item).  SPLIT: tasks may
+// carry a jump polynomial.
+template <int N, int TN, int B, int MODE, bool SPLIT>
+__global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1536 : 2048) / TN)
 k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
-          unsigned *__restrict__ counter) {
-    __shared__ uint32_t ring[RING];
+          unsigned *__restrict__ counter, uint32_t *__restrict__ stage, int nwords) {
+    __shared__ __align__(16) uint32_t buf[B];
     __shared__ int s_task;
-    constexpr uint32_t M = RING - 1;
     for (;;) {
         if (threadIdx.x == 0) s_task = (int)atomicAdd(counter, 1u);
         __syncthreads();
@@ -34,36 +54,47 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
         Lane32 L;
         L.load(params[T.pidx], threadIdx.x & 31);
         uint32_t *st = states + (size_t)T.stream * stateStride(N);
-        for (int k = threadIdx.x; k < N; k += TN) ring[k] = st[k];
+        for (int k = threadIdx.x; k < N; k += TN) buf[k] = st[k];
+        if constexpr (SPLIT && kSplit32<N>) {
+            using G = typename SplitGeo32<N>::G;
+            static_assert(G::NT == TN, "jump geometry must use the kernel's threads");
+            if (T.jpoly) jump_one<Tr32, G>(buf, L, T.jpoly, nwords);
+        }
         __syncthreads();
-        uint32_t phase = 0;
         for (int i = 0; i < T.nitems; i++) {
             const BatchItem I = items[T.first + i];
             char *o = out + I.out_off;
-            switch (I.kind) {
-            case 0: run32<N, TN, RING, 0>(ring, L, L.tmp, phase, I.count, (uint32_t *)o); break;
-            case 1: run32<N, TN, RING, 1>(ring, L, L.flt, phase, I.count, (float *)o); break;
-            case 2: run32<N, TN, RING, 2>(ring, L, L.flt, phase, I.count, (float *)o); break;
-            case 3: run32<N, TN, RING, 3>(ring, L, L.flt, phase, I.count, (float *)o); break;
-            case 4: run32<N, TN, RING, 4>(ring, L, L.flt, phase, I.count, (float *)o); break;
-            default: run32<N, TN, RING, -1>(ring, L, L.tmp, phase, I.count, nullptr); break;
+            if constexpr (MODE >= -1) {
+                using OT = typename Out32<(MODE < 0 ? 0 : MODE)>::T;
+                run32<N, TN, B, MODE>(buf, L, L.otab(MODE < 0 ? 0 : MODE), I.count, (OT *)o);
+            } else {
+                switch (I.kind) {
+                case 0: run32<N, TN, B, 0>(buf, L, L.tmp, I.count, (uint32_t *)o); break;
+                case 1: run32<N, TN, B, 1>(buf, L, L.flt, I.count, (float *)o); break;
+                case 2: run32<N, TN, B, 2>(buf, L, L.flt, I.count, (float *)o); break;
+                case 3: run32<N, TN, B, 3>(buf, L, L.flt, I.count, (float *)o); break;
+                case 4: run32<N, TN, B, 4>(buf, L, L.flt, I.count, (float *)o); break;
+                default: run32<N, TN, B, -1>(buf, L, L.tmp, I.count, nullptr); break;
+                }
             }
-            phase += (uint32_t)I.count;
         }
-        for (int k = threadIdx.x; k < N; k += TN) st[k] = ring[(phase + k) & M];
+        uint32_t *dst = T.wb == kWbStream ? st
+                      : T.wb >= 0         ? stage + (size_t)T.wb * stateStride(N)
+                                          : nullptr;
+        if (dst)
+            for (int k = threadIdx.x; k < N; k += TN) dst[k] = buf[k];
         __syncthreads();
     }
 }
 
-template <int N, int TN, int RING>
-__global__ void __launch_bounds__(TN)
+template <int N, int TN, int B, int MODE, bool SPLIT>
+__global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1536 : 2048) / TN)
 k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
-          unsigned *__restrict__ counter) {
-    __shared__ uint64_t ring[RING];
+          unsigned *__restrict__ counter, uint64_t *__restrict__ stage, int nwords) {
+    __shared__ __align__(16) uint64_t buf[B];
     __shared__ int s_task;
-    constexpr uint32_t M = RING - 1;
     for (;;) {
         if (threadIdx.x == 0) s_task = (int)atomicAdd(counter, 1u);
         __syncthreads();
@@ -74,29 +105,51 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
         Lane64 L;
         L.load(params[T.pidx], threadIdx.x & 31);
         uint64_t *st = states + (size_t)T.stream * stateStride(N);
-        for (int k = threadIdx.x; k < N; k += TN) ring[k] = st[k];
+        for (int k = threadIdx.x; k < N; k += TN) buf[k] = st[k];
+        if constexpr (SPLIT && kSplit64<N>) {
+            using G = typename SplitGeo64<N>::G;
+            static_assert(G::NT == TN, "jump geometry must use the kernel's threads");
+            if (T.jpoly) jump_one<Tr64, G>(buf, L, T.jpoly, nwords);
+        }
         __syncthreads();
-        uint32_t phase = 0;
         for (int i = 0; i < T.nitems; i++) {
             const BatchItem I = items[T.first + i];
             char *o = out + I.out_off;
-            switch (I.kind) {
-            case 0: run64<N, TN, RING, 0>(ring, L, L.tmp_lo, L.tmp_hi, phase, I.count, (uint64_t *)o); break;
-            case 1: run64<N, TN, RING, 1>(ring, L, L.dbl_lo, L.dbl_hi, phase, I.count, (double *)o); break;
-            case 2: run64<N, TN, RING, 2>(ring, L, L.dbl_lo, L.dbl_hi, phase, I.count, (double *)o); break;
-            case 3: run64<N, TN, RING, 3>(ring, L, L.dbl_lo, L.dbl_hi, phase, I.count, (double *)o); break;
-            case 4: run64<N, TN, RING, 4>(ring, L, L.dbl_lo, L.dbl_hi, phase, I.count, (double *)o); break;
-            default: run64<N, TN, RING, -1>(ring, L, L.tmp_lo, L.tmp_hi, phase, I.count, nullptr); break;
+            if constexpr (MODE >= -1) {
+                using OT = typename Out64<(MODE < 0 ? 0 : MODE)>::T;
+                run64<N, TN, B, MODE>(buf, L, L.otab_lo(MODE < 0 ? 0 : MODE),
+                                      L.otab_hi(MODE < 0 ? 0 : MODE), I.count, (OT *)o);
+            } else {
+                switch (I.kind) {
+                case 0: run64<N, TN, B, 0>(buf, L, L.tmp_lo, L.tmp_hi, I.count, (uint64_t *)o); break;
+                case 1: run64<N, TN, B, 1>(buf, L, L.dbl_lo, L.dbl_hi, I.count, (double *)o); break;
+                case 2: run64<N, TN, B, 2>(buf, L, L.dbl_lo, L.dbl_hi, I.count, (double *)o); break;
+                case 3: run64<N, TN, B, 3>(buf, L, L.dbl_lo, L.dbl_hi, I.count, (double *)o); break;
+                case 4: run64<N, TN, B, 4>(buf, L, L.dbl_lo, L.dbl_hi, I.count, (double *)o); break;
+                default: run64<N, TN, B, -1>(buf, L, L.tmp_lo, L.tmp_hi, I.count, nullptr); break;
+                }
             }
-            phase += (uint32_t)I.count;
         }
-        for (int k = threadIdx.x; k < N; k += TN) st[k] = ring[(phase + k) & M];
+        uint64_t *dst = T.wb == kWbStream ? st
+                      : T.wb >= 0         ? stage + (size_t)T.wb * stateStride(N)
+                                          : nullptr;
+        if (dst)
+            for (int k = threadIdx.x; k < N; k += TN) dst[k] = buf[k];
         __syncthreads();
     }
 }
 
+// Staged windows back to their streams: block k copies slot k.
+template <typename W, int N>
+__global__ void k_unstage(W *__restrict__ states, const W *__restrict__ stage,
+                          const int32_t *__restrict__ streams) {
+    const W *src = stage + (size_t)blockIdx.x * stateStride(N);
+    W *dst = states + (size_t)streams[blockIdx.x] * stateStride(N);
+    for (int k = threadIdx.x; k < N; k += blockDim.x) dst[k] = src[k];
+}
+
 template <class K>
-static cudaError_t occupancy(K kern, int tn, int *grid) {
+static cudaError_t resident(K kern, int tn, int *grid) {
     int dev = 0, sms = 0, per = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -105,65 +158,127 @@ static cudaError_t occupancy(K kern, int tn, int *grid) {
     return e;
 }
 
-template <int N, int TN, int RING>
-static cudaError_t batch32(const DevParams32 *params, uint32_t *states, const BatchTask *tasks,
-                           int ntasks, const BatchItem *items, char *out, unsigned *counter,
-                           int grid, cudaStream_t s) {
-    auto kern = k_batch32<N, TN, RING>;
+template <typename W, class K, class P>
+static cudaError_t go(K kern, int tn, const BatchLaunch &b, const P *params, W *states,
+                      cudaStream_t s, int n) {
+    int grid = b.grid;
     if (grid <= 0) {
-        cudaError_t e = occupancy(kern, TN, &grid);
+        cudaError_t e = resident(kern, tn, &grid);
         if (e != cudaSuccess) return e;
     }
-    if (grid > ntasks) grid = ntasks;
-    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
+    if (grid > b.ntasks) grid = b.ntasks;
+    cudaError_t e = cudaMemsetAsync(b.counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
-    kern<<<grid, TN, 0, s>>>(params, states, tasks, ntasks, items, out, counter);
+    kern<<<grid, tn, 0, s>>>(params, states, b.tasks, b.ntasks, b.items,
+                             static_cast<char *>(b.out), b.counter, static_cast<W *>(b.stage),
+                             b.nwords);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || b.nstage <= 0) return e;
+    (void)n;
+    return cudaSuccess;
+}
+
+template <int N, int TN, int B, bool SPLIT>
+static cudaError_t mode32(const BatchLaunch &b, const DevParams32 *p, uint32_t *st,
+                          cudaStream_t s) {
+    switch (b.mode) {
+    case -1: return go<uint32_t>(k_batch32<N, TN, B, -1, SPLIT>, TN, b, p, st, s, N);
+    case 0: return go<uint32_t>(k_batch32<N, TN, B, 0, SPLIT>, TN, b, p, st, s, N);
+    case 1: return go<uint32_t>(k_batch32<N, TN, B, 1, SPLIT>, TN, b, p, st, s, N);
+    case 2: return go<uint32_t>(k_batch32<N, TN, B, 2, SPLIT>, TN, b, p, st, s, N);
+    case 3: return go<uint32_t>(k_batch32<N, TN, B, 3, SPLIT>, TN, b, p, st, s, N);
+    case 4: return go<uint32_t>(k_batch32<N, TN, B, 4, SPLIT>, TN, b, p, st, s, N);
+    default: return go<uint32_t>(k_batch32<N, TN, B, -2, SPLIT>, TN, b, p, st, s, N);
+    }
+}
+
+template <int N, int TN, int B, bool SPLIT>
+static cudaError_t mode64(const BatchLaunch &b, const DevParams64 *p, uint64_t *st,
+                          cudaStream_t s) {
+    switch (b.mode) {
+    case -1: return go<uint64_t>(k_batch64<N, TN, B, -1, SPLIT>, TN, b, p, st, s, N);
+    case 0: return go<uint64_t>(k_batch64<N, TN, B, 0, SPLIT>, TN, b, p, st, s, N);
+    case 1: return go<uint64_t>(k_batch64<N, TN, B, 1, SPLIT>, TN, b, p, st, s, N);
+    case 2: return go<uint64_t>(k_batch64<N, TN, B, 2, SPLIT>, TN, b, p, st, s, N);
+    case 3: return go<uint64_t>(k_batch64<N, TN, B, 3, SPLIT>, TN, b, p, st, s, N);
+    case 4: return go<uint64_t>(k_batch64<N, TN, B, 4, SPLIT>, TN, b, p, st, s, N);
+    default: return go<uint64_t>(k_batch64<N, TN, B, -2, SPLIT>, TN, b, p, st, s, N);
+    }
+}
+
+template <int N, int TN, int B>
+static cudaError_t run32x(const BatchLaunch &b, const DevParams32 *p, uint32_t *st,
+                          cudaStream_t s) {
+    cudaError_t e;
+    if constexpr (kSplit32<N>) {
+        e = b.split ? mode32<N, TN, B, true>(b, p, st, s) : mode32<N, TN, B, false>(b, p, st, s);
+    } else {
+        if (b.split) return cudaErrorInvalidValue;
+        e = mode32<N, TN, B, false>(b, p, st, s);
+    }
+    if (e != cudaSuccess || b.nstage <= 0) return e;
+    k_unstage<uint32_t, N><<<b.nstage, 128, 0, s>>>(st, static_cast<const uint32_t *>(b.stage),
+                                                    b.stage_streams);
     return cudaGetLastError();
 }
 
-template <int N, int TN, int RING>
-static cudaError_t batch64(const DevParams64 *params, uint64_t *states, const BatchTask *tasks,
-                           int ntasks, const BatchItem *items, char *out, unsigned *counter,
-                           int grid, cudaStream_t s) {
-    auto kern = k_batch64<N, TN, RING>;
-    if (grid <= 0) {
-        cudaError_t e = occupancy(kern, TN, &grid);
-        if (e != cudaSuccess) return e;
+template <int N, int TN, int B>
+static cudaError_t run64x(const BatchLaunch &b, const DevParams64 *p, uint64_t *st,
+                          cudaStream_t s) {
+    cudaError_t e;
+    if constexpr (kSplit64<N>) {
+        e = b.split ? mode64<N, TN, B, true>(b, p, st, s) : mode64<N, TN, B, false>(b, p, st, s);
+    } else {
+        if (b.split) return cudaErrorInvalidValue;
+        e = mode64<N, TN, B, false>(b, p, st, s);
     }
-    if (grid > ntasks) grid = ntasks;
-    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned), s);
-    if (e != cudaSuccess) return e;
-    kern<<<grid, TN, 0, s>>>(params, states, tasks, ntasks, items, out, counter);
+    if (e != cudaSuccess || b.nstage <= 0) return e;
+    k_unstage<uint64_t, N><<<b.nstage, 128, 0, s>>>(st, static_cast<const uint64_t *>(b.stage),
+                                                    b.stage_streams);
     return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launchBatch32(int mexp, const DevParams32 *params, uint32_t *states,
-                          const BatchTask *tasks, int ntasks, const BatchItem *items,
-                          void *out, unsigned *counter, int grid, cudaStream_t s) {
-    if (ntasks <= 0) return cudaSuccess;
-    char *o = static_cast<char *>(out);
-    switch (mexp) {
-    case 11213: return batch32<351, 256, 1024>(params, states, tasks, ntasks, items, o, counter, grid, s);
-    case 23209: return batch32<726, 512, 2048>(params, states, tasks, ntasks, items, o, counter, grid, s);
-    case 44497: return batch32<1391, 1024, 4096>(params, states, tasks, ntasks, items, o, counter, grid, s);
-    default: return cudaErrorInvalidValue;
-    }
+cudaError_t launchBatch32(const BatchLaunch &b, const DevParams32 *params, uint32_t *states,
+                          cudaStream_t s) {
+    if (b.ntasks <= 0) return cudaSuccess;
+#define X(M, N, T, B) \
+    if (b.mexp == M) return run32x<N, T, B>(b, params, states, s);
+    MTGP_SHAPES32(X)
+#undef X
+    return cudaErrorInvalidValue;
 }
 
-cudaError_t launchBatch64(int mexp, const DevParams64 *params, uint64_t *states,
-                          const BatchTask *tasks, int ntasks, const BatchItem *items,
-                          void *out, unsigned *counter, int grid, cudaStream_t s) {
-    if (ntasks <= 0) return cudaSuccess;
-    char *o = static_cast<char *>(out);
-    switch (mexp) {
-    case 11213: return batch64<176, 128, 512>(params, states, tasks, ntasks, items, o, counter, grid, s);
-    case 23209: return batch64<363, 256, 1024>(params, states, tasks, ntasks, items, o, counter, grid, s);
-    case 44497: return batch64<696, 512, 2048>(params, states, tasks, ntasks, items, o, counter, grid, s);
-    case 110503: return batch64<1727, 1024, 4096>(params, states, tasks, ntasks, items, o, counter, grid, s);
-    default: return cudaErrorInvalidValue;
-    }
+cudaError_t launchBatch64(const BatchLaunch &b, const DevParams64 *params, uint64_t *states,
+                          cudaStream_t s) {
+    if (b.ntasks <= 0) return cudaSuccess;
+#define X(M, N, T, B) \
+    if (b.mexp == M) return run64x<N, T, B>(b, params, states, s);
+    MTGP_SHAPES64(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+bool batchSplits32(int mexp) { return mexp == 11213 || mexp == 23209; }
+bool batchSplits64(int mexp) { return mexp == 11213 || mexp == 23209; }
+
+int batchResident32(int mexp) {
+    int g = 0;
+#define X(M, N, T, B) \
+    if (mexp == M) resident(k_batch32<N, T, B, 0, false>, T, &g);
+    MTGP_SHAPES32(X)
+#undef X
+    return g;
+}
+
+int batchResident64(int mexp) {
+    int g = 0;
+#define X(M, N, T, B) \
+    if (mexp == M) resident(k_batch64<N, T, B, 0, false>, T, &g);
+    MTGP_SHAPES64(X)
+#undef X
+    return g;
 }
 
 }  // namespace mtgp

@@ -11,30 +11,27 @@
 namespace mtgp {
 
 bool shape32(int mexp, Shape *s) {
-    switch (mexp) {
-    case 11213: *s = {11213, 351, 256, 1024}; return true;
-    case 23209: *s = {23209, 726, 512, 2048}; return true;
-    case 44497: *s = {44497, 1391, 1024, 4096}; return true;
-    default: return false;
-    }
+#define X(M, N, T, B) \
+    if (mexp == M) { *s = {M, N, T, B}; return true; }
+    MTGP_SHAPES32(X)
+#undef X
+    return false;
 }
 
 bool shape64(int mexp, Shape *s) {
-    switch (mexp) {
-    case 11213: *s = {11213, 176, 128, 512}; return true;
-    case 23209: *s = {23209, 363, 256, 1024}; return true;
-    case 44497: *s = {44497, 696, 512, 2048}; return true;
-    case 110503: *s = {110503, 1727, 1024, 4096}; return true;
-    default: return false;
-    }
+#define X(M, N, T, B) \
+    if (mexp == M) { *s = {M, N, T, B}; return true; }
+    MTGP_SHAPES64(X)
+#undef X
+    return false;
 }
 
-template <int N, int TN, int RING, int KIND>
+template <int N, int TN, int B, int KIND>
 __global__ void __launch_bounds__(TN)
 k_gen32(const DevParams32 *__restrict__ params, const int *__restrict__ pidx,
         uint32_t *__restrict__ states, void *__restrict__ out, uint64_t n,
         uint64_t out_stride) {
-    __shared__ uint32_t ring[RING];
+    __shared__ uint32_t ring[B];
     const int g = blockIdx.x;
     const DevParams32 &P = params[pidx ? pidx[g] : g];
     Lane32 L;
@@ -44,16 +41,16 @@ k_gen32(const DevParams32 *__restrict__ params, const int *__restrict__ pidx,
     __syncthreads();
     using T = typename Out32<(KIND < 0 ? 0 : KIND)>::T;
     T *o = KIND < 0 ? nullptr : reinterpret_cast<T *>(out) + (size_t)g * out_stride;
-    run32<N, TN, RING, KIND>(ring, L, L.otab(KIND < 0 ? 0 : KIND), 0u, n, o);
-    for (int k = threadIdx.x; k < N; k += TN) st[k] = ring[((uint32_t)n + k) & (RING - 1)];
+    run32<N, TN, B, KIND>(ring, L, L.otab(KIND < 0 ? 0 : KIND), n, o);
+    for (int k = threadIdx.x; k < N; k += TN) st[k] = ring[k];
 }
 
-template <int N, int TN, int RING, int KIND>
+template <int N, int TN, int B, int KIND>
 __global__ void __launch_bounds__(TN)
 k_gen64(const DevParams64 *__restrict__ params, const int *__restrict__ pidx,
         uint64_t *__restrict__ states, void *__restrict__ out, uint64_t n,
         uint64_t out_stride) {
-    __shared__ uint64_t ring[RING];
+    __shared__ uint64_t ring[B];
     const int g = blockIdx.x;
     const DevParams64 &P = params[pidx ? pidx[g] : g];
     Lane64 L;
@@ -63,40 +60,40 @@ k_gen64(const DevParams64 *__restrict__ params, const int *__restrict__ pidx,
     __syncthreads();
     using T = typename Out64<(KIND < 0 ? 0 : KIND)>::T;
     T *o = KIND < 0 ? nullptr : reinterpret_cast<T *>(out) + (size_t)g * out_stride;
-    run64<N, TN, RING, KIND>(ring, L, L.otab_lo(KIND < 0 ? 0 : KIND),
-                             L.otab_hi(KIND < 0 ? 0 : KIND), 0u, n, o);
-    for (int k = threadIdx.x; k < N; k += TN) st[k] = ring[((uint32_t)n + k) & (RING - 1)];
+    run64<N, TN, B, KIND>(ring, L, L.otab_lo(KIND < 0 ? 0 : KIND),
+                          L.otab_hi(KIND < 0 ? 0 : KIND), n, o);
+    for (int k = threadIdx.x; k < N; k += TN) st[k] = ring[k];
 }
 
-template <int N, int TN, int RING>
+template <int N, int TN, int B>
 static cudaError_t gen32_kind(int kind, const DevParams32 *params, const int *pidx,
                               uint32_t *states, int ngen, void *out, uint64_t n,
                               uint64_t os, cudaStream_t s) {
     dim3 grid(ngen), block(TN);
     switch (kind) {
-    case -1: k_gen32<N, TN, RING, -1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 0: k_gen32<N, TN, RING, 0><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 1: k_gen32<N, TN, RING, 1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 2: k_gen32<N, TN, RING, 2><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 3: k_gen32<N, TN, RING, 3><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 4: k_gen32<N, TN, RING, 4><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case -1: k_gen32<N, TN, B, -1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 0: k_gen32<N, TN, B, 0><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 1: k_gen32<N, TN, B, 1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 2: k_gen32<N, TN, B, 2><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 3: k_gen32<N, TN, B, 3><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 4: k_gen32<N, TN, B, 4><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
 
-template <int N, int TN, int RING>
+template <int N, int TN, int B>
 static cudaError_t gen64_kind(int kind, const DevParams64 *params, const int *pidx,
                               uint64_t *states, int ngen, void *out, uint64_t n,
                               uint64_t os, cudaStream_t s) {
     dim3 grid(ngen), block(TN);
     switch (kind) {
-    case -1: k_gen64<N, TN, RING, -1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 0: k_gen64<N, TN, RING, 0><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 1: k_gen64<N, TN, RING, 1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 2: k_gen64<N, TN, RING, 2><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 3: k_gen64<N, TN, RING, 3><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
-    case 4: k_gen64<N, TN, RING, 4><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case -1: k_gen64<N, TN, B, -1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 0: k_gen64<N, TN, B, 0><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 1: k_gen64<N, TN, B, 1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 2: k_gen64<N, TN, B, 2><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 3: k_gen64<N, TN, B, 3><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 4: k_gen64<N, TN, B, 4><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -106,25 +103,22 @@ cudaError_t launchGen32(int mexp, int kind, const DevParams32 *params, const int
                         uint32_t *states, int ngen, void *out, uint64_t n,
                         uint64_t os, cudaStream_t s) {
     if (ngen <= 0 || n == 0) return cudaSuccess;
-    switch (mexp) {
-    case 11213: return gen32_kind<351, 256, 1024>(kind, params, pidx, states, ngen, out, n, os, s);
-    case 23209: return gen32_kind<726, 512, 2048>(kind, params, pidx, states, ngen, out, n, os, s);
-    case 44497: return gen32_kind<1391, 1024, 4096>(kind, params, pidx, states, ngen, out, n, os, s);
-    default: return cudaErrorInvalidValue;
-    }
+#define X(M, N, T, B) \
+    if (mexp == M) return gen32_kind<N, T, B>(kind, params, pidx, states, ngen, out, n, os, s);
+    MTGP_SHAPES32(X)
+#undef X
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launchGen64(int mexp, int kind, const DevParams64 *params, const int *pidx,
                         uint64_t *states, int ngen, void *out, uint64_t n,
                         uint64_t os, cudaStream_t s) {
     if (ngen <= 0 || n == 0) return cudaSuccess;
-    switch (mexp) {
-    case 11213: return gen64_kind<176, 128, 512>(kind, params, pidx, states, ngen, out, n, os, s);
-    case 23209: return gen64_kind<363, 256, 1024>(kind, params, pidx, states, ngen, out, n, os, s);
-    case 44497: return gen64_kind<696, 512, 2048>(kind, params, pidx, states, ngen, out, n, os, s);
-    case 110503: return gen64_kind<1727, 1024, 4096>(kind, params, pidx, states, ngen, out, n, os, s);
-    default: return cudaErrorInvalidValue;
-    }
+#define X(M, N, T, B) \
+    if (mexp == M) return gen64_kind<N, T, B>(kind, params, pidx, states, ngen, out, n, os, s);
+    MTGP_SHAPES64(X)
+#undef X
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace mtgp

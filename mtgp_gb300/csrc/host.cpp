@@ -72,6 +72,15 @@ int cudaErr(cudaError_t e, const char *what) {
 
 inline cudaStream_t S(void *s) { return static_cast<cudaStream_t>(s); }
 
+// Tuning knobs (mtgp_gpu_set_tuning).  split_chunk: 0 = automatic, < 0 =
+// never split long requests, > 0 = split into chunks of this many values.
+// batch_grid: 0 = one CTA per resident slot, > 0 = that many CTAs.
+struct Tuning {
+    int64_t split_chunk = 0;
+    int64_t batch_grid = 0;
+};
+Tuning g_tune;
+
 // ------------------------------------------------------------------------
 // Seeding (host).  Same integer arithmetic as the reference.
 // ------------------------------------------------------------------------
@@ -172,10 +181,11 @@ struct T32 {
                             cudaStream_t s) {
         return launchJump32(mexp, p, st, d, nd, nw, s);
     }
-    static cudaError_t batch(int mexp, const DP *p, W *st, const BatchTask *t, int nt,
-                             const BatchItem *i, void *out, unsigned *c, int g, cudaStream_t s) {
-        return launchBatch32(mexp, p, st, t, nt, i, out, c, g, s);
+    static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
+        return launchBatch32(b, p, st, s);
     }
+    static bool splits(int mexp) { return batchSplits32(mexp); }
+    static int resident(int mexp) { return batchResident32(mexp); }
     static void seed(const HP &p, W s, W *a) { seed32(p, s, a); }
     static void byArray(const HP &p, const W *key, int len, W *a) {
         keyed<W>(a, p.mexp / 32 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
@@ -203,10 +213,11 @@ struct T64 {
                             cudaStream_t s) {
         return launchJump64(mexp, p, st, d, nd, nw, s);
     }
-    static cudaError_t batch(int mexp, const DP *p, W *st, const BatchTask *t, int nt,
-                             const BatchItem *i, void *out, unsigned *c, int g, cudaStream_t s) {
-        return launchBatch64(mexp, p, st, t, nt, i, out, c, g, s);
+    static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
+        return launchBatch64(b, p, st, s);
     }
+    static bool splits(int mexp) { return batchSplits64(mexp); }
+    static int resident(int mexp) { return batchResident64(mexp); }
     static void seed(const HP &p, W s, W *a) { seed64(p, s, a); }
     static void byArray(const HP &p, const W *key, int len, W *a) {
         keyed<W>(a, p.mexp / 64 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
@@ -253,8 +264,12 @@ struct Pool {
     size_t desc_cap = 0;
     std::vector<gf2::Poly> chi;   // characteristic polynomial per parameter set
     std::vector<int> chideg;
+    // device copies of X^steps mod chi, keyed by (parameter set, steps)
+    std::vector<std::pair<std::pair<int, uint64_t>, uint32_t *>> jcache;
+    int resident = 0;
 
     ~Pool() {
+        for (auto &kv : jcache) cudaFree(kv.second);
         cudaFree(d_params);
         cudaFree(d_pidx);
         cudaFree(d_states);
@@ -442,6 +457,32 @@ struct Pool {
         return MTGP_OK;
     }
 
+    int polyWords() const { return sh.mexp / 32 + 1; }
+
+    // Device copy of X^steps mod chi_k (cached).
+    int jumpPoly(int k, uint64_t steps, const uint32_t **out) {
+        for (auto &kv : jcache)
+            if (kv.first.first == k && kv.first.second == steps) {
+                *out = kv.second;
+                return MTGP_OK;
+            }
+        int rc = characteristic(k);
+        if (rc) return rc;
+        std::vector<uint32_t> e = {(uint32_t)steps, (uint32_t)(steps >> 32)};
+        gf2::Poly p = gf2::powxmod(e, chi[k], chideg[k]);
+        std::vector<uint32_t> w = gf2::toWords32(p, polyWords());
+        uint32_t *d = nullptr;
+        CK(cudaMalloc(&d, sizeof(uint32_t) * w.size()), "cudaMalloc(jump poly)");
+        cudaError_t e2 = cudaMemcpy(d, w.data(), sizeof(uint32_t) * w.size(), cudaMemcpyHostToDevice);
+        if (e2 != cudaSuccess) {
+            cudaFree(d);
+            return cudaErr(e2, "upload jump poly");
+        }
+        jcache.push_back({{k, steps}, d});
+        *out = d;
+        return MTGP_OK;
+    }
+
     int jumpSteps(int i, uint64_t lo, uint64_t hi, void *s) {
         if (i < 0 || i >= count) return setErr(MTGP_ERR_INVALID, "stream %d out of range", i);
         if (lo == 0 && hi == 0) return MTGP_OK;
@@ -533,12 +574,20 @@ struct mtgp_gpu_plan {
     BatchItem *d_items = nullptr;
     unsigned *d_counter = nullptr;
     int ntasks = 0;
+    int mode = -2;         // shared output kind of all items, or -2 (mixed)
     uint64_t out_bytes = 0;
     int grid = 0;
+    bool split = false;    // some tasks are chunks of split requests
+    int64_t chunk = 0;     // chunk length used when splitting
+    void *d_stage = nullptr;
+    int32_t *d_stage_streams = nullptr;
+    int nstage = 0;
     cudaGraphExec_t exec = nullptr;
     void *graph_out = nullptr;
     ~mtgp_gpu_plan() {
         if (exec) cudaGraphExecDestroy(exec);
+        cudaFree(d_stage);
+        cudaFree(d_stage_streams);
         cudaFree(d_tasks);
         cudaFree(d_items);
         cudaFree(d_counter);
@@ -556,6 +605,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     // group by stream, keeping the caller's order within a stream
     std::vector<std::vector<int>> by(P.count);
     uint64_t out_bytes = 0;
+    int mode = -3;  // -3: no item yet
     for (int k = 0; k < nitems; k++) {
         const mtgp_work_item_t &it = items[k];
         if (it.stream >= (uint32_t)P.count)
@@ -565,43 +615,109 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         if (it.kind >= 0 && it.out_offset % sizeof(W))
             return setErr(MTGP_ERR_INVALID, "item %d: offset not a multiple of %zu", k, sizeof(W));
         if (it.count == 0) continue;
+        mode = (mode == -3 || mode == it.kind) ? it.kind : -2;
         by[it.stream].push_back(k);
         if (it.kind >= 0) out_bytes = std::max(out_bytes, it.out_offset + it.count * sizeof(W));
     }
-    struct Tk { int stream; uint64_t total; };
+    // One task per stream (its items in order), then split the long
+    // single-item tasks into chunks (see batch_kernels.cu).
+    struct Tk {
+        BatchTask t;
+        std::vector<BatchItem> items;
+        uint64_t total;
+    };
     std::vector<Tk> order;
+    uint64_t grand = 0;
     for (int s = 0; s < P.count; s++) {
         if (by[s].empty()) continue;
-        uint64_t tot = 0;
-        for (int k : by[s]) tot += items[k].count;
-        order.push_back({s, tot});
-    }
-    // longest task first
-    std::stable_sort(order.begin(), order.end(), [](const Tk &a, const Tk &b) { return a.total > b.total; });
-    std::vector<BatchTask> tasks;
-    std::vector<BatchItem> bitems;
-    for (const Tk &t : order) {
-        BatchTask bt{};
-        bt.stream = t.stream;
-        bt.first = (int)bitems.size();
-        bt.nitems = (int)by[t.stream].size();
-        bt.pidx = P.hpidx[t.stream];
-        for (int k : by[t.stream]) {
+        Tk tk{};
+        tk.t.stream = s;
+        tk.t.nitems = (int)by[s].size();
+        tk.t.pidx = P.hpidx[s];
+        tk.t.jpoly = nullptr;
+        tk.t.wb = kWbStream;
+        for (int k : by[s]) {
             BatchItem bi{};
             bi.out_off = items[k].out_offset;
             bi.count = items[k].count;
             bi.kind = items[k].kind;
-            bitems.push_back(bi);
+            tk.items.push_back(bi);
+            tk.total += items[k].count;
         }
-        tasks.push_back(bt);
+        grand += tk.total;
+        order.push_back(std::move(tk));
+    }
+    int64_t chunk = 0;
+    if (g_tune.split_chunk > 0) {
+        chunk = g_tune.split_chunk;
+    } else if (g_tune.split_chunk == 0 && T::splits(P.sh.mexp)) {
+        if (!P.resident) P.resident = T::resident(P.sh.mexp);
+        const uint64_t per = grand / (uint64_t)std::max(P.resident, 1);
+        chunk = 1 << 17;
+        while ((uint64_t)chunk < per) chunk <<= 1;
+    }
+    std::vector<int32_t> stage_streams;
+    bool split = false;
+    if (chunk > 0 && T::splits(P.sh.mexp)) {
+        std::vector<Tk> out;
+        for (Tk &tk : order) {
+            if (tk.t.nitems != 1 || tk.total <= (uint64_t)chunk + (uint64_t)chunk / 4) {
+                out.push_back(std::move(tk));
+                continue;
+            }
+            const BatchItem it = tk.items[0];
+            const uint64_t k = (it.count + chunk - 1) / chunk;
+            for (uint64_t c = 0; c < k; c++) {
+                Tk ch{};
+                ch.t = tk.t;
+                const uint64_t off = c * (uint64_t)chunk;
+                BatchItem bi = it;
+                bi.count = std::min<uint64_t>((uint64_t)chunk, it.count - off);
+                if (it.kind >= 0) bi.out_off = it.out_off + off * sizeof(W);
+                ch.items.push_back(bi);
+                ch.total = bi.count;
+                if (c > 0) {
+                    int rc = P.jumpPoly(tk.t.pidx, off, &ch.t.jpoly);
+                    if (rc) return rc;
+                }
+                ch.t.wb = (c + 1 == k) ? (int32_t)stage_streams.size() : kWbNone;
+                out.push_back(std::move(ch));
+            }
+            stage_streams.push_back(tk.t.stream);
+            split = true;
+        }
+        order.swap(out);
+    }
+    // longest task first
+    std::stable_sort(order.begin(), order.end(),
+                     [](const Tk &a, const Tk &b) { return a.total > b.total; });
+    std::vector<BatchTask> tasks;
+    std::vector<BatchItem> bitems;
+    for (Tk &tk : order) {
+        tk.t.first = (int)bitems.size();
+        tk.t.nitems = (int)tk.items.size();
+        for (const BatchItem &bi : tk.items) bitems.push_back(bi);
+        tasks.push_back(tk.t);
     }
     mtgp_gpu_plan *pl = new (std::nothrow) mtgp_gpu_plan();
     if (!pl) return setErr(MTGP_ERR_ALLOC, "plan allocation");
     pl->bits = T::kBits;
     pl->pool = &P;
     pl->ntasks = (int)tasks.size();
+    pl->mode = mode == -3 ? -1 : mode;
     pl->out_bytes = out_bytes;
+    pl->grid = (int)g_tune.batch_grid;
+    pl->split = split;
+    pl->chunk = split ? chunk : 0;
+    pl->nstage = (int)stage_streams.size();
     cudaError_t e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
+    if (e == cudaSuccess && pl->nstage) {
+        e = cudaMalloc(&pl->d_stage, sizeof(W) * (size_t)P.stride * pl->nstage);
+        if (e == cudaSuccess) e = cudaMalloc(&pl->d_stage_streams, sizeof(int32_t) * pl->nstage);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(pl->d_stage_streams, stage_streams.data(),
+                           sizeof(int32_t) * pl->nstage, cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess && !tasks.empty()) e = cudaMalloc(&pl->d_tasks, sizeof(BatchTask) * tasks.size());
     if (e == cudaSuccess && !bitems.empty()) e = cudaMalloc(&pl->d_items, sizeof(BatchItem) * bitems.size());
     if (e == cudaSuccess && !tasks.empty())
@@ -621,9 +737,21 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     Pool<T> &P = *static_cast<Pool<T> *>(pl->pool);
     if (pl->ntasks == 0) return MTGP_OK;
     if (pl->out_bytes && !out) return setErr(MTGP_ERR_INVALID, "null output pointer");
-    CK(T::batch(P.sh.mexp, P.d_params, P.d_states, pl->d_tasks, pl->ntasks, pl->d_items, out,
-                pl->d_counter, pl->grid, S(s)),
-       "batched launch");
+    BatchLaunch b{};
+    b.mexp = P.sh.mexp;
+    b.mode = pl->mode;
+    b.grid = pl->grid;
+    b.split = pl->split;
+    b.nwords = P.polyWords();
+    b.tasks = pl->d_tasks;
+    b.ntasks = pl->ntasks;
+    b.items = pl->d_items;
+    b.out = out;
+    b.counter = pl->d_counter;
+    b.stage = pl->d_stage;
+    b.stage_streams = pl->d_stage_streams;
+    b.nstage = pl->nstage;
+    CK(T::batch(b, P.d_params, P.d_states, S(s)), "batched launch");
     return MTGP_OK;
 }
 
@@ -958,6 +1086,26 @@ int mtgp_gpu_plan_graph_launch(mtgp_gpu_plan_t *pl, void *out, void *s) {
 }
 
 uint64_t mtgp_gpu_plan_output_bytes(const mtgp_gpu_plan_t *pl) { return pl ? pl->out_bytes : 0; }
+
+int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *pl, int64_t *tasks, int64_t *chunk) {
+    if (!pl) return setErr(MTGP_ERR_INVALID, "null plan");
+    if (tasks) *tasks = pl->ntasks;
+    if (chunk) *chunk = pl->chunk;
+    return MTGP_OK;
+}
+
+int mtgp_gpu_set_tuning(const char *key, int64_t value) {
+    if (!key) return setErr(MTGP_ERR_INVALID, "null key");
+    if (!std::strcmp(key, "split_chunk")) {
+        g_tune.split_chunk = value;
+    } else if (!std::strcmp(key, "batch_grid")) {
+        if (value < 0) return setErr(MTGP_ERR_INVALID, "batch_grid must be >= 0");
+        g_tune.batch_grid = value;
+    } else {
+        return setErr(MTGP_ERR_INVALID, "unknown tuning key '%s'", key);
+    }
+    return MTGP_OK;
+}
 
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *pl) {
     if (!pl) return;

@@ -40,11 +40,18 @@ struct DevParams64 {
 
 // Shape of one supported Mersenne exponent: N live words, TN parallel lanes
 // (threads per generator; the reference guarantees size - pos > TN,
-// mtgp32-fast.h:96-106), RING = shared-memory ring length (power of two,
-// >= N + TN so one sub-step's reads and writes never alias).
+// mtgp32-fast.h:96-106), B = words of the generation core's shared buffer
+// (at most 48 KB, so static shared memory suffices).
 struct Shape {
-    int mexp, n, tn, ring;
+    int mexp, n, tn, buf;
 };
+// Per exponent: live words N, lanes TN (threads per generator; N - pos >= TN
+// for every set of the reference's tables), and the shared buffer B (words)
+// of the generation core (B <= 48 KB, so static shared memory suffices).
+#define MTGP_SHAPES32(X) X(11213, 351, 256, 4096) X(23209, 726, 512, 8192) X(44497, 1391, 1024, 12000)
+#define MTGP_SHAPES64(X) X(11213, 176, 128, 2048) X(23209, 363, 256, 4096) X(44497, 696, 512, 4096) \
+    X(110503, 1727, 512, 5760)
+
 
 bool shape32(int mexp, Shape *s);
 bool shape64(int mexp, Shape *s);

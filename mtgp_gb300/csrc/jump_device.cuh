@@ -1,0 +1,167 @@
+// jump_device.cuh -- GF(2) jump-ahead of one window inside a CTA.
+//
+// The reference jumps a state by a polynomial p(X) = sum c_i X^i
+// (mtgp32-fast-jump.c:51-79): it walks the coefficients, XOR-accumulating
+// the whole state after i steps whenever c_i = 1.  With seq = the live
+// window followed by the raw recursion words, the state after i steps is
+// seq[i .. i+N), so the jumped window is the correlation
+//
+//     J[l] = XOR_{i : c_i = 1} seq[i + l],      l = 0 .. N-1,
+//
+// bit-identical to the reference's result (word 0 included).  One CTA of NT
+// threads computes it:
+//   - seq is produced chunk by chunk in a shared ring by the parallel
+//     recursion (GW words per sub-step, GW <= the shape's lanes);
+//   - each chunk's taps are split over the warps; lane l of a warp owns R
+//     consecutive outputs and slides an R-word register window along seq,
+//     so a tap costs one shared load and R masked XORs;
+//   - the warps' partial sums are combined with shared-memory atomicXor.
+// A chain of polynomials is applied in order.
+#pragma once
+#include "mtgp_device.cuh"
+
+namespace mtgp {
+
+struct Tr32 {
+    using W = uint32_t;
+    using P = DevParams32;
+    using Lane = Lane32;
+    __device__ static __forceinline__ W rec(W x1, W x2, W y, const Lane &L) {
+        uint32_t yy = rec32_pre(x1, x2, y, L.mask, L.sh1, L.sh2);
+        return yy ^ lut(L.tbl, yy);
+    }
+    __device__ static __forceinline__ W andm(W v, uint32_t m) { return v & m; }
+    __device__ static __forceinline__ void axor(W *p, W v) { atomicXor(p, v); }
+};
+
+struct Tr64 {
+    using W = uint64_t;
+    using P = DevParams64;
+    using Lane = Lane64;
+    __device__ static __forceinline__ W rec(W x1, W x2, W y, const Lane &L) {
+        uint64_t yy = rec64_pre(x1, x2, y, L.mask, L.sh1, L.sh2);
+        return yy ^ lut64(L.tbl_lo, L.tbl_hi, (uint32_t)yy);
+    }
+    __device__ static __forceinline__ W andm(W v, uint32_t m) {
+        return v & (uint64_t)(int64_t)(int32_t)m;
+    }
+    __device__ static __forceinline__ void axor(W *p, W v) {
+        atomicXor(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+    }
+};
+
+// Geometry of one jump instance.
+//   N    live words          R    outputs per lane (odd: conflict-free loads)
+//   NT   threads of the CTA  GW   words per recursion sub-step (<= NT, <= lanes)
+//   RING shared ring length (power of two)
+// Shared layout, in words W: jin[NJ] | jout[NJ] | ring[RING] | poly (uint32).
+template <int N_, int R_, int NT_, int GW_, int RING_>
+struct JGeo {
+    static constexpr int N = N_, R = R_, NT = NT_, GW = GW_, RING = RING_;
+    static constexpr int NWARP = NT / 32;
+    static_assert(NT % 32 == 0 && GW % 32 == 0 && GW <= NT, "bad jump widths");
+    static_assert(R <= 64, "coefficient extraction handles up to 64 taps");
+    static constexpr int G = (N + 32 * R - 1) / (32 * R);  // output groups (passes)
+    static constexpr int TPW = R * ((128 + R - 1) / R);    // taps per warp per chunk
+    static constexpr int C = NWARP * TPW;                  // taps per chunk
+    static constexpr int NJ = (N + 3) & ~3;
+    static constexpr int PAD = C / 32 + 4;                 // zero words after the poly
+    static_assert(C + N + GW <= RING, "jump ring too small");
+    template <typename W>
+    __host__ __device__ static constexpr size_t bytes(int nwords) {
+        return sizeof(W) * (size_t)(2 * NJ + RING) + sizeof(uint32_t) * (size_t)(nwords + PAD);
+    }
+};
+
+// Jump the window jin[0..N) in place by chain[0], chain[1], ... (uint32-array
+// polynomials of nwords words).  smem must hold Geo::bytes<W>(nwords) bytes
+// laid out as described above (jin first).  All NT threads must call it; it
+// begins and ends with a barrier.
+template <class Tr, class Geo, class ChainAt>
+__device__ __forceinline__ void jump_chain_impl(typename Tr::W *smem, const typename Tr::Lane &L,
+                                                ChainAt chain, int nchain, int nwords) {
+    using W = typename Tr::W;
+    constexpr int N = Geo::N, R = Geo::R, NT = Geo::NT;
+    constexpr uint32_t M = Geo::RING - 1;
+    W *jin = smem;
+    W *jout = jin + Geo::NJ;
+    W *ring = jout + Geo::NJ;
+    uint32_t *poly = reinterpret_cast<uint32_t *>(ring + Geo::RING);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int taps = nwords * 32;
+    const int pwords = nwords + Geo::PAD;
+    __syncthreads();
+
+    for (int c = 0; c < nchain; c++) {
+        const uint32_t *pg = chain(c);
+        for (int k = tid; k < pwords; k += NT) poly[k] = k < nwords ? pg[k] : 0u;
+        for (int k = tid; k < N; k += NT) jout[k] = 0;
+        for (int g = 0; g < Geo::G; g++) {
+            for (int k = tid; k < N; k += NT) ring[k] = jin[k];
+            __syncthreads();
+            int generated = N;
+            const int l0 = g * 32 * R + lane * R;
+            W acc[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = 0;
+            for (int cs = 0; cs < taps; cs += Geo::C) {
+                // extend seq so that it covers every tap/output of this chunk
+                while (generated < cs + Geo::C + N) {
+                    if (tid < Geo::GW) {  // whole warps: the table shuffle needs all lanes
+                        uint32_t w = (uint32_t)(generated + tid);
+                        W x1 = ring[(w - N) & M];
+                        W x2 = ring[(w - N + 1) & M];
+                        W y = ring[(w - N + L.pos) & M];
+                        ring[w & M] = Tr::rec(x1, x2, y, L);
+                    }
+                    __syncthreads();
+                    generated += Geo::GW;
+                }
+                // this warp's taps: [i0, i0 + TPW)
+                const int i0 = cs + warp * Geo::TPW;
+                W win[R];
+#pragma unroll
+                for (int r = 0; r < R; r++) win[r] = ring[(uint32_t)(i0 + l0 + r) & M];
+                for (int jb = 0; jb < Geo::TPW; jb += R) {
+                    const int p = i0 + jb;
+                    // coefficient bits of taps p .. p+R-1 (R <= 64)
+                    const uint32_t bits_lo =
+                        __funnelshift_r(poly[p >> 5], poly[(p >> 5) + 1], p & 31);
+                    const uint32_t bits_hi =
+                        R > 32 ? __funnelshift_r(poly[(p >> 5) + 1], poly[(p >> 5) + 2], p & 31)
+                               : 0u;
+#pragma unroll
+                    for (int j = 0; j < R; j++) {
+                        const uint32_t bj = j < 32 ? bits_lo : bits_hi;
+                        const uint32_t m = (uint32_t)((int32_t)(bj << (31 - (j & 31))) >> 31);
+#pragma unroll
+                        for (int r = 0; r < R; r++) acc[r] ^= Tr::andm(win[(j + r) % R], m);
+                        win[j] = ring[(uint32_t)(p + l0 + R + j) & M];
+                    }
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                if (l0 + r < N) Tr::axor(&jout[l0 + r], acc[r]);
+            __syncthreads();
+        }
+        for (int k = tid; k < N; k += NT) jin[k] = jout[k];
+        __syncthreads();
+    }
+}
+
+template <class Tr, class Geo>
+__device__ void jump_chain(typename Tr::W *smem, const typename Tr::Lane &L,
+                           const uint32_t *const *chain, int nchain, int nwords) {
+    jump_chain_impl<Tr, Geo>(smem, L, [chain](int c) { return chain[c]; }, nchain, nwords);
+}
+
+// One polynomial.
+template <class Tr, class Geo>
+__device__ void jump_one(typename Tr::W *smem, const typename Tr::Lane &L, const uint32_t *poly,
+                         int nwords) {
+    jump_chain_impl<Tr, Geo>(smem, L, [poly](int) { return poly; }, 1, nwords);
+}
+
+}  // namespace mtgp

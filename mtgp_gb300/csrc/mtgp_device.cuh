@@ -142,57 +142,140 @@ __device__ __forceinline__ uint64_t rec64_pre(uint64_t x1, uint64_t x2,
     return ((uint64_t)yh << 32) | yl;
 }
 
-// Advance one generator by n steps inside a CTA of TN threads.
-//   ring   : shared ring of RING words; on entry the window (oldest first)
-//            is at ring[(phase + k) & (RING-1)], k < N.
-//   otab   : lane value of the output table (Lane32::otab(KIND)).
-//   out    : n outputs of KIND (ignored when KIND < 0: skip).
-// On exit the window is at ring[(phase + n + k) & (RING-1)].
-// All TN threads must call it (warp shuffles and barriers inside).
-template <int N, int TN, int RING, int KIND>
-__device__ __forceinline__ void run32(uint32_t *ring, const Lane32 &L, uint32_t otab,
-                                      uint32_t phase, uint64_t n,
-                                      typename Out32<(KIND < 0 ? 0 : KIND)>::T *out) {
-    constexpr uint32_t M = RING - 1;
-    const uint32_t t = threadIdx.x;
-    uint32_t w = phase + t;  // ring index of x1 for this thread
-    for (uint64_t base = 0; base < n; base += TN, w += TN) {
-        uint32_t x1 = ring[w & M];
-        uint32_t x2 = ring[(w + 1) & M];
-        uint32_t y = ring[(w + L.pos) & M];
-        uint32_t yy = rec32_pre(x1, x2, y, L.mask, L.sh1, L.sh2);
-        uint32_t r = yy ^ lut(L.tbl, yy);
-        ring[(w + N) & M] = r;
-        if constexpr (KIND >= 0) {
-            uint32_t tt = ring[(w + L.pos - 1) & M];
-            uint32_t o = lut(otab, fold(tt));
-            if (base + t < n) out[base + t] = Out32<KIND>::conv(r, o);
-        }
-        __syncthreads();
+// Generation core: advance one generator by n steps inside a CTA of TN
+// threads.
+//
+// The state lives in a linear shared buffer of B words.  On entry and on
+// exit the window (oldest word first) is at buf[0 .. N).  A segment of S
+// sub-steps appends S*TN words behind it (sub-step k, thread t reads words
+// kTN+t, +1, +pos-1, +pos and writes word kTN+t+N); then the newest N words
+// are copied back to buf[0 .. N) ("compaction").  Inside a segment every
+// shared and global address is a per-thread base plus a compile-time
+// offset, so the unrolled segment does no index arithmetic at all; the
+// price is copying N words every S*TN outputs (351 per 3584 for MEXP 11213).
+//
+// x << sh1 is computed as x * 2^sh1 so that it issues on the FMA pipe rather
+// than the ALU pipe.
+template <int N, int TN, int B>
+struct Seg {
+    static constexpr int S = (B - N - TN) / TN + 1;  // sub-steps per segment
+    static_assert(S >= 2 && S * TN >= N && S * TN + N <= B, "bad segment geometry");
+};
+
+// Copy buf[src .. src+N) to buf[0 .. N) (regions may overlap); all TN
+// threads; ends with a barrier.
+template <typename W, int N, int TN>
+__device__ __forceinline__ void compact(W *buf, uint32_t src) {
+    constexpr int PER = (N + TN - 1) / TN;
+    W v[PER];
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        int k = threadIdx.x + i * TN;
+        if (k < N) v[i] = buf[src + k];
     }
+    if (src < (uint32_t)N) __syncthreads();
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        int k = threadIdx.x + i * TN;
+        if (k < N) buf[k] = v[i];
+    }
+    __syncthreads();
 }
 
-template <int N, int TN, int RING, int KIND>
-__device__ __forceinline__ void run64(uint64_t *ring, const Lane64 &L, uint32_t otab_lo,
-                                      uint32_t otab_hi, uint32_t phase, uint64_t n,
-                                      typename Out64<(KIND < 0 ? 0 : KIND)>::T *out) {
-    constexpr uint32_t M = RING - 1;
-    const uint32_t t = threadIdx.x;
-    uint32_t w = phase + t;
-    for (uint64_t base = 0; base < n; base += TN, w += TN) {
-        uint64_t x1 = ring[w & M];
-        uint64_t x2 = ring[(w + 1) & M];
-        uint64_t y = ring[(w + L.pos) & M];
-        uint64_t yy = rec64_pre(x1, x2, y, L.mask, L.sh1, L.sh2);
-        uint64_t r = yy ^ lut64(L.tbl_lo, L.tbl_hi, (uint32_t)yy);
-        ring[(w + N) & M] = r;
-        if constexpr (KIND >= 0) {
-            uint64_t tt = ring[(w + L.pos - 1) & M];
-            uint64_t o = lut64(otab_lo, otab_hi, fold((uint32_t)tt));
-            if (base + t < n) out[base + t] = Out64<KIND>::conv(r, o);
-        }
-        __syncthreads();
+// One sub-step for 32-bit words.  px = buf + base + t, py = px + pos.
+template <int N, int TN, int KIND, bool GUARD>
+__device__ __forceinline__ void sub32(uint32_t *px, const Lane32 &L, uint32_t mul1,
+                                      uint32_t otab,
+                                      typename Out32<(KIND < 0 ? 0 : KIND)>::T *o,
+                                      bool live) {
+    const uint32_t *py = px + L.pos;
+    uint32_t x1 = px[0], x2 = px[1], y = py[0];
+    uint32_t x = (x1 & L.mask) ^ x2;
+    uint32_t yy = x ^ (x * mul1) ^ (y >> L.sh2);
+    uint32_t r = yy ^ lut(L.tbl, yy);
+    px[N] = r;
+    if constexpr (KIND >= 0) {
+        uint32_t tt = py[-1];
+        uint32_t ov = lut(otab, fold(tt));
+        if (!GUARD || live) *o = Out32<KIND>::conv(r, ov);
     }
+    __syncthreads();
+}
+
+template <int N, int TN, int KIND, bool GUARD>
+__device__ __forceinline__ void sub64(uint64_t *px, const Lane64 &L, uint32_t mul1,
+                                      uint32_t olo, uint32_t ohi,
+                                      typename Out64<(KIND < 0 ? 0 : KIND)>::T *o,
+                                      bool live) {
+    const uint64_t *py = px + L.pos;
+    uint64_t x1 = px[0], x2 = px[1], y = py[0];
+    uint64_t x = (x1 & L.mask) ^ x2;
+    uint32_t xh = (uint32_t)(x >> 32), xl = (uint32_t)x;
+    uint32_t yh = (uint32_t)(y >> 32), yl = (uint32_t)y;
+    xh ^= xh * mul1;
+    xl ^= xl * mul1;
+    yh = xl ^ (yh >> L.sh2);
+    yl = xh ^ (yl >> L.sh2);
+    uint64_t r = (((uint64_t)yh << 32) | yl) ^ lut64(L.tbl_lo, L.tbl_hi, yl);
+    px[N] = r;
+    if constexpr (KIND >= 0) {
+        uint64_t tt = py[-1];
+        uint64_t ov = lut64(olo, ohi, fold((uint32_t)tt));
+        if (!GUARD || live) *o = Out64<KIND>::conv(r, ov);
+    }
+    __syncthreads();
+}
+
+// Advance by n steps writing n outputs of KIND (KIND < 0: no output).
+// otab*: lane value of the output table (Lane32::otab(KIND)).
+template <int N, int TN, int B, int KIND>
+__device__ __forceinline__ void run32(uint32_t *buf, const Lane32 &L, uint32_t otab,
+                                      uint64_t n,
+                                      typename Out32<(KIND < 0 ? 0 : KIND)>::T *out) {
+    constexpr int S = Seg<N, TN, B>::S;
+    const int t = threadIdx.x;
+    const uint32_t mul1 = 1u << L.sh1;
+    uint32_t *px = buf + t;
+    auto *o = out + t;
+    while (n >= (uint64_t)S * TN) {
+#pragma unroll
+        for (int k = 0; k < S; k++)
+            sub32<N, TN, KIND, false>(px + k * TN, L, mul1, otab, o + k * TN, true);
+        compact<uint32_t, N, TN>(buf, S * TN);
+        n -= (uint64_t)S * TN;
+        if constexpr (KIND >= 0) o += S * TN;
+    }
+    const int rem = (int)n;  // < S*TN
+    if (rem == 0) return;
+    const int subs = (rem + TN - 1) / TN;
+    for (int k = 0; k < subs; k++)
+        sub32<N, TN, KIND, true>(px + k * TN, L, mul1, otab, o + k * TN, k * TN + t < rem);
+    compact<uint32_t, N, TN>(buf, (uint32_t)rem);
+}
+
+template <int N, int TN, int B, int KIND>
+__device__ __forceinline__ void run64(uint64_t *buf, const Lane64 &L, uint32_t olo,
+                                      uint32_t ohi, uint64_t n,
+                                      typename Out64<(KIND < 0 ? 0 : KIND)>::T *out) {
+    constexpr int S = Seg<N, TN, B>::S;
+    const int t = threadIdx.x;
+    const uint32_t mul1 = 1u << L.sh1;
+    uint64_t *px = buf + t;
+    auto *o = out + t;
+    while (n >= (uint64_t)S * TN) {
+#pragma unroll
+        for (int k = 0; k < S; k++)
+            sub64<N, TN, KIND, false>(px + k * TN, L, mul1, olo, ohi, o + k * TN, true);
+        compact<uint64_t, N, TN>(buf, S * TN);
+        n -= (uint64_t)S * TN;
+        if constexpr (KIND >= 0) o += S * TN;
+    }
+    const int rem = (int)n;
+    if (rem == 0) return;
+    const int subs = (rem + TN - 1) / TN;
+    for (int k = 0; k < subs; k++)
+        sub64<N, TN, KIND, true>(px + k * TN, L, mul1, olo, ohi, o + k * TN, k * TN + t < rem);
+    compact<uint64_t, N, TN>(buf, (uint32_t)rem);
 }
 
 }  // namespace mtgp

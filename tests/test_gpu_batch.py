@@ -125,3 +125,80 @@ def test_batch_rejects_bad_items(gpu):
         pool.plan(work_items([0], [0], [10], [2]))
     with pytest.raises(MTGPError):
         pool.plan(work_items([0], [7], [10], [0]))
+
+
+@pytest.mark.parametrize("bits,table", [(32, "mtgp32_fast_11213"), (64, "mtgp64dc_fast_11213"),
+                                        (32, "mtgp32_fast_23209"), (64, "mtgp64_fast_23209")])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_batch_split_long_requests(gpu, orc, bits, table, mixed):
+    """Long requests split into chunks whose start states are GF(2) jumps
+    done inside the batched kernel: bit-exact outputs and final states,
+    across two launches of the same plan."""
+    from mtgp_gb300.api import Pool, set_tuning, work_items
+    tbl = load_table(table)
+    rng = np.random.default_rng(bits + mixed + tbl[0].mexp)
+    nstreams = 24
+    plist = [tbl[i] for i in range(3)]
+    pidx = np.arange(nstreams) % 3
+    seeds = np.arange(nstreams) + 7
+    pool = Pool.create(plist, seeds, pidx)
+    counts = rng.integers(1, 30000, nstreams)
+    counts[:4] = [1, 1499, 1875, 30001]
+    kinds = rng.integers(0, 5, nstreams) if mixed else np.zeros(nstreams, np.int64)
+    esz = bits // 8
+    offs = np.concatenate([[0], np.cumsum(counts)[:-1]]) * esz
+    # one stream gets two items (a multi-item task is never split)
+    streams = list(range(nstreams)) + [5]
+    kinds = list(kinds) + [0]
+    counts = list(counts) + [20000]
+    offs = list(offs) + [int(sum(counts[:-1])) * esz]
+    set_tuning("split_chunk", 1500)
+    try:
+        plan = pool.plan(work_items(streams, kinds, counts, offs))
+    finally:
+        set_tuning("split_chunk", 0)
+    ntasks, chunk = plan.info()
+    assert chunk == 1500 and ntasks > nstreams
+    out = torch.zeros(int(sum(counts)) * esz // 4 + 16, dtype=torch.int32, device="cuda")
+    gens = {s: orc.gen(plist[pidx[s]], seed=int(seeds[s])) for s in range(nstreams)}
+    for rep in range(2):
+        plan.launch(out)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().view(np.uint8)
+        for k in range(len(streams)):
+            ref = np_bits(gens[streams[k]].fill(int(kinds[k]), int(counts[k])), bits).view(np.uint8)
+            assert np.array_equal(got[offs[k]:offs[k] + ref.size], ref), (rep, k)
+        w = pool.windows()
+        for s in range(nstreams):
+            assert np.array_equal(w[s], gens[s].window()), (rep, s)
+
+
+def test_batch_split_graph(gpu, orc):
+    """The split plan (batched kernel + staged-window copy) replays from a
+    CUDA graph."""
+    from mtgp_gb300.api import Pool, set_tuning, work_items
+    p = load_table("mtgp32_fast_11213")[0]
+    pool = Pool.substreams(p, 1234, 16, jump_table(32))
+    counts = np.array([100000, 5, 70000, 4096] + [3000] * 12)
+    offs = np.concatenate([[0], np.cumsum(counts)[:-1]]) * 4
+    set_tuning("split_chunk", 16384)
+    try:
+        plan = pool.plan(work_items(np.arange(16), np.zeros(16), counts, offs))
+    finally:
+        set_tuning("split_chunk", 0)
+    assert plan.info()[1] == 16384
+    start = pool.windows()
+    out = torch.zeros(int(counts.sum()), dtype=torch.int32, device="cuda")
+    s = torch.cuda.Stream()
+    gens = []
+    for j in range(16):
+        o = orc.gen(p, seed=1234)
+        o.set_window(start[j])
+        gens.append(o)
+    for rep in range(3):
+        plan.graph_launch(out, s)
+        s.synchronize()
+        got = out.cpu().numpy().view(np.uint32)
+        for j in range(16):
+            a = int(offs[j]) // 4
+            assert np.array_equal(got[a:a + int(counts[j])], gens[j].fill(0, int(counts[j]))), (rep, j)
