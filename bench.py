@@ -199,6 +199,11 @@ def main():
                     help="substreams of the batched workload (profiling runs use fewer)")
     ap.add_argument("--only", default="all", choices=["all", "batched", "bank"],
                     help="profiling runs: time only one path, no e2e / plain / CPU legs")
+    ap.add_argument("--uniform", type=int, default=0,
+                    help="profiling runs: every substream requests this many values "
+                         "(steady-state throughput instead of the lognormal workload)")
+    ap.add_argument("--tune", action="append", default=[],
+                    help="key=value tuning knob (split_chunk, batch_grid)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -219,12 +224,15 @@ def main():
 
     from mtgp_gb300 import build as b
     b.build()
-    from mtgp_gb300.api import Pool, work_items
+    from mtgp_gb300.api import Pool, set_tuning, work_items
+    for kv in args.tune:
+        k, v = kv.split("=")
+        set_tuning(k, int(v))
     from mtgp_gb300.params import jump_table, load_table
 
     p = load_table("mtgp32_fast_11213")[0]
     nsub = args.substreams
-    lens = lengths()[:nsub]
+    lens = lengths()[:nsub] if args.uniform <= 0 else np.full(nsub, args.uniform, np.int64)
     offs = np.concatenate([[0], np.cumsum(lens)[:-1]]) * 4
     total_bytes = int(lens.sum()) * 4
     s = torch.cuda.Stream()
