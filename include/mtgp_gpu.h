@@ -335,6 +335,33 @@ int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *plan, int64_t *tasks,
 int mtgp_gpu_set_tuning(const char *key, int64_t value);
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
 
+/* ========================================================================= */
+/* Batched generation without any allocation                                  */
+/* ========================================================================= */
+/* For callers that cannot allocate device memory: engines whose device memory
+ * is all reserved up front in their own arena or under a hard budget, and
+ * plug-ins that may only use the buffers a host application hands them.  No
+ * counterpart in the reference.
+ *
+ * The caller passes the stream windows and the output.  dev_windows holds
+ * nstreams windows (MEXP 11213/23209/44497), each mexp/32+1 words oldest word
+ * first, at a stride of roundup(mexp/32+1, 32) words; they are advanced in
+ * place.  Stream s uses params[param_idx ? param_idx[s] : s] (or params[0]
+ * when nparams != nstreams).  Items follow mtgp32_gpu_pool_submit's rules,
+ * without long-request splitting.  The kernel's descriptors go into one
+ * fixed array in device memory inside the library (about 116 KB, held by
+ * every GPU that loads the library until the process exits): at most 16
+ * parameter sets and 2048 items per call, larger requests are rejected with
+ * MTGP_ERR_INVALID.  The first call on a device looks up the array's device
+ * address, so it should come before any stream capture.  Every call
+ * overwrites the array: calls whose GPU work overlaps (other streams, other
+ * host threads) race and must be serialised by the caller.  The call returns
+ * once the descriptors are uploaded; generation runs on `stream`. */
+int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
+                             const int *param_idx, uint32_t *dev_windows,
+                             int nstreams, const mtgp_work_item_t *items,
+                             int nitems, void *dev_out, void *stream);
+
 #if defined(__cplusplus)
 }
 #endif

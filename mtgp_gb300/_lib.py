@@ -40,6 +40,7 @@ SIGS = {
     "mtgp_gpu_plan_free": (None, [vp]),
     "mtgp_gpu_plan_info": (c_int, [vp, vp, vp]),
     "mtgp_gpu_set_tuning": (c_int, [cp, ctypes.c_int64]),
+    "mtgp32_gpu_batch_noalloc": (c_int, [P32, c_int, vp, vp, c_int, vp, c_int, vp, vp]),
 }
 for B, P, W in ((32, P32, c_u32), (64, P64, c_u64)):
     pre = "mtgp%d_gpu_" % B

@@ -60,6 +60,12 @@ int setErr(int code, const char *fmt, ...) {
     return code;
 }
 
+}  // namespace
+
+int mtgp::recordError(int code, const char *msg) { return setErr(code, "%s", msg); }
+
+namespace {
+
 int cudaErr(cudaError_t e, const char *what) {
     return setErr(MTGP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }

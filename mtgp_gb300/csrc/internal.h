@@ -58,6 +58,8 @@ bool shape64(int mexp, Shape *s);
 __host__ __device__ constexpr int stateStride(int n) { return (n + 31) & ~31; }
 
 void toDev(const mtgp32_params_fast_t &p, DevParams32 *d);
+// Store msg as the calling thread's mtgp_gpu_last_error(); returns code.
+int recordError(int code, const char *msg);
 void toDev(const mtgp64_params_fast_t &p, DevParams64 *d);
 
 // ---- generation (gen_kernels.cu) ----------------------------------------
