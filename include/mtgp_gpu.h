@@ -316,6 +316,21 @@ int mtgp64_gpu_pool_set_windows_host(mtgp64_gpu_pool_t *p,
                                      const uint64_t *win, size_t nwords);
 int mtgp64_gpu_pool_export(mtgp64_gpu_pool_t *p, int s, mtgp64_fast_t *dst);
 
+/* Autotuner (no reference counterpart): builds a plan for each candidate
+ * configuration -- generation core (four words per thread in 64-thread CTAs
+ * with 128-bit stores, or one word per thread in 256-thread CTAs), the chunk
+ * length used to split long requests, and the grid size -- times each on
+ * these items and this output buffer (best of `reps` launches on `stream`),
+ * and returns the fastest.  The pool's windows are restored before every
+ * trial and at the end, so the pool is left unchanged.  `report` (optional)
+ * receives one line per candidate. */
+int mtgp32_gpu_pool_autotune(mtgp32_gpu_pool_t *p, const mtgp_work_item_t *items,
+                             int nitems, void *dev_out, void *stream, int reps,
+                             mtgp_gpu_plan_t **plan, char *report, int report_cap);
+int mtgp64_gpu_pool_autotune(mtgp64_gpu_pool_t *p, const mtgp_work_item_t *items,
+                             int nitems, void *dev_out, void *stream, int reps,
+                             mtgp_gpu_plan_t **plan, char *report, int report_cap);
+
 /* Launch a prepared batch (one persistent kernel).  Capturable. */
 int mtgp_gpu_plan_launch(mtgp_gpu_plan_t *plan, void *dev_out, void *stream);
 /* Same launch through a CUDA graph, captured on first use for this
@@ -331,7 +346,9 @@ int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *plan, int64_t *tasks,
 /* Process-wide tuning knobs for plans made afterwards (no reference
  * counterpart; the autotuner and tests use them):
  *   "split_chunk"  0 = automatic, < 0 = never split, > 0 = chunk length
- *   "batch_grid"   0 = one CTA per resident slot, > 0 = that many CTAs  */
+ *   "batch_grid"   0 = one CTA per resident slot, > 0 = that many CTAs
+ *   "core"         32-bit generation core for plans without split requests:
+ *                  4 = four adjacent words per thread (default), 1 = one */
 int mtgp_gpu_set_tuning(const char *key, int64_t value);
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
 

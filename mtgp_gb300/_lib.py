@@ -70,6 +70,7 @@ for B, P, W in ((32, P32, c_u32), (64, P64, c_u64)):
         pre + "pool_get_windows_host": (c_int, [vp, vp, c_size_t]),
         pre + "pool_set_windows_host": (c_int, [vp, vp, c_size_t]),
         pre + "pool_export": (c_int, [vp, c_int, vp]),
+        pre + "pool_autotune": (c_int, [vp, vp, c_int, vp, vp, c_int, pp, ctypes.c_char_p, c_int]),
     })
     kinds = ("uint%d" % B, "close1_open2", "close_open", "open_close", "open_open")
     for k in kinds:

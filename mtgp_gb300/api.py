@@ -257,6 +257,16 @@ class Pool:
         check(getattr(lib(), self.pre + "plan")(self.h, items, len(items), ctypes.byref(ph)))
         return Plan(ph, self)
 
+    def autotune(self, items, out, stream=None, reps=3):
+        """Fastest plan for these items on this output buffer (the pool's
+        windows are left unchanged); returns (plan, report text)."""
+        ph = ctypes.c_void_p()
+        buf = ctypes.create_string_buffer(8192)
+        check(getattr(lib(), self.pre + "autotune")(
+            self.h, items, len(items), ctypes.c_void_p(out.data_ptr()), _stream(stream), reps,
+            ctypes.byref(ph), buf, len(buf)))
+        return Plan(ph, self), buf.value.decode()
+
     def submit(self, items, out, stream=None):
         check(getattr(lib(), self.pre + "submit")(self.h, items, len(items),
                                                   ctypes.c_void_p(out.data_ptr()), _stream(stream)))

@@ -34,13 +34,14 @@ constexpr int32_t kWbNone = -2;
 // grid <= 0: size the grid to the resident-CTA capacity of the GPU.
 // mode: the output kind shared by every item (-1 = all skips), or -2 when
 // items mix kinds.
-// split: some tasks carry jpoly (kernel variant with the jump code).
-// stage / stage_streams / nstage: staged windows copied to their streams
-// after the launch (stage slot k -> stream stage_streams[k]).
+// One batched launch.  split: some tasks carry jpoly (the kernel variant
+// with the jump code runs).  After the kernel, staged final windows (stage
+// slot k -> stream stage_streams[k]) are copied back.
 struct BatchLaunch {
     int mexp, mode, grid;
+    int core;                       // 32-bit generation core (1 or 4) when not split
     bool split;
-    int nwords;                     // words of every jpoly
+    int nwords;                     // words of every jump polynomial
     const BatchTask *tasks;
     int ntasks;
     const BatchItem *items;
@@ -54,11 +55,11 @@ cudaError_t launchBatch32(const BatchLaunch &b, const DevParams32 *params, uint3
                           cudaStream_t s);
 cudaError_t launchBatch64(const BatchLaunch &b, const DevParams64 *params, uint64_t *states,
                           cudaStream_t s);
-// Whether the batched kernel of this exponent can split long requests.
+// Number of CTAs of the batched kernel resident at once on the device.
+int batchResident32(int mexp, bool split);
+int batchResident64(int mexp, bool split);
+// Whether split requests are supported for this exponent.
 bool batchSplits32(int mexp);
 bool batchSplits64(int mexp);
-// Number of CTAs of the batched kernel resident at once on the device.
-int batchResident32(int mexp);
-int batchResident64(int mexp);
 
 }  // namespace mtgp

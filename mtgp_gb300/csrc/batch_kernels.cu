@@ -6,16 +6,23 @@
 // order.  The grid is sized to the number of CTAs the GPU keeps resident;
 // each CTA takes the next task from a device counter (tasks are sorted
 // longest-first on the host, so the long ones start first), loads the
-// stream's window into shared memory, runs the items with the generation
-// core (mtgp_device.cuh), and writes the advanced window back.
+// stream's window into shared memory, runs the items with a generation core,
+// and writes the advanced window back.
 //
 // Long requests are split into chunks that run on different CTAs: chunk c
 // starts from the stream's window jumped ahead by its offset (X^off mod chi,
-// applied in the CTA with jump_device.cuh), and only the last chunk keeps
-// its final window, in a staging slot that a small kernel copies back after
-// the launch.
+// applied inside the chunk's CTA with jump_device.cuh).  The jump is
+// ALU-bound while generation is bound by the shared-memory data pipe, so the
+// jumps of some CTAs overlap the generation of the others.  Only the last
+// chunk keeps its final window, in a staging slot that k_unstage copies back
+// after the launch, so no chunk can read a window that another chunk has
+// already advanced.
+//
+// Plans without split requests use the four-words-per-thread core
+// (mtgp_device4.cuh) for 32-bit streams.
 #include "batch.h"
 #include "jump_device.cuh"
+#include "mtgp_device4.cuh"
 
 namespace mtgp {
 
@@ -23,21 +30,28 @@ namespace {
 
 // Jump geometry used inside the batched kernel (NT = the kernel's threads);
 // the jump's shared buffers alias the generation buffer.
-template <int N> struct SplitGeo32;
+template <int N> struct SplitGeo32 { using G = void; };
 template <> struct SplitGeo32<351> { using G = JGeo<351, 11, 256, 256, 2048>; };
 template <> struct SplitGeo32<726> { using G = JGeo<726, 23, 512, 512, 4096>; };
-template <int N> struct SplitGeo64;
+template <int N> struct SplitGeo64 { using G = void; };
 template <> struct SplitGeo64<176> { using G = JGeo<176, 7, 128, 128, 1024>; };
 template <> struct SplitGeo64<363> { using G = JGeo<363, 13, 256, 256, 2048>; };
 
 template <int N> constexpr bool kSplit32 = (N == 351 || N == 726);
 template <int N> constexpr bool kSplit64 = (N == 176 || N == 363);
 
+template <typename W>
+__device__ __forceinline__ W *endWindow(const BatchTask &T, W *states, W *stage, int stride) {
+    return T.wb == kWbStream ? states + (size_t)T.stream * stride
+         : T.wb >= 0         ? stage + (size_t)T.wb * stride
+                             : nullptr;
+}
+
 // MODE >= -1: every item has output kind MODE (-1 = skip); MODE == -2:
 // items of any kind (the kind is switched per item).  SPLIT: tasks may
 // carry a jump polynomial.
 template <int N, int TN, int B, int MODE, bool SPLIT>
-__global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1536 : 2048) / TN)
+__global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1280 : 2048) / TN)
 k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
@@ -58,6 +72,8 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
         if constexpr (SPLIT && kSplit32<N>) {
             using G = typename SplitGeo32<N>::G;
             static_assert(G::NT == TN, "jump geometry must use the kernel's threads");
+            static_assert(G::template bytes<uint32_t>(N / 32 + 1) <= sizeof(uint32_t) * B,
+                          "jump buffers must fit the generation buffer");
             if (T.jpoly) jump_one<Tr32, G>(buf, L, T.jpoly, nwords);
         }
         __syncthreads();
@@ -78,17 +94,64 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
                 }
             }
         }
-        uint32_t *dst = T.wb == kWbStream ? st
-                      : T.wb >= 0         ? stage + (size_t)T.wb * stateStride(N)
-                                          : nullptr;
+        uint32_t *dst = endWindow(T, states, stage, stateStride(N));
         if (dst)
             for (int k = threadIdx.x; k < N; k += TN) dst[k] = buf[k];
         __syncthreads();
     }
 }
 
+// Four-words-per-thread core (W/4 threads per CTA), for plans without split
+// requests.
+template <int N, int W, int B, int MODE>
+__global__ void __launch_bounds__(W / 4, MODE == -2 ? 1 : 1280 / W * 4)
+k_batch32x4(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
+            const BatchTask *__restrict__ tasks, int ntasks,
+            const BatchItem *__restrict__ items, char *__restrict__ out,
+            unsigned *__restrict__ counter, uint32_t *__restrict__ stage, int nwords) {
+    constexpr int T = W / 4;
+    constexpr int PW = Geo4<N, W, B>::PW;
+    __shared__ __align__(16) uint32_t buf[Geo4<N, W, B>::BUF];
+    __shared__ int s_task;
+    (void)nwords;
+    for (;;) {
+        if (threadIdx.x == 0) s_task = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int t = s_task;
+        __syncthreads();
+        if (t >= ntasks) break;
+        const BatchTask TK = tasks[t];
+        Lane32 L;
+        L.load(params[TK.pidx], threadIdx.x & 31);
+        const uint32_t *src = states + (size_t)TK.stream * stateStride(N);
+        for (int k = threadIdx.x; k < N; k += T) buf[plane_at<PW>(k)] = src[k];
+        __syncthreads();
+        for (int i = 0; i < TK.nitems; i++) {
+            const BatchItem I = items[TK.first + i];
+            char *o = out + I.out_off;
+            if constexpr (MODE >= -1) {
+                using C = Core4<N, W, B, MODE>;
+                C::run(buf, L, L.otab(MODE < 0 ? 0 : MODE), I.count, (typename C::OT *)o);
+            } else {
+                switch (I.kind) {
+                case 0: Core4<N, W, B, 0>::run(buf, L, L.tmp, I.count, (uint32_t *)o); break;
+                case 1: Core4<N, W, B, 1>::run(buf, L, L.flt, I.count, (float *)o); break;
+                case 2: Core4<N, W, B, 2>::run(buf, L, L.flt, I.count, (float *)o); break;
+                case 3: Core4<N, W, B, 3>::run(buf, L, L.flt, I.count, (float *)o); break;
+                case 4: Core4<N, W, B, 4>::run(buf, L, L.flt, I.count, (float *)o); break;
+                default: Core4<N, W, B, -1>::run(buf, L, L.tmp, I.count, nullptr); break;
+                }
+            }
+        }
+        uint32_t *dst = endWindow(TK, states, stage, stateStride(N));
+        if (dst)
+            for (int k = threadIdx.x; k < N; k += T) dst[k] = buf[plane_at<PW>(k)];
+        __syncthreads();
+    }
+}
+
 template <int N, int TN, int B, int MODE, bool SPLIT>
-__global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1536 : 2048) / TN)
+__global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1280 : 2048) / TN)
 k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
@@ -109,6 +172,8 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
         if constexpr (SPLIT && kSplit64<N>) {
             using G = typename SplitGeo64<N>::G;
             static_assert(G::NT == TN, "jump geometry must use the kernel's threads");
+            static_assert(G::template bytes<uint64_t>(N * 2) <= sizeof(uint64_t) * B,
+                          "jump buffers must fit the generation buffer");
             if (T.jpoly) jump_one<Tr64, G>(buf, L, T.jpoly, nwords);
         }
         __syncthreads();
@@ -130,9 +195,7 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
                 }
             }
         }
-        uint64_t *dst = T.wb == kWbStream ? st
-                      : T.wb >= 0         ? stage + (size_t)T.wb * stateStride(N)
-                                          : nullptr;
+        uint64_t *dst = endWindow(T, states, stage, stateStride(N));
         if (dst)
             for (int k = threadIdx.x; k < N; k += TN) dst[k] = buf[k];
         __syncthreads();
@@ -158,9 +221,10 @@ static cudaError_t resident(K kern, int tn, int *grid) {
     return e;
 }
 
+// work counter reset -> persistent kernel
 template <typename W, class K, class P>
 static cudaError_t go(K kern, int tn, const BatchLaunch &b, const P *params, W *states,
-                      cudaStream_t s, int n) {
+                      cudaStream_t s) {
     int grid = b.grid;
     if (grid <= 0) {
         cudaError_t e = resident(kern, tn, &grid);
@@ -172,23 +236,35 @@ static cudaError_t go(K kern, int tn, const BatchLaunch &b, const P *params, W *
     kern<<<grid, tn, 0, s>>>(params, states, b.tasks, b.ntasks, b.items,
                              static_cast<char *>(b.out), b.counter, static_cast<W *>(b.stage),
                              b.nwords);
-    e = cudaGetLastError();
-    if (e != cudaSuccess || b.nstage <= 0) return e;
-    (void)n;
-    return cudaSuccess;
+    return cudaGetLastError();
 }
 
 template <int N, int TN, int B, bool SPLIT>
 static cudaError_t mode32(const BatchLaunch &b, const DevParams32 *p, uint32_t *st,
                           cudaStream_t s) {
     switch (b.mode) {
-    case -1: return go<uint32_t>(k_batch32<N, TN, B, -1, SPLIT>, TN, b, p, st, s, N);
-    case 0: return go<uint32_t>(k_batch32<N, TN, B, 0, SPLIT>, TN, b, p, st, s, N);
-    case 1: return go<uint32_t>(k_batch32<N, TN, B, 1, SPLIT>, TN, b, p, st, s, N);
-    case 2: return go<uint32_t>(k_batch32<N, TN, B, 2, SPLIT>, TN, b, p, st, s, N);
-    case 3: return go<uint32_t>(k_batch32<N, TN, B, 3, SPLIT>, TN, b, p, st, s, N);
-    case 4: return go<uint32_t>(k_batch32<N, TN, B, 4, SPLIT>, TN, b, p, st, s, N);
-    default: return go<uint32_t>(k_batch32<N, TN, B, -2, SPLIT>, TN, b, p, st, s, N);
+    case -1: return go<uint32_t>(k_batch32<N, TN, B, -1, SPLIT>, TN, b, p, st, s);
+    case 0: return go<uint32_t>(k_batch32<N, TN, B, 0, SPLIT>, TN, b, p, st, s);
+    case 1: return go<uint32_t>(k_batch32<N, TN, B, 1, SPLIT>, TN, b, p, st, s);
+    case 2: return go<uint32_t>(k_batch32<N, TN, B, 2, SPLIT>, TN, b, p, st, s);
+    case 3: return go<uint32_t>(k_batch32<N, TN, B, 3, SPLIT>, TN, b, p, st, s);
+    case 4: return go<uint32_t>(k_batch32<N, TN, B, 4, SPLIT>, TN, b, p, st, s);
+    default: return go<uint32_t>(k_batch32<N, TN, B, -2, SPLIT>, TN, b, p, st, s);
+    }
+}
+
+template <int N, int W, int B>
+static cudaError_t mode32x4(const BatchLaunch &b, const DevParams32 *p, uint32_t *st,
+                            cudaStream_t s) {
+    constexpr int T = W / 4;
+    switch (b.mode) {
+    case -1: return go<uint32_t>(k_batch32x4<N, W, B, -1>, T, b, p, st, s);
+    case 0: return go<uint32_t>(k_batch32x4<N, W, B, 0>, T, b, p, st, s);
+    case 1: return go<uint32_t>(k_batch32x4<N, W, B, 1>, T, b, p, st, s);
+    case 2: return go<uint32_t>(k_batch32x4<N, W, B, 2>, T, b, p, st, s);
+    case 3: return go<uint32_t>(k_batch32x4<N, W, B, 3>, T, b, p, st, s);
+    case 4: return go<uint32_t>(k_batch32x4<N, W, B, 4>, T, b, p, st, s);
+    default: return go<uint32_t>(k_batch32x4<N, W, B, -2>, T, b, p, st, s);
     }
 }
 
@@ -196,13 +272,13 @@ template <int N, int TN, int B, bool SPLIT>
 static cudaError_t mode64(const BatchLaunch &b, const DevParams64 *p, uint64_t *st,
                           cudaStream_t s) {
     switch (b.mode) {
-    case -1: return go<uint64_t>(k_batch64<N, TN, B, -1, SPLIT>, TN, b, p, st, s, N);
-    case 0: return go<uint64_t>(k_batch64<N, TN, B, 0, SPLIT>, TN, b, p, st, s, N);
-    case 1: return go<uint64_t>(k_batch64<N, TN, B, 1, SPLIT>, TN, b, p, st, s, N);
-    case 2: return go<uint64_t>(k_batch64<N, TN, B, 2, SPLIT>, TN, b, p, st, s, N);
-    case 3: return go<uint64_t>(k_batch64<N, TN, B, 3, SPLIT>, TN, b, p, st, s, N);
-    case 4: return go<uint64_t>(k_batch64<N, TN, B, 4, SPLIT>, TN, b, p, st, s, N);
-    default: return go<uint64_t>(k_batch64<N, TN, B, -2, SPLIT>, TN, b, p, st, s, N);
+    case -1: return go<uint64_t>(k_batch64<N, TN, B, -1, SPLIT>, TN, b, p, st, s);
+    case 0: return go<uint64_t>(k_batch64<N, TN, B, 0, SPLIT>, TN, b, p, st, s);
+    case 1: return go<uint64_t>(k_batch64<N, TN, B, 1, SPLIT>, TN, b, p, st, s);
+    case 2: return go<uint64_t>(k_batch64<N, TN, B, 2, SPLIT>, TN, b, p, st, s);
+    case 3: return go<uint64_t>(k_batch64<N, TN, B, 3, SPLIT>, TN, b, p, st, s);
+    case 4: return go<uint64_t>(k_batch64<N, TN, B, 4, SPLIT>, TN, b, p, st, s);
+    default: return go<uint64_t>(k_batch64<N, TN, B, -2, SPLIT>, TN, b, p, st, s);
     }
 }
 
@@ -210,10 +286,12 @@ template <int N, int TN, int B>
 static cudaError_t run32x(const BatchLaunch &b, const DevParams32 *p, uint32_t *st,
                           cudaStream_t s) {
     cudaError_t e;
-    if constexpr (kSplit32<N>) {
-        e = b.split ? mode32<N, TN, B, true>(b, p, st, s) : mode32<N, TN, B, false>(b, p, st, s);
+    if (b.split) {
+        if constexpr (kSplit32<N>) e = mode32<N, TN, B, true>(b, p, st, s);
+        else return cudaErrorInvalidValue;
+    } else if (b.core == 4) {
+        e = mode32x4<N, TN, B>(b, p, st, s);
     } else {
-        if (b.split) return cudaErrorInvalidValue;
         e = mode32<N, TN, B, false>(b, p, st, s);
     }
     if (e != cudaSuccess || b.nstage <= 0) return e;
@@ -226,10 +304,10 @@ template <int N, int TN, int B>
 static cudaError_t run64x(const BatchLaunch &b, const DevParams64 *p, uint64_t *st,
                           cudaStream_t s) {
     cudaError_t e;
-    if constexpr (kSplit64<N>) {
-        e = b.split ? mode64<N, TN, B, true>(b, p, st, s) : mode64<N, TN, B, false>(b, p, st, s);
+    if (b.split) {
+        if constexpr (kSplit64<N>) e = mode64<N, TN, B, true>(b, p, st, s);
+        else return cudaErrorInvalidValue;
     } else {
-        if (b.split) return cudaErrorInvalidValue;
         e = mode64<N, TN, B, false>(b, p, st, s);
     }
     if (e != cudaSuccess || b.nstage <= 0) return e;
@@ -263,19 +341,26 @@ cudaError_t launchBatch64(const BatchLaunch &b, const DevParams64 *params, uint6
 bool batchSplits32(int mexp) { return mexp == 11213 || mexp == 23209; }
 bool batchSplits64(int mexp) { return mexp == 11213 || mexp == 23209; }
 
-int batchResident32(int mexp) {
+int batchResident32(int mexp, bool split) {
     int g = 0;
-#define X(M, N, T, B) \
-    if (mexp == M) resident(k_batch32<N, T, B, 0, false>, T, &g);
+#define X(M, N, T, B)                                                              \
+    if (mexp == M) {                                                               \
+        if (split) resident(k_batch32<N, T, B, 0, true>, T, &g);                  \
+        else if (genCore32() == 4) resident(k_batch32x4<N, T, B, 0>, T / 4, &g);   \
+        else resident(k_batch32<N, T, B, 0, false>, T, &g);                        \
+    }
     MTGP_SHAPES32(X)
 #undef X
     return g;
 }
 
-int batchResident64(int mexp) {
+int batchResident64(int mexp, bool split) {
     int g = 0;
 #define X(M, N, T, B) \
-    if (mexp == M) resident(k_batch64<N, T, B, 0, false>, T, &g);
+    if (mexp == M) {                                                  \
+        if (split) resident(k_batch64<N, T, B, 0, true>, T, &g);      \
+        else resident(k_batch64<N, T, B, 0, false>, T, &g);           \
+    }
     MTGP_SHAPES64(X)
 #undef X
     return g;

@@ -6,9 +6,13 @@
 // writes the advanced window back.  Unlike the sample it accepts any n (not
 // a multiple of 3*TN), any parameter set per CTA, all five output kinds and
 // every Mersenne exponent of the reference's tables.
-#include "mtgp_device.cuh"
+#include "mtgp_device4.cuh"
 
 namespace mtgp {
+
+static int g_core32 = 4;
+int genCore32() { return g_core32; }
+void setGenCore32(int c) { g_core32 = (c == 1) ? 1 : 4; }
 
 bool shape32(int mexp, Shape *s) {
 #define X(M, N, T, B) \
@@ -45,6 +49,28 @@ k_gen32(const DevParams32 *__restrict__ params, const int *__restrict__ pidx,
     for (int k = threadIdx.x; k < N; k += TN) st[k] = ring[k];
 }
 
+// Same as k_gen32 with the four-words-per-thread core (W = parallel width,
+// W/4 threads per CTA).
+template <int N, int W, int B, int KIND>
+__global__ void __launch_bounds__(W / 4)
+k_gen32x4(const DevParams32 *__restrict__ params, const int *__restrict__ pidx,
+          uint32_t *__restrict__ states, void *__restrict__ out, uint64_t n,
+          uint64_t out_stride) {
+    using C = Core4<N, W, B, KIND>;
+    __shared__ __align__(16) uint32_t buf[Geo4<N, W, B>::BUF];
+    const int g = blockIdx.x;
+    const DevParams32 &P = params[pidx ? pidx[g] : g];
+    Lane32 L;
+    L.load(P, threadIdx.x & 31);
+    uint32_t *st = states + (size_t)g * stateStride(N);
+    for (int k = threadIdx.x; k < N; k += W / 4) buf[plane_at<C::G::PW>(k)] = st[k];
+    __syncthreads();
+    using T = typename C::OT;
+    T *o = KIND < 0 ? nullptr : reinterpret_cast<T *>(out) + (size_t)g * out_stride;
+    C::run(buf, L, L.otab(KIND < 0 ? 0 : KIND), n, o);
+    for (int k = threadIdx.x; k < N; k += W / 4) st[k] = buf[plane_at<C::G::PW>(k)];
+}
+
 template <int N, int TN, int B, int KIND>
 __global__ void __launch_bounds__(TN)
 k_gen64(const DevParams64 *__restrict__ params, const int *__restrict__ pidx,
@@ -70,6 +96,19 @@ static cudaError_t gen32_kind(int kind, const DevParams32 *params, const int *pi
                               uint32_t *states, int ngen, void *out, uint64_t n,
                               uint64_t os, cudaStream_t s) {
     dim3 grid(ngen), block(TN);
+    if (genCore32() == 4) {
+        dim3 b4(TN / 4);
+        switch (kind) {
+        case -1: k_gen32x4<N, TN, B, -1><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
+        case 0: k_gen32x4<N, TN, B, 0><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
+        case 1: k_gen32x4<N, TN, B, 1><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
+        case 2: k_gen32x4<N, TN, B, 2><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
+        case 3: k_gen32x4<N, TN, B, 3><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
+        case 4: k_gen32x4<N, TN, B, 4><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
     switch (kind) {
     case -1: k_gen32<N, TN, B, -1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
     case 0: k_gen32<N, TN, B, 0><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;

@@ -190,8 +190,8 @@ struct T32 {
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch32(b, p, st, s);
     }
+    static int resident(int mexp, bool split) { return batchResident32(mexp, split); }
     static bool splits(int mexp) { return batchSplits32(mexp); }
-    static int resident(int mexp) { return batchResident32(mexp); }
     static void seed(const HP &p, W s, W *a) { seed32(p, s, a); }
     static void byArray(const HP &p, const W *key, int len, W *a) {
         keyed<W>(a, p.mexp / 32 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
@@ -222,8 +222,8 @@ struct T64 {
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch64(b, p, st, s);
     }
+    static int resident(int mexp, bool split) { return batchResident64(mexp, split); }
     static bool splits(int mexp) { return batchSplits64(mexp); }
-    static int resident(int mexp) { return batchResident64(mexp); }
     static void seed(const HP &p, W s, W *a) { seed64(p, s, a); }
     static void byArray(const HP &p, const W *key, int len, W *a) {
         keyed<W>(a, p.mexp / 64 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
@@ -272,7 +272,7 @@ struct Pool {
     std::vector<int> chideg;
     // device copies of X^steps mod chi, keyed by (parameter set, steps)
     std::vector<std::pair<std::pair<int, uint64_t>, uint32_t *>> jcache;
-    int resident = 0;
+    int resident = 0, resident_split = 0;
 
     ~Pool() {
         for (auto &kv : jcache) cudaFree(kv.second);
@@ -584,16 +584,20 @@ struct mtgp_gpu_plan {
     uint64_t out_bytes = 0;
     int grid = 0;
     bool split = false;    // some tasks are chunks of split requests
+    int core = 4;          // 32-bit generation core of unsplit plans
     int64_t chunk = 0;     // chunk length used when splitting
     void *d_stage = nullptr;
     int32_t *d_stage_streams = nullptr;
     int nstage = 0;
+
     cudaGraphExec_t exec = nullptr;
     void *graph_out = nullptr;
     ~mtgp_gpu_plan() {
         if (exec) cudaGraphExecDestroy(exec);
+
         cudaFree(d_stage);
         cudaFree(d_stage_streams);
+
         cudaFree(d_tasks);
         cudaFree(d_items);
         cudaFree(d_counter);
@@ -654,17 +658,21 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         order.push_back(std::move(tk));
     }
     int64_t chunk = 0;
-    if (g_tune.split_chunk > 0) {
-        chunk = g_tune.split_chunk;
-    } else if (g_tune.split_chunk == 0 && T::splits(P.sh.mexp)) {
-        if (!P.resident) P.resident = T::resident(P.sh.mexp);
-        const uint64_t per = grand / (uint64_t)std::max(P.resident, 1);
-        chunk = 1 << 17;
-        while ((uint64_t)chunk < per) chunk <<= 1;
+    if (T::splits(P.sh.mexp)) {
+        if (!P.resident_split) P.resident_split = T::resident(P.sh.mexp, true);
+        if (g_tune.split_chunk > 0) {
+            chunk = g_tune.split_chunk;
+        } else if (g_tune.split_chunk == 0) {
+            // a task longer than the average load of one CTA slot would set
+            // the length of the whole launch
+            const uint64_t per = grand / (uint64_t)std::max(P.resident_split, 1);
+            chunk = 1 << 17;
+            while ((uint64_t)chunk < per) chunk <<= 1;
+        }
     }
     std::vector<int32_t> stage_streams;
     bool split = false;
-    if (chunk > 0 && T::splits(P.sh.mexp)) {
+    if (chunk > 0) {
         std::vector<Tk> out;
         for (Tk &tk : order) {
             if (tk.t.nitems != 1 || tk.total <= (uint64_t)chunk + (uint64_t)chunk / 4) {
@@ -714,6 +722,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->out_bytes = out_bytes;
     pl->grid = (int)g_tune.batch_grid;
     pl->split = split;
+    pl->core = genCore32();
     pl->chunk = split ? chunk : 0;
     pl->nstage = (int)stage_streams.size();
     cudaError_t e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
@@ -747,8 +756,9 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     b.mexp = P.sh.mexp;
     b.mode = pl->mode;
     b.grid = pl->grid;
-    b.split = pl->split;
     b.nwords = P.polyWords();
+    b.split = pl->split;
+    b.core = pl->core;
     b.tasks = pl->d_tasks;
     b.ntasks = pl->ntasks;
     b.items = pl->d_items;
@@ -763,6 +773,119 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
 
 int planLaunch(mtgp_gpu_plan *pl, void *out, void *s) {
     return pl->bits == 32 ? launchPlan<T32>(pl, out, s) : launchPlan<T64>(pl, out, s);
+}
+
+// Autotuner: build one plan per candidate configuration, time each on the
+// caller's own items and output buffer (CUDA events on the caller's stream,
+// best of `reps` launches after one warm-up), and keep the fastest.  The
+// stream windows are restored from a snapshot before every launch, so every
+// candidate does exactly the same work and the pool ends where it started.
+// Candidates: generation core (32-bit: four words per thread in 64-thread
+// CTAs with 128-bit stores, or one word per thread in 256-thread CTAs with
+// 32-bit stores), split-chunk length for long requests (none, or 2^17 to
+// 2^20 in steps of 2^17), and grid size (all resident CTAs or three
+// quarters of them).
+template <class T>
+int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, void *s,
+             int reps, mtgp_gpu_plan **best, char *report, int cap) {
+    using W = typename T::W;
+    if (!best) return setErr(MTGP_ERR_INVALID, "null plan pointer");
+    *best = nullptr;
+    if (reps < 1) reps = 1;
+    struct Cand {
+        int core;
+        int64_t chunk, grid;
+    };
+    std::vector<Cand> cands;
+    const int cores[2] = {4, 1};
+    for (int c = 0; c < (T::kBits == 32 ? 2 : 1); c++) cands.push_back({cores[c], -1, 0});
+    if (T::splits(P.sh.mexp))
+        for (int64_t ch = 1 << 17; ch <= (1 << 20); ch += 1 << 17) cands.push_back({1, ch, 0});
+    const size_t sbytes = sizeof(W) * (size_t)P.stride * P.count;
+    W *snap = nullptr;
+    CK(cudaMalloc(&snap, sbytes), "cudaMalloc(autotune snapshot)");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const Tuning saved = g_tune;
+    const int saved_core = genCore32();
+    std::string rep;
+    float best_ms = 0;
+    int rc = MTGP_OK;
+    cudaError_t ce = cudaMemcpyAsync(snap, P.d_states, sbytes, cudaMemcpyDeviceToDevice, S(s));
+    if (ce != cudaSuccess) rc = cudaErr(ce, "autotune snapshot");
+    auto timeOne = [&](mtgp_gpu_plan *pl, float *ms) -> int {
+        float bestt = 1e30f;
+        for (int r = 0; r <= reps; r++) {
+            cudaError_t e = cudaMemcpyAsync(P.d_states, snap, sbytes, cudaMemcpyDeviceToDevice, S(s));
+            if (e == cudaSuccess) e = cudaEventRecord(e0, S(s));
+            if (e != cudaSuccess) return cudaErr(e, "autotune");
+            int r2 = launchPlan<T>(pl, out, s);
+            if (r2) return r2;
+            e = cudaEventRecord(e1, S(s));
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float t = 0;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+            if (e != cudaSuccess) return cudaErr(e, "autotune timing");
+            if (r > 0 && t < bestt) bestt = t;
+        }
+        *ms = bestt;
+        return MTGP_OK;
+    };
+    for (size_t k = 0; k < cands.size() && !rc; k++) {
+        for (int g = 0; g < 2 && !rc; g++) {
+            g_tune.split_chunk = cands[k].chunk;
+            g_tune.batch_grid = 0;
+            setGenCore32(cands[k].core);
+            mtgp_gpu_plan *pl = nullptr;
+            rc = makePlan(P, items, nitems, &pl);
+            if (rc) break;
+            if (cands[k].chunk > 0 && !pl->split) {  // nothing long enough to split
+                delete pl;
+                break;
+            }
+            if (g == 1) {
+                // three quarters of the resident CTAs
+                const int full = T::resident(P.sh.mexp, pl->split);
+                pl->grid = std::max(1, full * 3 / 4);
+            }
+            float ms = 0;
+            rc = timeOne(pl, &ms);
+            if (rc) {
+                delete pl;
+                break;
+            }
+            char line[160];
+            std::snprintf(line, sizeof line, "core=%d chunk=%lld grid=%s tasks=%d: %.4f ms\n",
+                          pl->split ? 1 : pl->core, (long long)(pl->split ? pl->chunk : 0),
+                          g ? "3/4" : "all", pl->ntasks, ms);
+            rep += line;
+            if (!*best || ms < best_ms) {
+                delete *best;
+                *best = pl;
+                best_ms = ms;
+            } else {
+                delete pl;
+            }
+        }
+    }
+    g_tune = saved;
+    setGenCore32(saved_core);
+    ce = cudaMemcpyAsync(P.d_states, snap, sbytes, cudaMemcpyDeviceToDevice, S(s));
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(s));
+    if (!rc && ce != cudaSuccess) rc = cudaErr(ce, "autotune restore");
+    cudaFree(snap);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) {
+        delete *best;
+        *best = nullptr;
+        return rc;
+    }
+    if (report && cap > 0) {
+        std::snprintf(report, (size_t)cap, "%s", rep.c_str());
+    }
+    return MTGP_OK;
 }
 
 template <class Obj>
@@ -1060,6 +1183,20 @@ int mtgp64_gpu_set_window_host(mtgp64_gpu_t *h, const uint64_t *w, int size) {
 POOL_API(32, uint32_t)
 POOL_API(64, uint64_t)
 
+int mtgp32_gpu_pool_autotune(mtgp32_gpu_pool_t *p, const mtgp_work_item_t *items, int nitems,
+                             void *dev_out, void *stream, int reps, mtgp_gpu_plan_t **plan,
+                             char *report, int report_cap) {
+    if (!p) return setErr(MTGP_ERR_INVALID, "null pool");
+    return autotune(p->pool, items, nitems, dev_out, stream, reps, plan, report, report_cap);
+}
+
+int mtgp64_gpu_pool_autotune(mtgp64_gpu_pool_t *p, const mtgp_work_item_t *items, int nitems,
+                             void *dev_out, void *stream, int reps, mtgp_gpu_plan_t **plan,
+                             char *report, int report_cap) {
+    if (!p) return setErr(MTGP_ERR_INVALID, "null pool");
+    return autotune(p->pool, items, nitems, dev_out, stream, reps, plan, report, report_cap);
+}
+
 int mtgp_gpu_plan_launch(mtgp_gpu_plan_t *pl, void *out, void *s) {
     if (!pl) return setErr(MTGP_ERR_INVALID, "null plan");
     return planLaunch(pl, out, s);
@@ -1104,6 +1241,9 @@ int mtgp_gpu_set_tuning(const char *key, int64_t value) {
     if (!key) return setErr(MTGP_ERR_INVALID, "null key");
     if (!std::strcmp(key, "split_chunk")) {
         g_tune.split_chunk = value;
+    } else if (!std::strcmp(key, "core")) {
+        if (value != 1 && value != 4) return setErr(MTGP_ERR_INVALID, "core must be 1 or 4");
+        setGenCore32((int)value);
     } else if (!std::strcmp(key, "batch_grid")) {
         if (value < 0) return setErr(MTGP_ERR_INVALID, "batch_grid must be >= 0");
         g_tune.batch_grid = value;

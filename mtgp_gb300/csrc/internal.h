@@ -54,6 +54,10 @@ struct Shape {
 
 
 bool shape32(int mexp, Shape *s);
+// Which 32-bit generation core the plain and batched kernels use: 4 = four
+// adjacent words per thread (default), 1 = one word per thread.
+int genCore32();
+void setGenCore32(int core);
 bool shape64(int mexp, Shape *s);
 __host__ __device__ constexpr int stateStride(int n) { return (n + 31) & ~31; }
 
@@ -88,6 +92,22 @@ struct JumpDesc {
     uint64_t src;      // element offset of the source window
     uint64_t dst;      // element offset of the destination window
 };
+// Partial jumps: CTA b correlates the tap chunks [ch0, ch1) of one jump and
+// XORs the result into dst (a zeroed window); the parts of a jump together
+// give the full jump.  jumpChunks*() = tap chunks of one jump.
+struct JumpPart {
+    const uint32_t *poly;
+    uint64_t src;      // element offset of the source window in states
+    void *dst;         // destination window (global), zero on entry
+    int pidx;
+    int ch0, ch1;
+};
+cudaError_t launchJumpParts32(int mexp, const DevParams32 *params, const uint32_t *states,
+                              const JumpPart *parts, int nparts, int nwords, cudaStream_t s);
+cudaError_t launchJumpParts64(int mexp, const DevParams64 *params, const uint64_t *states,
+                              const JumpPart *parts, int nparts, int nwords, cudaStream_t s);
+int jumpChunks32(int mexp, int nwords);
+int jumpChunks64(int mexp, int nwords);
 cudaError_t launchJump32(int mexp, const DevParams32 *params, uint32_t *states,
                          const JumpDesc *descs, int ndesc, int nwords,
                          cudaStream_t s);

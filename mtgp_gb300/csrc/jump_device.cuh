@@ -164,4 +164,73 @@ __device__ void jump_one(typename Tr::W *smem, const typename Tr::Lane &L, const
     jump_chain_impl<Tr, Geo>(smem, L, [poly](int) { return poly; }, 1, nwords);
 }
 
+// Part of one jump: the correlation over the tap chunks [ch0, ch1) only
+// (chunks of Geo::C taps), XOR-ed into gdst[0..N) in global memory with
+// atomicXor (gdst must start at zero; the parts of one jump may run in any
+// order on any CTAs).  smem holds the window in jin on entry.  The recursion
+// is still generated from the window up to the last tap of the range.
+template <class Tr, class Geo>
+__device__ void jump_part(typename Tr::W *smem, const typename Tr::Lane &L, const uint32_t *pg,
+                          int nwords, int ch0, int ch1, typename Tr::W *gdst) {
+    using W = typename Tr::W;
+    constexpr int N = Geo::N, R = Geo::R, NT = Geo::NT;
+    constexpr uint32_t M = Geo::RING - 1;
+    W *jin = smem;
+    W *ring = jin + 2 * Geo::NJ;
+    uint32_t *poly = reinterpret_cast<uint32_t *>(ring + Geo::RING);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int pwords = nwords + Geo::PAD;
+    for (int k = tid; k < pwords; k += NT) poly[k] = k < nwords ? pg[k] : 0u;
+    for (int g = 0; g < Geo::G; g++) {
+        for (int k = tid; k < N; k += NT) ring[k] = jin[k];
+        __syncthreads();
+        int generated = N;
+        const int l0 = g * 32 * R + lane * R;
+        W acc[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) acc[r] = 0;
+        for (int ch = 0; ch < ch1; ch++) {
+            const int cs = ch * Geo::C;
+            while (generated < cs + Geo::C + N) {
+                if (tid < Geo::GW) {
+                    uint32_t w = (uint32_t)(generated + tid);
+                    W x1 = ring[(w - N) & M];
+                    W x2 = ring[(w - N + 1) & M];
+                    W y = ring[(w - N + L.pos) & M];
+                    ring[w & M] = Tr::rec(x1, x2, y, L);
+                }
+                __syncthreads();
+                generated += Geo::GW;
+            }
+            if (ch >= ch0) {
+                const int i0 = cs + warp * Geo::TPW;
+                W win[R];
+#pragma unroll
+                for (int r = 0; r < R; r++) win[r] = ring[(uint32_t)(i0 + l0 + r) & M];
+                for (int jb = 0; jb < Geo::TPW; jb += R) {
+                    const int p = i0 + jb;
+                    const uint32_t bits_lo =
+                        __funnelshift_r(poly[p >> 5], poly[(p >> 5) + 1], p & 31);
+                    const uint32_t bits_hi =
+                        R > 32 ? __funnelshift_r(poly[(p >> 5) + 1], poly[(p >> 5) + 2], p & 31)
+                               : 0u;
+#pragma unroll
+                    for (int j = 0; j < R; j++) {
+                        const uint32_t bj = j < 32 ? bits_lo : bits_hi;
+                        const uint32_t m = (uint32_t)((int32_t)(bj << (31 - (j & 31))) >> 31);
+#pragma unroll
+                        for (int r = 0; r < R; r++) acc[r] ^= Tr::andm(win[(j + r) % R], m);
+                        win[j] = ring[(uint32_t)(p + l0 + R + j) & M];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (l0 + r < N) Tr::axor(&gdst[l0 + r], acc[r]);
+        __syncthreads();
+    }
+}
+
 }  // namespace mtgp

@@ -28,6 +28,40 @@ k_jump(const typename Tr::P *__restrict__ params, typename Tr::W *__restrict__ s
     for (int k = threadIdx.x; k < Geo::N; k += Geo::NT) states[D.dst + k] = smem[k];
 }
 
+// One CTA per (jump, slice of tap chunks): partial correlation XOR-ed into
+// the zeroed destination window (jump_device.cuh: jump_part).
+template <class Tr, class Geo>
+__global__ void __launch_bounds__(Geo::NT)
+k_jump_part(const typename Tr::P *__restrict__ params, const typename Tr::W *__restrict__ states,
+            const JumpPart *__restrict__ parts, int nwords) {
+    using W = typename Tr::W;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    W *smem = reinterpret_cast<W *>(smem_raw);
+    const JumpPart &D = parts[blockIdx.x];
+    typename Tr::Lane L;
+    L.load(params[D.pidx], threadIdx.x & 31);
+    for (int k = threadIdx.x; k < Geo::N; k += Geo::NT) smem[k] = states[D.src + k];
+    __syncthreads();
+    jump_part<Tr, Geo>(smem, L, D.poly, nwords, D.ch0, D.ch1, static_cast<W *>(D.dst));
+}
+
+template <class Tr, class Geo>
+cudaError_t launchParts(const typename Tr::P *params, const typename Tr::W *states,
+                        const JumpPart *parts, int nparts, int nwords, cudaStream_t s) {
+    using W = typename Tr::W;
+    const size_t smem = Geo::template bytes<W>(nwords);
+    auto kern = k_jump_part<Tr, Geo>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    if (nparts <= 0) return cudaSuccess;
+    kern<<<nparts, Geo::NT, smem, s>>>(params, states, parts, nwords);
+    return cudaGetLastError();
+}
+
+template <class Geo>
+int chunksOf(int nwords) { return (nwords * 32 + Geo::C - 1) / Geo::C; }
+
 template <class Tr, class Geo>
 cudaError_t launch(const typename Tr::P *params, typename Tr::W *states,
                    const JumpDesc *descs, int ndesc, int nwords, cudaStream_t s) {
@@ -44,27 +78,70 @@ cudaError_t launch(const typename Tr::P *params, typename Tr::W *states,
 
 }  // namespace
 
+#define MTGP_JGEO32(X)                                     \
+    X(11213, (JGeo<351, 11, kJumpThreads, 256, 2048>))     \
+    X(23209, (JGeo<726, 23, kJumpThreads, 256, 4096>))     \
+    X(44497, (JGeo<1391, 45, kJumpThreads, 256, 4096>))
+#define MTGP_JGEO64(X)                                     \
+    X(11213, (JGeo<176, 7, kJumpThreads, 128, 2048>))      \
+    X(23209, (JGeo<363, 13, kJumpThreads, 256, 2048>))     \
+    X(44497, (JGeo<696, 23, kJumpThreads, 256, 4096>))     \
+    X(110503, (JGeo<1727, 27, kJumpThreads, 256, 4096>))
+
+template <class G> struct Unwrap;
+template <class G> struct Unwrap<void(G)> { using T = G; };
+#define UNWRAP(G) typename Unwrap<void G>::T
+
 cudaError_t launchJump32(int mexp, const DevParams32 *params, uint32_t *states,
                          const JumpDesc *descs, int ndesc, int nwords, cudaStream_t s) {
-    constexpr int T = kJumpThreads;
-    switch (mexp) {
-    case 11213: return launch<Tr32, JGeo<351, 11, T, 256, 2048>>(params, states, descs, ndesc, nwords, s);
-    case 23209: return launch<Tr32, JGeo<726, 23, T, 256, 4096>>(params, states, descs, ndesc, nwords, s);
-    case 44497: return launch<Tr32, JGeo<1391, 45, T, 256, 4096>>(params, states, descs, ndesc, nwords, s);
-    default: return cudaErrorInvalidValue;
-    }
+#define X(M, G) \
+    if (mexp == M) return launch<Tr32, UNWRAP(G)>(params, states, descs, ndesc, nwords, s);
+    MTGP_JGEO32(X)
+#undef X
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launchJump64(int mexp, const DevParams64 *params, uint64_t *states,
                          const JumpDesc *descs, int ndesc, int nwords, cudaStream_t s) {
-    constexpr int T = kJumpThreads;
-    switch (mexp) {
-    case 11213: return launch<Tr64, JGeo<176, 7, T, 128, 2048>>(params, states, descs, ndesc, nwords, s);
-    case 23209: return launch<Tr64, JGeo<363, 13, T, 256, 2048>>(params, states, descs, ndesc, nwords, s);
-    case 44497: return launch<Tr64, JGeo<696, 23, T, 256, 4096>>(params, states, descs, ndesc, nwords, s);
-    case 110503: return launch<Tr64, JGeo<1727, 27, T, 256, 4096>>(params, states, descs, ndesc, nwords, s);
-    default: return cudaErrorInvalidValue;
-    }
+#define X(M, G) \
+    if (mexp == M) return launch<Tr64, UNWRAP(G)>(params, states, descs, ndesc, nwords, s);
+    MTGP_JGEO64(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launchJumpParts32(int mexp, const DevParams32 *params, const uint32_t *states,
+                              const JumpPart *parts, int nparts, int nwords, cudaStream_t s) {
+#define X(M, G) \
+    if (mexp == M) return launchParts<Tr32, UNWRAP(G)>(params, states, parts, nparts, nwords, s);
+    MTGP_JGEO32(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launchJumpParts64(int mexp, const DevParams64 *params, const uint64_t *states,
+                              const JumpPart *parts, int nparts, int nwords, cudaStream_t s) {
+#define X(M, G) \
+    if (mexp == M) return launchParts<Tr64, UNWRAP(G)>(params, states, parts, nparts, nwords, s);
+    MTGP_JGEO64(X)
+#undef X
+    return cudaErrorInvalidValue;
+}
+
+int jumpChunks32(int mexp, int nwords) {
+#define X(M, G) \
+    if (mexp == M) return chunksOf<UNWRAP(G)>(nwords);
+    MTGP_JGEO32(X)
+#undef X
+    return 1;
+}
+
+int jumpChunks64(int mexp, int nwords) {
+#define X(M, G) \
+    if (mexp == M) return chunksOf<UNWRAP(G)>(nwords);
+    MTGP_JGEO64(X)
+#undef X
+    return 1;
 }
 
 }  // namespace mtgp

@@ -159,6 +159,7 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
     b.mexp = sh.mexp;
     b.mode = mode == -3 ? -1 : mode;
     b.grid = 0;
+    b.core = genCore32();
     b.split = false;
     b.nwords = 0;
     b.tasks = reinterpret_cast<const BatchTask *>(base + NaLayout::tasks);

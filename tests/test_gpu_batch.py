@@ -202,3 +202,29 @@ def test_batch_split_graph(gpu, orc):
         for j in range(16):
             a = int(offs[j]) // 4
             assert np.array_equal(got[a:a + int(counts[j])], gens[j].fill(0, int(counts[j]))), (rep, j)
+
+
+def test_autotune_leaves_pool_and_picks_exact_plan(gpu, orc):
+    """The autotuner times candidates on the real items, restores the
+    windows, and returns a plan whose output is bit-exact."""
+    from mtgp_gb300.api import Pool, work_items
+    p = load_table("mtgp32_fast_11213")[0]
+    pool = Pool.substreams(p, 1234, 64, jump_table(32))
+    rng = np.random.default_rng(5)
+    counts = rng.integers(1000, 400000, 64)
+    counts[0] = 1 << 20  # long enough to make split candidates real
+    offs = np.concatenate([[0], np.cumsum(counts)[:-1]]) * 4
+    items = work_items(np.arange(64), np.zeros(64), counts, offs)
+    out = torch.zeros(int(counts.sum()), dtype=torch.int32, device="cuda")
+    before = pool.windows()
+    plan, report = pool.autotune(items, out, reps=1)
+    assert np.array_equal(pool.windows(), before)
+    assert report.count("ms") >= 3, report
+    plan.launch(out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(np.uint32)
+    for j in (0, 1, 37, 63):
+        o = orc.gen(p, seed=1234)
+        o.set_window(before[j])
+        a = int(offs[j]) // 4
+        assert np.array_equal(got[a:a + int(counts[j])], o.fill(0, int(counts[j]))), j
