@@ -236,15 +236,21 @@ int mtgp64_gpu_set_window_host(mtgp64_gpu_t *h, const uint64_t *win,
 typedef struct mtgp32_gpu_pool mtgp32_gpu_pool_t;
 typedef struct mtgp64_gpu_pool mtgp64_gpu_pool_t;
 
-/* One unit of batched work: continue stream `stream` by `count` values of
- * `kind` (MTGP_KIND_*, or -1 = advance without output), written at byte
- * offset `out_offset` of the output buffer (a multiple of the value size).
- * Items naming the same stream are applied in array order. */
+/* One unit of batched work: advance stream `stream` by `skip` values
+ * without output, then produce `count` values of `kind` (MTGP_KIND_*, or
+ * -1 = advance without output) at byte offset `out_offset` of the output
+ * buffer (a multiple of the value size).  Items naming the same stream are
+ * applied in array order.  For MEXP 11213 and 23209, a skip (or an
+ * advance-only item) of 2^17 values or more is done by a GF(2) jump (X^skip
+ * mod chi, inside the batched kernel) instead of generation; for the other
+ * exponents skips are generated, and a skip above 2^34 is rejected with
+ * MTGP_ERR_UNSUPPORTED. */
 typedef struct mtgp_work_item {
     uint32_t stream;
     int32_t kind;
     uint64_t count;
     uint64_t out_offset;
+    uint64_t skip;
 } mtgp_work_item_t;
 
 /* A prepared batch: descriptors uploaded once, launched many times. */
@@ -279,6 +285,10 @@ int mtgp32_gpu_pool_submit(mtgp32_gpu_pool_t *p, const mtgp_work_item_t *items,
                            int nitems, void *dev_out, void *stream);
 int mtgp32_gpu_pool_plan(mtgp32_gpu_pool_t *p, const mtgp_work_item_t *items,
                          int nitems, mtgp_gpu_plan_t **plan);
+/* Refill an existing plan of this pool with new items, keeping (and only
+ * growing) its device buffers.  The plan must not be in use on the GPU. */
+int mtgp32_gpu_pool_replan(mtgp32_gpu_pool_t *p, const mtgp_work_item_t *items,
+                           int nitems, mtgp_gpu_plan_t *plan);
 /* Jump stream s by a polynomial (uint32-array form). */
 int mtgp32_gpu_pool_jump_array(mtgp32_gpu_pool_t *p, int s,
                                const uint32_t *poly, int nwords, void *stream);
@@ -308,6 +318,8 @@ int mtgp64_gpu_pool_submit(mtgp64_gpu_pool_t *p, const mtgp_work_item_t *items,
                            int nitems, void *dev_out, void *stream);
 int mtgp64_gpu_pool_plan(mtgp64_gpu_pool_t *p, const mtgp_work_item_t *items,
                          int nitems, mtgp_gpu_plan_t **plan);
+int mtgp64_gpu_pool_replan(mtgp64_gpu_pool_t *p, const mtgp_work_item_t *items,
+                           int nitems, mtgp_gpu_plan_t *plan);
 int mtgp64_gpu_pool_jump_array(mtgp64_gpu_pool_t *p, int s,
                                const uint32_t *poly, int nwords, void *stream);
 int mtgp64_gpu_pool_get_windows_host(mtgp64_gpu_pool_t *p, uint64_t *win,
@@ -378,6 +390,62 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
                              const int *param_idx, uint32_t *dev_windows,
                              int nstreams, const mtgp_work_item_t *items,
                              int nitems, void *dev_out, void *stream);
+
+/* ========================================================================= */
+/* Serving loop: continuous batching over resident pools                      */
+/* ========================================================================= */
+/* No counterpart in the reference (its generators are filled by the caller,
+ * one launch per request).  A server owns a device output arena of
+ * `budget_bytes` (the memory budget) and a scheduler thread that admits
+ * pending requests first-come-first-served into batches of at most
+ * `max_batch` requests, keeps up to `slots` batches in flight on their own
+ * CUDA streams, and copies each result to its destination when the batch
+ * completes.  Requests of one stream run in submission order; a request's
+ * values depend only on its stream's position, so they are the same alone and
+ * in any mix.  While a server runs, its pools must not be used otherwise. */
+typedef struct mtgp_server mtgp_server_t;
+
+/* One request of a trace (mtgp_server_replay). */
+typedef struct mtgp_request {
+    int32_t pool;     /* 0 = the 32-bit pool, 1 = the 64-bit pool          */
+    uint32_t stream;  /* stream of that pool                               */
+    int32_t kind;     /* MTGP_KIND_*, or -1 = advance only                 */
+    int32_t pad_;
+    uint64_t skip;    /* values skipped first (GF(2) jump when large)      */
+    uint64_t count;   /* values produced                                   */
+    void *dst;        /* device or host destination, or NULL = discard     */
+} mtgp_request_t;
+
+/* Either pool may be NULL (not both).  The pools must outlive the server. */
+int mtgp_server_create(mtgp_server_t **out, mtgp32_gpu_pool_t *p32,
+                       mtgp64_gpu_pool_t *p64, uint64_t budget_bytes,
+                       int slots, int max_batch);
+/* Queue a request (thread-safe).  Tickets count from 1.  A request whose
+ * output alone exceeds the budget is rejected with MTGP_ERR_BUDGET. */
+int mtgp_server_submit(mtgp_server_t *s, int pool, uint32_t stream, int kind,
+                       uint64_t skip, uint64_t count, void *dst,
+                       uint64_t *ticket);
+/* Remove a request that has not been admitted yet; its status becomes
+ * MTGP_ERR_BUSY.  Fails with MTGP_ERR_INVALID once it is admitted. */
+int mtgp_server_cancel(mtgp_server_t *s, uint64_t ticket);
+/* Wait until a request is done (its destination holds the result);
+ * `status` receives MTGP_OK or the error it ended with. */
+int mtgp_server_wait(mtgp_server_t *s, uint64_t ticket, double timeout_s,
+                     int *status);
+/* Wait until every submitted request is done. */
+int mtgp_server_drain(mtgp_server_t *s, double timeout_s);
+/* Per-ticket latency in seconds (submission to completion; -1 while
+ * pending) and status, for tickets 1..min(cap, submitted); n = submitted. */
+int mtgp_server_results(mtgp_server_t *s, double *latency, int *status,
+                        uint64_t cap, uint64_t *n);
+int mtgp_server_stats(mtgp_server_t *s, uint64_t *completed, uint64_t *bytes,
+                      uint64_t *batches);
+/* Submit n requests at their arrival times (seconds after the call starts),
+ * then drain; wall_s receives the elapsed time. */
+int mtgp_server_replay(mtgp_server_t *s, const mtgp_request_t *reqs,
+                       const double *arrival_s, int n, double *wall_s);
+/* Drains, stops the scheduler and frees the arena (the pools stay). */
+void mtgp_server_destroy(mtgp_server_t *s);
 
 #if defined(__cplusplus)
 }

@@ -25,10 +25,19 @@ pp = ctypes.POINTER(ctypes.c_void_p)
 class WorkItem(ctypes.Structure):
     """mtgp_work_item_t."""
     _fields_ = [("stream", c_u32), ("kind", ctypes.c_int32), ("count", c_u64),
-                ("out_offset", c_u64)]
+                ("out_offset", c_u64), ("skip", c_u64)]
 
 
-assert ctypes.sizeof(WorkItem) == 24
+assert ctypes.sizeof(WorkItem) == 32
+
+
+class Request(ctypes.Structure):
+    """mtgp_request_t (one request of a serving trace)."""
+    _fields_ = [("pool", ctypes.c_int32), ("stream", c_u32), ("kind", ctypes.c_int32),
+                ("pad_", ctypes.c_int32), ("skip", c_u64), ("count", c_u64), ("dst", vp)]
+
+
+assert ctypes.sizeof(Request) == 40
 
 # name -> (restype, argtypes)
 SIGS = {
@@ -41,6 +50,15 @@ SIGS = {
     "mtgp_gpu_plan_info": (c_int, [vp, vp, vp]),
     "mtgp_gpu_set_tuning": (c_int, [cp, ctypes.c_int64]),
     "mtgp32_gpu_batch_noalloc": (c_int, [P32, c_int, vp, vp, c_int, vp, c_int, vp, vp]),
+    "mtgp_server_create": (c_int, [pp, vp, vp, c_u64, c_int, c_int]),
+    "mtgp_server_submit": (c_int, [vp, c_int, c_u32, c_int, c_u64, c_u64, vp, vp]),
+    "mtgp_server_cancel": (c_int, [vp, c_u64]),
+    "mtgp_server_wait": (c_int, [vp, c_u64, ctypes.c_double, vp]),
+    "mtgp_server_drain": (c_int, [vp, ctypes.c_double]),
+    "mtgp_server_results": (c_int, [vp, vp, vp, c_u64, vp]),
+    "mtgp_server_stats": (c_int, [vp, vp, vp, vp]),
+    "mtgp_server_replay": (c_int, [vp, vp, vp, c_int, vp]),
+    "mtgp_server_destroy": (None, [vp]),
 }
 for B, P, W in ((32, P32, c_u32), (64, P64, c_u64)):
     pre = "mtgp%d_gpu_" % B
@@ -66,6 +84,7 @@ for B, P, W in ((32, P32, c_u32), (64, P64, c_u64)):
         pre + "pool_fill_stream": (c_int, [vp, c_int, c_int, vp, c_size_t, vp]),
         pre + "pool_submit": (c_int, [vp, vp, c_int, vp, vp]),
         pre + "pool_plan": (c_int, [vp, vp, c_int, pp]),
+        pre + "pool_replan": (c_int, [vp, vp, c_int, vp]),
         pre + "pool_jump_array": (c_int, [vp, c_int, vp, c_int, vp]),
         pre + "pool_get_windows_host": (c_int, [vp, vp, c_size_t]),
         pre + "pool_set_windows_host": (c_int, [vp, vp, c_size_t]),

@@ -188,7 +188,7 @@ def set_tuning(key, value):
     check(lib().mtgp_gpu_set_tuning(key.encode(), int(value)))
 
 
-def work_items(streams, kinds, counts, offsets):
+def work_items(streams, kinds, counts, offsets, skips=None):
     n = len(streams)
     arr = (WorkItem * n)()
     for k in range(n):
@@ -196,6 +196,7 @@ def work_items(streams, kinds, counts, offsets):
         arr[k].kind = int(kinds[k])
         arr[k].count = int(counts[k])
         arr[k].out_offset = int(offsets[k])
+        arr[k].skip = 0 if skips is None else int(skips[k])
     return arr
 
 
@@ -257,6 +258,11 @@ class Pool:
         check(getattr(lib(), self.pre + "plan")(self.h, items, len(items), ctypes.byref(ph)))
         return Plan(ph, self)
 
+    def replan(self, items, plan):
+        """Refill `plan` (made by this pool, idle on the GPU) with new items."""
+        check(getattr(lib(), self.pre + "replan")(self.h, items, len(items), plan.h))
+        return plan
+
     def autotune(self, items, out, stream=None, reps=3):
         """Fastest plan for these items on this output buffer (the pool's
         windows are left unchanged); returns (plan, report text)."""
@@ -286,3 +292,81 @@ class Pool:
         w = np.ascontiguousarray(win, dtype=np.uint32 if self.bits == 32 else np.uint64).ravel()
         check(getattr(lib(), self.pre + "set_windows_host")(self.h, w.ctypes.data_as(ctypes.c_void_p),
                                                             w.size))
+
+
+class Server:
+    """Continuous-batching request loop over resident pools (mtgp_server_t).
+
+    `submit` queues a request and returns its ticket; the values land in
+    `dst` (a CUDA or CPU tensor of the pool's word size, or None to discard)
+    once `wait(ticket)` returns."""
+
+    def __init__(self, pool32=None, pool64=None, budget_bytes=1 << 30, slots=4, max_batch=4096):
+        self.pools = (pool32, pool64)  # keep the pools alive
+        h = ctypes.c_void_p()
+        check(lib().mtgp_server_create(ctypes.byref(h), pool32.h if pool32 else None,
+                                       pool64.h if pool64 else None, budget_bytes, slots,
+                                       max_batch))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, pool, stream, kind, count, dst=None, skip=0):
+        t = ctypes.c_uint64()
+        ptr = None if dst is None else ctypes.c_void_p(dst.data_ptr())
+        check(lib().mtgp_server_submit(self.h, pool, stream, kind, skip, count, ptr,
+                                       ctypes.byref(t)))
+        if dst is not None:
+            self._keep[t.value] = dst
+        return t.value
+
+    def wait(self, ticket, timeout=60.0):
+        """Status of the finished request (0 = done)."""
+        st = ctypes.c_int()
+        check(lib().mtgp_server_wait(self.h, ticket, timeout, ctypes.byref(st)))
+        self._keep.pop(ticket, None)
+        return st.value
+
+    def cancel(self, ticket):
+        check(lib().mtgp_server_cancel(self.h, ticket))
+
+    def drain(self, timeout=600.0):
+        check(lib().mtgp_server_drain(self.h, timeout))
+        self._keep.clear()
+
+    def results(self):
+        """(latency seconds, status) arrays by ticket - 1."""
+        n = ctypes.c_uint64()
+        check(lib().mtgp_server_results(self.h, None, None, 0, ctypes.byref(n)))
+        lat = np.empty(n.value, dtype=np.float64)
+        st = np.empty(n.value, dtype=np.int32)
+        check(lib().mtgp_server_results(self.h, lat.ctypes.data_as(ctypes.c_void_p),
+                                        st.ctypes.data_as(ctypes.c_void_p), n.value,
+                                        ctypes.byref(n)))
+        return lat, st
+
+    def stats(self):
+        """(completed requests, bytes produced, batches launched)."""
+        c, b, k = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        check(lib().mtgp_server_stats(self.h, ctypes.byref(c), ctypes.byref(b), ctypes.byref(k)))
+        return c.value, b.value, k.value
+
+    def replay(self, requests, arrivals):
+        """Submit `requests` (an array of Request) at `arrivals` (seconds
+        from now) and drain; returns the wall time in seconds."""
+        arr = np.ascontiguousarray(arrivals, dtype=np.float64)
+        wall = ctypes.c_double()
+        check(lib().mtgp_server_replay(self.h, requests, arr.ctypes.data_as(ctypes.c_void_p),
+                                       len(arr), ctypes.byref(wall)))
+        return wall.value
+
+    def close(self):
+        if self.h:
+            lib().mtgp_server_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -60,7 +60,7 @@ def build(verbose=False, force=False):
         for _, log in results:
             sys.stderr.write(log)
     tmp = LIB + ".tmp"
-    cmd = [NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + [o for o, _ in results]
+    cmd = [NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + [o for o, _ in results] + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

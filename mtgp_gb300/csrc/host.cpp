@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <new>
 #include <string>
 #include <vector>
@@ -81,6 +82,13 @@ inline cudaStream_t S(void *s) { return static_cast<cudaStream_t>(s); }
 // Tuning knobs (mtgp_gpu_set_tuning).  split_chunk: 0 = automatic, < 0 =
 // never split long requests, > 0 = split into chunks of this many values.
 // batch_grid: 0 = one CTA per resident slot, > 0 = that many CTAs.
+// A skip at least this long is done by a GF(2) jump inside the batched
+// kernel (about the work of 2^17 generated values) instead of generation.
+constexpr uint64_t kJumpMinSkip = 1 << 17;
+// Longest skip generated step by step (on exponents without the in-kernel
+// jump): about ten seconds of one CTA.
+constexpr uint64_t kMaxGenSkip = uint64_t(1) << 34;
+
 struct Tuning {
     int64_t split_chunk = 0;
     int64_t batch_grid = 0;
@@ -270,12 +278,11 @@ struct Pool {
     size_t desc_cap = 0;
     std::vector<gf2::Poly> chi;   // characteristic polynomial per parameter set
     std::vector<int> chideg;
-    // device copies of X^steps mod chi, keyed by (parameter set, steps)
-    std::vector<std::pair<std::pair<int, uint64_t>, uint32_t *>> jcache;
+    // X^steps mod chi in word form, keyed by (parameter set, steps); bounded
+    std::map<std::pair<int, uint64_t>, std::vector<uint32_t>> jcache;
     int resident = 0, resident_split = 0;
 
     ~Pool() {
-        for (auto &kv : jcache) cudaFree(kv.second);
         cudaFree(d_params);
         cudaFree(d_pidx);
         cudaFree(d_states);
@@ -465,27 +472,18 @@ struct Pool {
 
     int polyWords() const { return sh.mexp / 32 + 1; }
 
-    // Device copy of X^steps mod chi_k (cached).
-    int jumpPoly(int k, uint64_t steps, const uint32_t **out) {
-        for (auto &kv : jcache)
-            if (kv.first.first == k && kv.first.second == steps) {
-                *out = kv.second;
-                return MTGP_OK;
-            }
-        int rc = characteristic(k);
-        if (rc) return rc;
-        std::vector<uint32_t> e = {(uint32_t)steps, (uint32_t)(steps >> 32)};
-        gf2::Poly p = gf2::powxmod(e, chi[k], chideg[k]);
-        std::vector<uint32_t> w = gf2::toWords32(p, polyWords());
-        uint32_t *d = nullptr;
-        CK(cudaMalloc(&d, sizeof(uint32_t) * w.size()), "cudaMalloc(jump poly)");
-        cudaError_t e2 = cudaMemcpy(d, w.data(), sizeof(uint32_t) * w.size(), cudaMemcpyHostToDevice);
-        if (e2 != cudaSuccess) {
-            cudaFree(d);
-            return cudaErr(e2, "upload jump poly");
+    // X^steps mod chi_k as polyWords() words (host, cached).
+    int jumpPoly(int k, uint64_t steps, const std::vector<uint32_t> **out) {
+        auto hit = jcache.find({k, steps});
+        if (hit == jcache.end()) {
+            int rc = characteristic(k);
+            if (rc) return rc;
+            if (jcache.size() >= 16384) jcache.clear();
+            std::vector<uint32_t> e = {(uint32_t)steps, (uint32_t)(steps >> 32)};
+            gf2::Poly p = gf2::powxmod(e, chi[k], chideg[k]);
+            hit = jcache.emplace(std::make_pair(k, steps), gf2::toWords32(p, polyWords())).first;
         }
-        jcache.push_back({{k, steps}, d});
-        *out = d;
+        *out = &hit->second;
         return MTGP_OK;
     }
 
@@ -583,12 +581,15 @@ struct mtgp_gpu_plan {
     int mode = -2;         // shared output kind of all items, or -2 (mixed)
     uint64_t out_bytes = 0;
     int grid = 0;
-    bool split = false;    // some tasks are chunks of split requests
+    bool split = false;    // some tasks start with an in-kernel jump
     int core = 4;          // 32-bit generation core of unsplit plans
+    size_t cap_tasks = 0, cap_items = 0, cap_stage = 0;  // device buffer capacities
     int64_t chunk = 0;     // chunk length used when splitting
     void *d_stage = nullptr;
     int32_t *d_stage_streams = nullptr;
     int nstage = 0;
+    uint32_t *d_polys = nullptr;  // jump polynomials of the tasks that jump
+    size_t cap_polys = 0;
 
     cudaGraphExec_t exec = nullptr;
     void *graph_out = nullptr;
@@ -597,7 +598,7 @@ struct mtgp_gpu_plan {
 
         cudaFree(d_stage);
         cudaFree(d_stage_streams);
-
+        cudaFree(d_polys);
         cudaFree(d_tasks);
         cudaFree(d_items);
         cudaFree(d_counter);
@@ -610,12 +611,12 @@ template <class T>
 int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_plan **out) {
     using W = typename T::W;
     if (!out) return setErr(MTGP_ERR_INVALID, "null plan pointer");
-    *out = nullptr;
+    if (*out && (*out)->pool != &P) return setErr(MTGP_ERR_INVALID, "plan belongs to another pool");
     if (nitems < 0 || (nitems > 0 && !items)) return setErr(MTGP_ERR_INVALID, "bad item list");
     // group by stream, keeping the caller's order within a stream
     std::vector<std::vector<int>> by(P.count);
     uint64_t out_bytes = 0;
-    int mode = -3;  // -3: no item yet
+
     for (int k = 0; k < nitems; k++) {
         const mtgp_work_item_t &it = items[k];
         if (it.stream >= (uint32_t)P.count)
@@ -624,41 +625,84 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             return setErr(MTGP_ERR_INVALID, "item %d: unknown kind %d", k, it.kind);
         if (it.kind >= 0 && it.out_offset % sizeof(W))
             return setErr(MTGP_ERR_INVALID, "item %d: offset not a multiple of %zu", k, sizeof(W));
-        if (it.count == 0) continue;
-        mode = (mode == -3 || mode == it.kind) ? it.kind : -2;
+        if (it.count == 0 && it.skip == 0) continue;
         by[it.stream].push_back(k);
         if (it.kind >= 0) out_bytes = std::max(out_bytes, it.out_offset + it.count * sizeof(W));
     }
-    // One task per stream (its items in order), then split the long
-    // single-item tasks into chunks (see batch_kernels.cu).
-    struct Tk {
-        BatchTask t;
+    // Each stream's items become one or more tasks.  Positions count steps
+    // from the stream's window at launch.  On exponents whose batched
+    // kernels carry the jump code, a skip of at least kJumpMinSkip (or an
+    // advance-only item that long) is not generated: the work after it is a
+    // new task whose window is the stream's window jumped by X^start mod chi
+    // inside the kernel.  A run of work between jumps much longer than `chunk`
+    // is cut into chunks the same way.  The tasks of one stream all start
+    // from the same window and run in parallel; when there are several, the
+    // last leaves its final window in a staging slot that a second kernel
+    // copies back after the launch (see batch_kernels.cu).
+    struct Run {
+        int s;
+        uint64_t start, total;
         std::vector<BatchItem> items;
-        uint64_t total;
     };
-    std::vector<Tk> order;
+    const bool can_jump = T::splits(P.sh.mexp);
+    std::vector<Run> runs;
     uint64_t grand = 0;
     for (int s = 0; s < P.count; s++) {
         if (by[s].empty()) continue;
-        Tk tk{};
-        tk.t.stream = s;
-        tk.t.nitems = (int)by[s].size();
-        tk.t.pidx = P.hpidx[s];
-        tk.t.jpoly = nullptr;
-        tk.t.wb = kWbStream;
+        Run cur{s, 0, 0, {}};
+        uint64_t pos = 0;
         for (int k : by[s]) {
-            BatchItem bi{};
-            bi.out_off = items[k].out_offset;
-            bi.count = items[k].count;
-            bi.kind = items[k].kind;
-            tk.items.push_back(bi);
-            tk.total += items[k].count;
+            const mtgp_work_item_t &it = items[k];
+            uint64_t skip = it.skip, count = it.count;
+            if (it.kind < 0) {  // advance only: all of it is a skip
+                skip += count;
+                count = 0;
+                if (skip < it.skip) return setErr(MTGP_ERR_INVALID, "item %d: skip overflows", k);
+            }
+            if (pos + skip < pos || pos + skip + count < pos + skip)
+                return setErr(MTGP_ERR_INVALID, "item %d: stream position overflows 64 bits", k);
+            if (skip >= kJumpMinSkip && can_jump) {
+                if (!cur.items.empty()) {
+                    grand += cur.total;
+                    runs.push_back(std::move(cur));
+                }
+                pos += skip;
+                cur = Run{s, pos, 0, {}};
+            } else if (skip) {
+                if (skip > kMaxGenSkip)
+                    return setErr(MTGP_ERR_UNSUPPORTED,
+                                  "item %d: skip of %llu values would be generated (no in-kernel "
+                                  "jump for this exponent); jump the stream instead",
+                                  k, (unsigned long long)skip);
+                BatchItem sk{};
+                sk.count = skip;
+                sk.kind = -1;
+                cur.items.push_back(sk);
+                cur.total += skip;
+                pos += skip;
+            }
+            if (count) {
+                BatchItem bi{};
+                bi.out_off = it.out_offset;
+                bi.count = count;
+                bi.kind = it.kind;
+                cur.items.push_back(bi);
+                cur.total += count;
+                pos += count;
+            }
         }
-        grand += tk.total;
-        order.push_back(std::move(tk));
+        if (!cur.items.empty() || cur.start) {
+            if (cur.items.empty()) {  // ends with a jump: a task that only jumps
+                BatchItem z{};
+                z.kind = -1;
+                cur.items.push_back(z);
+            }
+            grand += cur.total;
+            runs.push_back(std::move(cur));
+        }
     }
     int64_t chunk = 0;
-    if (T::splits(P.sh.mexp)) {
+    if (can_jump) {
         if (!P.resident_split) P.resident_split = T::resident(P.sh.mexp, true);
         if (g_tune.split_chunk > 0) {
             chunk = g_tune.split_chunk;
@@ -670,51 +714,106 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             while ((uint64_t)chunk < per) chunk <<= 1;
         }
     }
+    struct Tk {
+        BatchTask t;
+        std::vector<BatchItem> items;
+        uint64_t total, start;
+        int poly;  // index into the plan's jump polynomials, or -1
+    };
+    std::vector<Tk> order;
     std::vector<int32_t> stage_streams;
-    bool split = false;
-    if (chunk > 0) {
-        std::vector<Tk> out;
-        for (Tk &tk : order) {
-            if (tk.t.nitems != 1 || tk.total <= (uint64_t)chunk + (uint64_t)chunk / 4) {
-                out.push_back(std::move(tk));
-                continue;
-            }
-            const BatchItem it = tk.items[0];
-            const uint64_t k = (it.count + chunk - 1) / chunk;
-            for (uint64_t c = 0; c < k; c++) {
-                Tk ch{};
-                ch.t = tk.t;
-                const uint64_t off = c * (uint64_t)chunk;
-                BatchItem bi = it;
-                bi.count = std::min<uint64_t>((uint64_t)chunk, it.count - off);
-                if (it.kind >= 0) bi.out_off = it.out_off + off * sizeof(W);
-                ch.items.push_back(bi);
-                ch.total = bi.count;
-                if (c > 0) {
-                    int rc = P.jumpPoly(tk.t.pidx, off, &ch.t.jpoly);
-                    if (rc) return rc;
-                }
-                ch.t.wb = (c + 1 == k) ? (int32_t)stage_streams.size() : kWbNone;
-                out.push_back(std::move(ch));
-            }
-            stage_streams.push_back(tk.t.stream);
-            split = true;
+    std::map<std::pair<int, uint64_t>, int> poly_at;  // (parameter set, start) -> index
+    std::vector<const std::vector<uint32_t> *> polys;
+    bool cut = false;
+    for (size_t r0 = 0, r1; r0 < runs.size(); r0 = r1) {
+        for (r1 = r0; r1 < runs.size() && runs[r1].s == runs[r0].s; r1++) {
         }
-        order.swap(out);
+        const int s = runs[r0].s;
+        const size_t first = order.size();
+        for (size_t r = r0; r < r1; r++) {
+            const Run &R = runs[r];
+            uint64_t k = 1;
+            if (chunk > 0 && R.total > (uint64_t)chunk + (uint64_t)chunk / 4) {
+                k = (R.total + (uint64_t)chunk - 1) / (uint64_t)chunk;
+                cut = true;
+            }
+            size_t ii = 0;      // item of R being cut
+            uint64_t used = 0;  // values of it already taken
+            for (uint64_t c = 0; c < k; c++) {
+                Tk tk{};
+                tk.t.stream = s;
+                tk.t.pidx = P.hpidx[s];
+                tk.t.jpoly = nullptr;
+                tk.start = R.start + c * (uint64_t)chunk;
+                tk.poly = -1;
+                uint64_t want = (c + 1 == k) ? ~uint64_t(0) : (uint64_t)chunk;
+                while (ii < R.items.size() && (want || R.items[ii].count == used)) {
+                    BatchItem bi = R.items[ii];
+                    const uint64_t take = std::min(bi.count - used, want);
+                    if (bi.kind >= 0) bi.out_off += used * sizeof(W);
+                    bi.count = take;
+                    tk.items.push_back(bi);
+                    tk.total += take;
+                    want -= take;
+                    used += take;
+                    if (used == R.items[ii].count) {
+                        ii++;
+                        used = 0;
+                    }
+                }
+                order.push_back(std::move(tk));
+            }
+        }
+        const size_t m = order.size() - first;
+        for (size_t q = first; q < order.size(); q++) {
+            Tk &tk = order[q];
+            tk.t.wb = m == 1 ? kWbStream
+                             : (q + 1 == order.size() ? (int32_t)stage_streams.size() : kWbNone);
+            if (!tk.start) continue;
+            auto hit = poly_at.find({tk.t.pidx, tk.start});
+            if (hit == poly_at.end()) {
+                const std::vector<uint32_t> *w = nullptr;
+                int rc = P.jumpPoly(tk.t.pidx, tk.start, &w);
+                if (rc) return rc;
+                hit = poly_at.emplace(std::make_pair(tk.t.pidx, tk.start), (int)polys.size()).first;
+                polys.push_back(w);
+            }
+            tk.poly = hit->second;
+        }
+        if (m > 1) stage_streams.push_back(s);
     }
     // longest task first
     std::stable_sort(order.begin(), order.end(),
                      [](const Tk &a, const Tk &b) { return a.total > b.total; });
     std::vector<BatchTask> tasks;
+    std::vector<int> task_poly;
     std::vector<BatchItem> bitems;
+    int mode = -3;  // the output kind shared by all items, -2 if mixed
     for (Tk &tk : order) {
         tk.t.first = (int)bitems.size();
         tk.t.nitems = (int)tk.items.size();
-        for (const BatchItem &bi : tk.items) bitems.push_back(bi);
+        for (const BatchItem &bi : tk.items) {
+            bitems.push_back(bi);
+            if (bi.count) mode = (mode == -3 || mode == bi.kind) ? bi.kind : -2;
+        }
         tasks.push_back(tk.t);
+        task_poly.push_back(tk.poly);
     }
-    mtgp_gpu_plan *pl = new (std::nothrow) mtgp_gpu_plan();
-    if (!pl) return setErr(MTGP_ERR_ALLOC, "plan allocation");
+    const bool split = !polys.empty();  // the kernel variant with the jump code
+    const size_t pw = (size_t)P.polyWords();
+    // reuse the caller's plan (replan) when given: its device buffers are
+    // kept and only grown, so a server can refill plans without freeing
+    // device memory (cudaFree would wait for every batch in flight)
+    mtgp_gpu_plan *pl = *out;
+    const bool fresh = (pl == nullptr);
+    if (fresh) {
+        pl = new (std::nothrow) mtgp_gpu_plan();
+        if (!pl) return setErr(MTGP_ERR_ALLOC, "plan allocation");
+    } else if (pl->exec) {
+        cudaGraphExecDestroy(pl->exec);
+        pl->exec = nullptr;
+        pl->graph_out = nullptr;
+    }
     pl->bits = T::kBits;
     pl->pool = &P;
     pl->ntasks = (int)tasks.size();
@@ -723,24 +822,61 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->grid = (int)g_tune.batch_grid;
     pl->split = split;
     pl->core = genCore32();
-    pl->chunk = split ? chunk : 0;
+    pl->chunk = cut ? chunk : 0;
     pl->nstage = (int)stage_streams.size();
-    cudaError_t e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
+    auto grow = [](void **p, size_t *cap, size_t need) -> cudaError_t {
+        if (need <= *cap) return cudaSuccess;
+        cudaFree(*p);
+        *p = nullptr;
+        *cap = 0;
+        size_t n = need + need / 4;
+        cudaError_t e = cudaMalloc(p, n);
+        if (e == cudaSuccess) *cap = n;
+        return e;
+    };
+    cudaError_t e = cudaSuccess;
+    if (!pl->d_counter) e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
     if (e == cudaSuccess && pl->nstage) {
-        e = cudaMalloc(&pl->d_stage, sizeof(W) * (size_t)P.stride * pl->nstage);
-        if (e == cudaSuccess) e = cudaMalloc(&pl->d_stage_streams, sizeof(int32_t) * pl->nstage);
+        const size_t need = (sizeof(W) * (size_t)P.stride + sizeof(int32_t)) * pl->nstage;
+        if (need > pl->cap_stage) {
+            cudaFree(pl->d_stage);
+            cudaFree(pl->d_stage_streams);
+            pl->d_stage = nullptr;
+            pl->d_stage_streams = nullptr;
+            pl->cap_stage = 0;
+            const int n = pl->nstage + pl->nstage / 4 + 1;
+            e = cudaMalloc(&pl->d_stage, sizeof(W) * (size_t)P.stride * n);
+            if (e == cudaSuccess) e = cudaMalloc(&pl->d_stage_streams, sizeof(int32_t) * n);
+            if (e == cudaSuccess) pl->cap_stage = (sizeof(W) * (size_t)P.stride + sizeof(int32_t)) * n;
+        }
         if (e == cudaSuccess)
             e = cudaMemcpy(pl->d_stage_streams, stage_streams.data(),
                            sizeof(int32_t) * pl->nstage, cudaMemcpyHostToDevice);
     }
-    if (e == cudaSuccess && !tasks.empty()) e = cudaMalloc(&pl->d_tasks, sizeof(BatchTask) * tasks.size());
-    if (e == cudaSuccess && !bitems.empty()) e = cudaMalloc(&pl->d_items, sizeof(BatchItem) * bitems.size());
+    if (e == cudaSuccess)
+        e = grow(reinterpret_cast<void **>(&pl->d_tasks), &pl->cap_tasks,
+                 sizeof(BatchTask) * tasks.size());
+    if (e == cudaSuccess)
+        e = grow(reinterpret_cast<void **>(&pl->d_items), &pl->cap_items,
+                 sizeof(BatchItem) * bitems.size());
+    if (e == cudaSuccess && !polys.empty()) {
+        e = grow(reinterpret_cast<void **>(&pl->d_polys), &pl->cap_polys,
+                 sizeof(uint32_t) * pw * polys.size());
+        std::vector<uint32_t> flat(pw * polys.size());
+        for (size_t k = 0; k < polys.size(); k++)
+            std::copy(polys[k]->begin(), polys[k]->end(), flat.begin() + k * pw);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(pl->d_polys, flat.data(), sizeof(uint32_t) * flat.size(),
+                           cudaMemcpyHostToDevice);
+        for (size_t q = 0; q < tasks.size(); q++)
+            if (task_poly[q] >= 0) tasks[q].jpoly = pl->d_polys + (size_t)task_poly[q] * pw;
+    }
     if (e == cudaSuccess && !tasks.empty())
         e = cudaMemcpy(pl->d_tasks, tasks.data(), sizeof(BatchTask) * tasks.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !bitems.empty())
         e = cudaMemcpy(pl->d_items, bitems.data(), sizeof(BatchItem) * bitems.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
-        delete pl;
+        if (fresh) delete pl;
         return cudaErr(e, "upload plan");
     }
     *out = pl;
@@ -1149,7 +1285,15 @@ int mtgp64_gpu_set_window_host(mtgp64_gpu_t *h, const uint64_t *w, int size) {
     int mtgp##B##_gpu_pool_plan(mtgp##B##_gpu_pool_t *p, const mtgp_work_item_t *items,          \
                                 int nitems, mtgp_gpu_plan_t **plan) {                            \
         if (!p) return setErr(MTGP_ERR_INVALID, "null pool");                                   \
+        if (!plan) return setErr(MTGP_ERR_INVALID, "null plan pointer");                        \
+        *plan = nullptr;                                                                         \
         return makePlan(p->pool, items, nitems, plan);                                           \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_replan(mtgp##B##_gpu_pool_t *p, const mtgp_work_item_t *items,        \
+                                  int nitems, mtgp_gpu_plan_t *plan) {                           \
+        if (!p || !plan) return setErr(MTGP_ERR_INVALID, "null pool or plan");                  \
+        mtgp_gpu_plan_t *pl = plan;                                                              \
+        return makePlan(p->pool, items, nitems, &pl);                                            \
     }                                                                                            \
     int mtgp##B##_gpu_pool_submit(mtgp##B##_gpu_pool_t *p, const mtgp_work_item_t *items,        \
                                   int nitems, void *out, void *s) {                              \

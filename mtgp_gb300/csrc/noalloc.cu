@@ -105,6 +105,7 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
         if (it.stream >= (uint32_t)nstreams) return fail(MTGP_ERR_INVALID, "stream out of range");
         if (it.kind < -1 || it.kind > 4) return fail(MTGP_ERR_INVALID, "unknown output kind");
         if (it.kind >= 0 && it.out_offset % 4) return fail(MTGP_ERR_INVALID, "misaligned offset");
+        if (it.skip) return fail(MTGP_ERR_INVALID, "skip is not supported here");
         if (it.count == 0) continue;
         mode = (mode == -3 || mode == it.kind) ? it.kind : -2;
         cnt[it.stream]++;

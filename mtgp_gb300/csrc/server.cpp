@@ -1,0 +1,398 @@
+// server.cpp -- continuous-batching request loop over resident stream pools.
+//
+// The streams of a 32-bit and a 64-bit pool stay resident on the device.
+// Clients submit requests (stream, skip, count, output kind, destination);
+// a scheduler thread admits them into batches and runs each batch as one
+// persistent launch (the batched kernels, through the public plan API):
+//   - up to `slots` batches are in flight at once, each on its own CUDA
+//     stream, so a batch admitted while others run overlaps them on the GPU;
+//   - a request is admitted when a slot is free and its output fits in the
+//     device output arena (the memory budget); admission is first-come,
+//     first-served, and a request whose stream is busy waits (requests of one
+//     stream run in submission order, each seeing the stream where the
+//     previous one left it);
+//   - a request's skip is done by generation when short and by a GF(2) jump
+//     when long (mtgp_work_item_t);
+//   - when a batch completes, results are copied to the callers'
+//     destinations (device or host memory; none = discard), the arena space
+//     is returned and the latency (completion - submission) is recorded.
+// A request's output depends only on its stream's position, so it is the
+// same alone and in any mix.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+// First-fit allocator over the output arena, 256-byte granules.
+class Arena {
+  public:
+    void init(uint64_t n) {
+        size_ = n;
+        free_.clear();
+        free_[0] = n;
+    }
+    static uint64_t round(uint64_t n) { return (n + 255) & ~uint64_t(255); }
+    bool alloc(uint64_t n, uint64_t *off) {
+        n = round(n);
+        if (n == 0) {
+            *off = 0;
+            return true;
+        }
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < n) continue;
+            *off = it->first;
+            const uint64_t rest = it->second - n, at = it->first + n;
+            free_.erase(it);
+            if (rest) free_[at] = rest;
+            return true;
+        }
+        return false;
+    }
+    void release(uint64_t off, uint64_t n) {
+        n = round(n);
+        if (n == 0) return;
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    uint64_t size() const { return size_; }
+
+  private:
+    uint64_t size_ = 0;
+    std::map<uint64_t, uint64_t> free_;
+};
+
+struct Req {
+    uint64_t ticket;
+    int pool;
+    uint32_t stream;
+    int kind;
+    uint64_t skip, count, bytes, off;
+    void *dst;
+    Clock::time_point t_submit;
+};
+
+struct Slot {
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev = nullptr;
+    mtgp_gpu_plan_t *plan[2] = {nullptr, nullptr};
+    std::vector<Req> reqs;
+    bool busy = false;
+};
+
+}  // namespace
+
+struct mtgp_server {
+    mtgp32_gpu_pool_t *p32 = nullptr;
+    mtgp64_gpu_pool_t *p64 = nullptr;
+    int nstreams[2] = {0, 0};
+    int device = 0;
+    unsigned char *d_arena = nullptr;
+    Arena arena;
+    std::vector<Slot> slots;
+    int max_batch = 4096;
+    std::mutex mu;
+    std::condition_variable cv, cv_done;
+    std::deque<Req> pending;
+    std::vector<char> busy[2];
+    std::thread th;
+    std::atomic<bool> stop{false};
+    uint64_t submitted = 0, completed = 0, bytes_done = 0, batches = 0;
+    std::vector<double> latency;  // seconds, by ticket - 1; -1 = not done
+    std::vector<int> status;      // MTGP_* by ticket - 1
+    Clock::time_point t0;
+
+    void loop();
+    int launch(Slot &sl, std::vector<Req> &reqs);
+};
+
+int mtgp_server::launch(Slot &sl, std::vector<Req> &reqs) {
+    std::vector<mtgp_work_item_t> items[2];
+    for (const Req &r : reqs) {
+        mtgp_work_item_t it{};
+        it.stream = r.stream;
+        it.kind = r.kind;
+        it.count = r.count;
+        it.out_offset = r.off;
+        it.skip = r.skip;
+        items[r.pool].push_back(it);
+    }
+    for (int p = 0; p < 2; p++) {
+        if (items[p].empty()) continue;
+        int rc;
+        const int n = (int)items[p].size();
+        if (!sl.plan[p]) {
+            rc = p == 0 ? mtgp32_gpu_pool_plan(p32, items[p].data(), n, &sl.plan[p])
+                        : mtgp64_gpu_pool_plan(p64, items[p].data(), n, &sl.plan[p]);
+        } else {
+            rc = p == 0 ? mtgp32_gpu_pool_replan(p32, items[p].data(), n, sl.plan[p])
+                        : mtgp64_gpu_pool_replan(p64, items[p].data(), n, sl.plan[p]);
+        }
+        if (!rc) rc = mtgp_gpu_plan_launch(sl.plan[p], d_arena, sl.cs);
+        if (rc) return rc;
+    }
+    for (const Req &r : reqs) {
+        if (!r.dst || !r.bytes) continue;
+        cudaError_t e = cudaMemcpyAsync(r.dst, d_arena + r.off, r.bytes, cudaMemcpyDefault, sl.cs);
+        if (e != cudaSuccess) return mtgp::recordError(MTGP_ERR_CUDA, cudaGetErrorString(e));
+    }
+    cudaError_t e = cudaEventRecord(sl.ev, sl.cs);
+    if (e != cudaSuccess) return mtgp::recordError(MTGP_ERR_CUDA, cudaGetErrorString(e));
+    return MTGP_OK;
+}
+
+void mtgp_server::loop() {
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    while (!stop.load()) {
+        bool progressed = false;
+        // retire finished batches
+        for (Slot &sl : slots) {
+            if (!sl.busy) continue;
+            const cudaError_t q = cudaEventQuery(sl.ev);
+            if (q == cudaErrorNotReady) continue;
+            const Clock::time_point now = Clock::now();
+            for (const Req &r : sl.reqs) {
+                latency[r.ticket - 1] = std::chrono::duration<double>(now - r.t_submit).count();
+                status[r.ticket - 1] = q == cudaSuccess ? MTGP_OK : MTGP_ERR_CUDA;
+                arena.release(r.off, r.bytes);
+                busy[r.pool][r.stream] = 0;
+                completed++;
+                bytes_done += r.bytes;
+            }
+            sl.reqs.clear();
+            sl.busy = false;
+            progressed = true;
+        }
+        if (progressed) cv_done.notify_all();
+        // admit pending requests into a free slot
+        Slot *fs = nullptr;
+        for (Slot &sl : slots)
+            if (!sl.busy) {
+                fs = &sl;
+                break;
+            }
+        if (fs && !pending.empty()) {
+            std::vector<Req> take;
+            for (auto it = pending.begin(); it != pending.end() && (int)take.size() < max_batch;) {
+                if (busy[it->pool][it->stream]) {
+                    ++it;
+                    continue;
+                }
+                uint64_t off = 0;
+                if (!arena.alloc(it->bytes, &off)) break;  // first come, first served
+                it->off = off;
+                busy[it->pool][it->stream] = 1;
+                take.push_back(*it);
+                it = pending.erase(it);
+            }
+            if (!take.empty()) {
+                lk.unlock();
+                const int rc = launch(*fs, take);
+                lk.lock();
+                if (rc) {
+                    for (const Req &r : take) {
+                        latency[r.ticket - 1] = 0;
+                        status[r.ticket - 1] = rc;
+                        arena.release(r.off, r.bytes);
+                        busy[r.pool][r.stream] = 0;
+                        completed++;
+                    }
+                    cv_done.notify_all();
+                } else {
+                    fs->reqs.swap(take);
+                    fs->busy = true;
+                    batches++;
+                }
+                progressed = true;
+            }
+        }
+        if (!progressed) cv.wait_for(lk, std::chrono::microseconds(20));
+    }
+}
+
+extern "C" {
+
+int mtgp_server_create(mtgp_server_t **out, mtgp32_gpu_pool_t *p32, mtgp64_gpu_pool_t *p64,
+                       uint64_t budget_bytes, int slots, int max_batch) {
+    if (!out || (!p32 && !p64) || budget_bytes < 256 || slots < 1 || max_batch < 1)
+        return mtgp::recordError(MTGP_ERR_INVALID, "bad server arguments");
+    *out = nullptr;
+    mtgp_server *s = new (std::nothrow) mtgp_server();
+    if (!s) return mtgp::recordError(MTGP_ERR_ALLOC, "server allocation");
+    s->p32 = p32;
+    s->p64 = p64;
+    s->nstreams[0] = p32 ? mtgp32_gpu_pool_size(p32) : 0;
+    s->nstreams[1] = p64 ? mtgp64_gpu_pool_size(p64) : 0;
+    s->busy[0].assign(s->nstreams[0], 0);
+    s->busy[1].assign(s->nstreams[1], 0);
+    s->max_batch = max_batch;
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_arena, budget_bytes);
+    if (e != cudaSuccess) {
+        delete s;
+        return mtgp::recordError(MTGP_ERR_ALLOC, cudaGetErrorString(e));
+    }
+    s->arena.init(budget_bytes);
+    s->slots.resize(slots);
+    for (Slot &sl : s->slots) {
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.cs, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        mtgp_server_destroy(s);
+        return mtgp::recordError(MTGP_ERR_CUDA, cudaGetErrorString(e));
+    }
+    s->t0 = Clock::now();
+    s->th = std::thread([s] { s->loop(); });
+    *out = s;
+    return MTGP_OK;
+}
+
+int mtgp_server_submit(mtgp_server_t *s, int pool, uint32_t stream, int kind, uint64_t skip,
+                       uint64_t count, void *dst, uint64_t *ticket) {
+    if (!s || !ticket) return mtgp::recordError(MTGP_ERR_INVALID, "null server or ticket");
+    if (pool < 0 || pool > 1 || stream >= (uint32_t)s->nstreams[pool])
+        return mtgp::recordError(MTGP_ERR_INVALID, "no such pool or stream");
+    if (kind < -1 || kind > 4) return mtgp::recordError(MTGP_ERR_INVALID, "unknown output kind");
+    const uint64_t bytes = kind < 0 ? 0 : count * (pool == 0 ? 4u : 8u);
+    if (Arena::round(bytes) > s->arena.size())
+        return mtgp::recordError(MTGP_ERR_BUDGET, "request larger than the device budget");
+    std::lock_guard<std::mutex> lk(s->mu);
+    Req r{};
+    r.ticket = ++s->submitted;
+    r.pool = pool;
+    r.stream = stream;
+    r.kind = kind;
+    r.skip = skip;
+    r.count = count;
+    r.bytes = bytes;
+    r.dst = dst;
+    r.t_submit = Clock::now();
+    s->latency.push_back(-1.0);
+    s->status.push_back(1);
+    s->pending.push_back(r);
+    *ticket = r.ticket;
+    s->cv.notify_one();
+    return MTGP_OK;
+}
+
+int mtgp_server_cancel(mtgp_server_t *s, uint64_t ticket) {
+    if (!s) return mtgp::recordError(MTGP_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto it = s->pending.begin(); it != s->pending.end(); ++it) {
+        if (it->ticket != ticket) continue;
+        s->latency[ticket - 1] = 0;
+        s->status[ticket - 1] = MTGP_ERR_BUSY;  // cancelled before it ran
+        s->completed++;
+        s->pending.erase(it);
+        s->cv_done.notify_all();
+        return MTGP_OK;
+    }
+    return mtgp::recordError(MTGP_ERR_INVALID, "ticket is not pending");
+}
+
+int mtgp_server_wait(mtgp_server_t *s, uint64_t ticket, double timeout_s, int *status) {
+    if (!s || ticket == 0) return mtgp::recordError(MTGP_ERR_INVALID, "bad wait");
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (ticket > s->submitted) return mtgp::recordError(MTGP_ERR_INVALID, "unknown ticket");
+    const bool ok = s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                                        [&] { return s->latency[ticket - 1] >= 0; });
+    if (!ok) return mtgp::recordError(MTGP_ERR_TIMEOUT, "request not done in time");
+    if (status) *status = s->status[ticket - 1];
+    return MTGP_OK;
+}
+
+int mtgp_server_drain(mtgp_server_t *s, double timeout_s) {
+    if (!s) return mtgp::recordError(MTGP_ERR_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    const bool ok = s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                                        [&] { return s->completed == s->submitted; });
+    return ok ? MTGP_OK : mtgp::recordError(MTGP_ERR_TIMEOUT, "requests still in flight");
+}
+
+int mtgp_server_results(mtgp_server_t *s, double *latency, int *status, uint64_t cap,
+                        uint64_t *n) {
+    if (!s) return mtgp::recordError(MTGP_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    const uint64_t m = std::min<uint64_t>(cap, s->latency.size());
+    for (uint64_t k = 0; k < m; k++) {
+        if (latency) latency[k] = s->latency[k];
+        if (status) status[k] = s->status[k];
+    }
+    if (n) *n = s->latency.size();
+    return MTGP_OK;
+}
+
+int mtgp_server_stats(mtgp_server_t *s, uint64_t *completed, uint64_t *bytes, uint64_t *batches) {
+    if (!s) return mtgp::recordError(MTGP_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (completed) *completed = s->completed;
+    if (bytes) *bytes = s->bytes_done;
+    if (batches) *batches = s->batches;
+    return MTGP_OK;
+}
+
+int mtgp_server_replay(mtgp_server_t *s, const mtgp_request_t *reqs, const double *arrival_s,
+                       int n, double *wall_s) {
+    if (!s || n < 0 || (n > 0 && (!reqs || !arrival_s)))
+        return mtgp::recordError(MTGP_ERR_INVALID, "bad trace");
+    const Clock::time_point start = Clock::now();
+    for (int k = 0; k < n; k++) {
+        const Clock::time_point at =
+            start + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[k]));
+        while (Clock::now() < at) {
+            const auto left = at - Clock::now();
+            if (left > std::chrono::microseconds(200)) std::this_thread::sleep_for(left / 2);
+        }
+        uint64_t t = 0;
+        const mtgp_request_t &r = reqs[k];
+        int rc = mtgp_server_submit(s, r.pool, r.stream, r.kind, r.skip, r.count, r.dst, &t);
+        if (rc) return rc;
+    }
+    int rc = mtgp_server_drain(s, 600.0);
+    if (wall_s) *wall_s = std::chrono::duration<double>(Clock::now() - start).count();
+    return rc;
+}
+
+void mtgp_server_destroy(mtgp_server_t *s) {
+    if (!s) return;
+    if (s->th.joinable()) {
+        mtgp_server_drain(s, 600.0);
+        s->stop.store(true);
+        s->cv.notify_all();
+        s->th.join();
+    }
+    for (Slot &sl : s->slots) {
+        if (sl.cs) cudaStreamSynchronize(sl.cs);
+        for (int p = 0; p < 2; p++) mtgp_gpu_plan_free(sl.plan[p]);
+        if (sl.ev) cudaEventDestroy(sl.ev);
+        if (sl.cs) cudaStreamDestroy(sl.cs);
+    }
+    cudaFree(s->d_arena);
+    delete s;
+}
+
+}  // extern "C"

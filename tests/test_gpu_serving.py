@@ -1,0 +1,253 @@
+"""Skips inside batched work items (generated when short, GF(2) jump when
+long), plan reuse, and the continuous-batching server: bit-exact vs the
+oracle, the same result alone and in a mix, and admission under a device
+memory budget."""
+import numpy as np
+import pytest
+import torch
+
+from mtgp_gb300.params import jump_table, load_table
+from gpu_util import np_bits
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(32, "mtgp32_fast_11213"), (64, "mtgp64dc_fast_11213")]
+DT = {32: torch.int32, 64: torch.int64}
+
+
+def _pool(bits, table, n, seed0=100):
+    from mtgp_gb300.api import Pool
+    tbl = load_table(table)
+    plist = [tbl[i % 3] for i in range(3)]
+    pidx = np.arange(n) % 3
+    seeds = np.arange(n) + seed0
+    return Pool.create(plist, seeds, pidx), plist, pidx, seeds
+
+
+def _masked_equal(a, b, p):
+    return ((int(a[0]) ^ int(b[0])) & int(p.mask)) == 0 and np.array_equal(a[1:], b[1:])
+
+
+@pytest.mark.parametrize("bits,table", CASES)
+def test_skip_items_vs_oracle(gpu, orc, bits, table):
+    """Short skips are generated; skips of 2^17 or more (first item or
+    later) start a new task that jumps inside the kernel; a jump followed by
+    a long request that is split into chunks; an advance-only item."""
+    from mtgp_gb300.api import work_items
+    pool, plist, pidx, seeds = _pool(bits, table, 6)
+    #        stream kind count    skip
+    spec = [(0, 0, 1000, 100),
+            (0, 2, 777, 5000),            # later item: generated skip
+            (1, 0, 4000, 200000),         # first item: jump
+            (1, 0, 100, 1 << 17),         # later item: a second task that jumps
+            (2, 1, 3_000_000, (1 << 20) + 7),  # jump, then a split request
+            (3, -1, 0, 300000),           # jump only
+            (4, 3, 5000, 0),
+            (5, 4, 2500, 131071)]         # just below the jump threshold
+    esz = bits // 8
+    offs, pos = [], 0
+    for s, k, c, _ in spec:
+        offs.append(pos)
+        pos += c * esz if k >= 0 else 0
+    items = work_items([x[0] for x in spec], [x[1] for x in spec], [x[2] for x in spec], offs,
+                       [x[3] for x in spec])
+    out = torch.zeros(pos // 4 + 16, dtype=torch.int32, device="cuda")
+    pool.submit(items, out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(np.uint8)
+    gens = {}
+    for (s, k, c, sk), off in zip(spec, offs):
+        o = gens.setdefault(s, orc.gen(plist[pidx[s]], seed=int(seeds[s])))
+        o.skip(sk)
+        if k < 0:
+            o.skip(c)
+            continue
+        ref = np_bits(o.fill(k, c), bits).view(np.uint8)
+        assert np.array_equal(got[off:off + ref.size], ref), (s, k, c, sk)
+    w = pool.windows()
+    for s, o in gens.items():
+        assert _masked_equal(w[s], o.window(), plist[pidx[s]]), s
+
+
+def test_skip_2_40_by_jump(gpu, orc):
+    """A skip of 2^40 (far beyond stepping) equals the oracle's jump by
+    X^(2^40) mod chi."""
+    from mtgp_gb300.api import work_items
+    pool, plist, pidx, seeds = _pool(32, "mtgp32_fast_11213", 3)
+    steps = 1 << 40
+    items = work_items([1], [0], [5000], [0], [steps])
+    out = torch.zeros(5000, dtype=torch.int32, device="cuda")
+    pool.submit(items, out)
+    torch.cuda.synchronize()
+    p = plist[pidx[1]]
+    chi_bits = (orc.gen(p, seed=1).fill(0, 2 * p.mexp) & 1).astype(np.uint8)
+    d, chi = orc.minpoly(chi_bits)
+    poly = orc.powxmod(steps, chi, d).view(np.uint32)[:351]
+    o = orc.gen(p, seed=int(seeds[1]))
+    o.jump_words(poly)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), o.fill(0, 5000))
+
+
+@pytest.mark.parametrize("bits,table", CASES)
+def test_replan_reuses_plan(gpu, orc, bits, table):
+    """One plan refilled with new items (more of them, so its buffers grow)
+    keeps producing the oracle's sequence."""
+    from mtgp_gb300.api import work_items
+    pool, plist, pidx, seeds = _pool(bits, table, 12)
+    gens = [orc.gen(plist[pidx[s]], seed=int(seeds[s])) for s in range(12)]
+    rng = np.random.default_rng(5)
+    plan = None
+    for rnd, n in enumerate((3, 12, 7, 12)):
+        streams = rng.permutation(12)[:n]
+        counts = rng.integers(1, 30000, n)
+        counts[0] = 2_500_000 if rnd == 1 else counts[0]   # one split request
+        esz = bits // 8
+        offs = np.concatenate([[0], np.cumsum(counts)[:-1]]) * esz
+        items = work_items(streams, np.zeros(n), counts, offs)
+        plan = pool.plan(items) if plan is None else pool.replan(items, plan)
+        out = torch.zeros(int(counts.sum()), dtype=DT[bits], device="cuda")
+        plan.launch(out)
+        torch.cuda.synchronize()
+        got = np_bits(out.cpu().numpy(), bits)
+        for j in range(n):
+            ref = gens[streams[j]].fill(0, int(counts[j]))
+            o = int(offs[j]) // esz
+            assert np.array_equal(got[o:o + counts[j]], ref), (rnd, j)
+
+
+def _server_pools():
+    from mtgp_gb300.api import Pool
+    p32 = load_table("mtgp32_fast_11213")[0]
+    p64 = load_table("mtgp64dc_fast_11213")[0]
+    a = Pool.substreams(p32, 4321, 32, jump_table(32))
+    b = Pool.substreams(p64, 4321, 8, jump_table(64))
+    return a, b, p32, p64
+
+
+def _oracle_streams(orc, pool, params):
+    gens = []
+    for row in pool.windows():
+        o = orc.gen(params, seed=1)
+        o.set_window(row)
+        gens.append(o)
+    return gens
+
+
+def _trace(rng, n, nst32, nst64):
+    reqs = []
+    for _ in range(n):
+        pool = int(rng.random() < 0.3)
+        st = int(rng.integers(0, nst64 if pool else nst32))
+        kind = int(rng.choice([0, 0, 0, 2, 1, 3, 4, -1]))
+        count = int(min(rng.lognormal(np.log(20000), 1.5), 3_000_000))
+        skip = 0
+        u = rng.random()
+        if u < 0.1:
+            skip = 1 << int(rng.integers(17, 41))
+        elif u < 0.2:
+            skip = int(rng.integers(1, 5000))
+        reqs.append((pool, st, kind, count, skip))
+    return reqs
+
+
+def test_server_vs_oracle(gpu, orc):
+    """A random trace through the server (several batches in flight, both
+    pools, skips, advance-only requests) equals each stream's sequence
+    replayed in submission order."""
+    from mtgp_gb300.api import Server
+    a, b, p32, p64 = _server_pools()
+    ga, gb = _oracle_streams(orc, a, p32), _oracle_streams(orc, b, p64)
+    # the oracle's jump polynomials for the jumped skips
+    chis = {}
+    for bits, p in ((32, p32), (64, p64)):
+        seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
+        chis[bits] = orc.minpoly((seq & 1).astype(np.uint8))
+    rng = np.random.default_rng(11)
+    trace = _trace(rng, 300, 32, 8)
+    srv = Server(a, b, budget_bytes=64 << 20, slots=3, max_batch=64)
+    outs, tickets = [], []
+    for pool, st, kind, count, skip in trace:
+        dst = None if kind < 0 else torch.empty(count, dtype=DT[32 if pool == 0 else 64],
+                                                device="cuda")
+        outs.append(dst)
+        tickets.append(srv.submit(pool, st, kind, count, dst, skip=skip))
+    for t in tickets:
+        assert srv.wait(t, 120.0) == 0
+    lat, status = srv.results()
+    assert (status == 0).all() and (lat >= 0).all()
+    done, nbytes, batches = srv.stats()
+    assert done == len(trace) and batches >= 2
+    srv.close()
+    for (pool, st, kind, count, skip), dst in zip(trace, outs):
+        bits = 32 if pool == 0 else 64
+        o = (ga if pool == 0 else gb)[st]
+        if skip >= (1 << 17):
+            # skips up to 2^40: the oracle jumps by X^skip mod chi (outputs
+            # equal stepping's)
+            d, chi = chis[bits]
+            o.jump_words(orc.powxmod(skip, chi, d).view(np.uint32)[:351])
+        else:
+            o.skip(skip)
+        if kind < 0:
+            o.skip(count)
+            continue
+        ref = o.fill(kind, count)
+        assert np.array_equal(np_bits(dst.cpu().numpy(), bits), np_bits(ref, bits)), (pool, st)
+
+
+def test_server_same_alone_and_in_mix(gpu):
+    """Each stream's first request gives the same values when it is served
+    alone and when it is batched with hundreds of others."""
+    from mtgp_gb300.api import Server
+    rng = np.random.default_rng(23)
+    trace = _trace(rng, 400, 32, 8)
+    a, b, _, _ = _server_pools()
+    srv = Server(a, b, budget_bytes=256 << 20, slots=4, max_batch=512)
+    outs = []
+    for pool, st, kind, count, skip in trace:
+        dst = torch.empty(max(count, 1), dtype=DT[32 if pool == 0 else 64], device="cuda")
+        outs.append(dst)
+        srv.submit(pool, st, max(kind, 0), count, dst, skip=skip)
+    srv.drain()
+    srv.close()
+    seen = set()
+    for j, (pool, st, kind, count, skip) in enumerate(trace):
+        if (pool, st) in seen:
+            continue
+        seen.add((pool, st))
+        a1, b1, _, _ = _server_pools()
+        one = Server(a1, b1, budget_bytes=64 << 20, slots=1, max_batch=1)
+        dst = torch.empty(max(count, 1), dtype=DT[32 if pool == 0 else 64], device="cuda")
+        assert one.wait(one.submit(pool, st, max(kind, 0), count, dst, skip=skip)) == 0
+        one.close()
+        assert torch.equal(dst, outs[j]), (pool, st)
+        if len(seen) >= 6:
+            break
+
+
+def test_server_budget_and_host_destination(gpu, orc):
+    """Requests larger than the budget are refused; a queue whose total is
+    many times the budget is admitted piece by piece; results land in pinned
+    host memory."""
+    from mtgp_gb300._lib import MTGPError
+    from mtgp_gb300.api import Server
+    a, b, p32, _ = _server_pools()
+    ga = _oracle_streams(orc, a, p32)
+    srv = Server(a, None, budget_bytes=1 << 20, slots=2, max_batch=8)
+    with pytest.raises(MTGPError) as e:
+        srv.submit(0, 0, 0, (1 << 18) + 1)
+    assert e.value.code == -7
+    with pytest.raises(MTGPError):
+        srv.submit(1, 0, 0, 10)          # no 64-bit pool
+    outs, tickets = [], []
+    for k in range(40):
+        dst = torch.empty(200_000, dtype=torch.int32).pin_memory()
+        outs.append(dst)
+        tickets.append(srv.submit(0, k % 32, 0, 200_000, dst))
+    srv.drain()
+    lat, st = srv.results()
+    assert (st == 0).all()
+    srv.close()
+    for k in range(40):
+        ref = ga[k % 32].fill(0, 200_000)
+        assert np.array_equal(outs[k].numpy().view(np.uint32), ref), k
