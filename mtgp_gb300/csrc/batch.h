@@ -18,30 +18,34 @@ struct BatchTask {
     int32_t first;     // first item (items of one task are consecutive)
     int32_t nitems;
     int32_t pidx;      // parameter-set index of the stream
-    // Chunk of a split request: the task starts from the stream's window
-    // jumped by this polynomial (uint32-array form); null = no jump.
-    const uint32_t *jpoly;
+    // The task starts from the stream's window jumped by polynomial j0,
+    // then by j1 (indices into BatchLaunch::polys, uint32-array form;
+    // -1 = none): a task that starts later in the stream than the window.
+    int32_t j0, j1;
     // Where the advanced window goes: kWbStream = back to the stream,
-    // kWbNone = nowhere (a chunk that is not the last), k >= 0 = staging
-    // slot k (the last chunk; copied to the stream after the launch, so no
-    // chunk can read a window that another chunk already advanced).
+    // kWbNone = nowhere (a task that is not the stream's last), k >= 0 =
+    // staging slot k (the last task of a stream with several; copied to the
+    // stream after the launch, so no task can read a window that another
+    // task already advanced).
     int32_t wb;
     int32_t pad_;
 };
+static_assert(sizeof(BatchTask) == 32, "BatchTask is 32 bytes");
 constexpr int32_t kWbStream = -1;
 constexpr int32_t kWbNone = -2;
 
 // grid <= 0: size the grid to the resident-CTA capacity of the GPU.
 // mode: the output kind shared by every item (-1 = all skips), or -2 when
 // items mix kinds.
-// One batched launch.  split: some tasks carry jpoly (the kernel variant
-// with the jump code runs).  After the kernel, staged final windows (stage
-// slot k -> stream stage_streams[k]) are copied back.
+// One batched launch.  split: some tasks start with a jump (the kernel
+// variant with the jump code runs).  After the kernel, staged final windows
+// (stage slot k -> stream stage_streams[k]) are copied back.
 struct BatchLaunch {
     int mexp, mode, grid;
     int core;                       // 32-bit generation core (1 or 4) when not split
     bool split;
     int nwords;                     // words of every jump polynomial
+    const uint32_t *polys;          // jump polynomials, nwords words each
     const BatchTask *tasks;
     int ntasks;
     const BatchItem *items;

@@ -47,15 +47,26 @@ __device__ __forceinline__ W *endWindow(const BatchTask &T, W *states, W *stage,
                              : nullptr;
 }
 
+// The task's start: the window jumped by polys[j0], then by polys[j1].
+template <class Tr, class G>
+__device__ __forceinline__ void jump_task(typename Tr::W *buf, const typename Tr::Lane &L,
+                                          const BatchTask &T, const uint32_t *polys, int nwords) {
+    const int j0 = T.j0, j1 = T.j1;
+    jump_chain_impl<Tr, G>(
+        buf, L, [=](int c) { return polys + (size_t)(c ? j1 : j0) * nwords; }, j1 >= 0 ? 2 : 1,
+        nwords);
+}
+
 // MODE >= -1: every item has output kind MODE (-1 = skip); MODE == -2:
 // items of any kind (the kind is switched per item).  SPLIT: tasks may
-// carry a jump polynomial.
+// start with a jump.
 template <int N, int TN, int B, int MODE, bool SPLIT>
 __global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1280 : 2048) / TN)
 k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
-          unsigned *__restrict__ counter, uint32_t *__restrict__ stage, int nwords) {
+          unsigned *__restrict__ counter, uint32_t *__restrict__ stage,
+          const uint32_t *__restrict__ polys, int nwords) {
     __shared__ __align__(16) uint32_t buf[B];
     __shared__ int s_task;
     for (;;) {
@@ -74,7 +85,7 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
             static_assert(G::NT == TN, "jump geometry must use the kernel's threads");
             static_assert(G::template bytes<uint32_t>(N / 32 + 1) <= sizeof(uint32_t) * B,
                           "jump buffers must fit the generation buffer");
-            if (T.jpoly) jump_one<Tr32, G>(buf, L, T.jpoly, nwords);
+            if (T.j0 >= 0) jump_task<Tr32, G>(buf, L, T, polys, nwords);
         }
         __syncthreads();
         for (int i = 0; i < T.nitems; i++) {
@@ -108,11 +119,13 @@ __global__ void __launch_bounds__(W / 4, MODE == -2 ? 1 : 1280 / W * 4)
 k_batch32x4(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
             const BatchTask *__restrict__ tasks, int ntasks,
             const BatchItem *__restrict__ items, char *__restrict__ out,
-            unsigned *__restrict__ counter, uint32_t *__restrict__ stage, int nwords) {
+            unsigned *__restrict__ counter, uint32_t *__restrict__ stage,
+            const uint32_t *__restrict__ polys, int nwords) {
     constexpr int T = W / 4;
     constexpr int PW = Geo4<N, W, B>::PW;
     __shared__ __align__(16) uint32_t buf[Geo4<N, W, B>::BUF];
     __shared__ int s_task;
+    (void)polys;
     (void)nwords;
     for (;;) {
         if (threadIdx.x == 0) s_task = (int)atomicAdd(counter, 1u);
@@ -155,7 +168,8 @@ __global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1280 : 2048) / T
 k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
-          unsigned *__restrict__ counter, uint64_t *__restrict__ stage, int nwords) {
+          unsigned *__restrict__ counter, uint64_t *__restrict__ stage,
+          const uint32_t *__restrict__ polys, int nwords) {
     __shared__ __align__(16) uint64_t buf[B];
     __shared__ int s_task;
     for (;;) {
@@ -174,7 +188,7 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
             static_assert(G::NT == TN, "jump geometry must use the kernel's threads");
             static_assert(G::template bytes<uint64_t>(N * 2) <= sizeof(uint64_t) * B,
                           "jump buffers must fit the generation buffer");
-            if (T.jpoly) jump_one<Tr64, G>(buf, L, T.jpoly, nwords);
+            if (T.j0 >= 0) jump_task<Tr64, G>(buf, L, T, polys, nwords);
         }
         __syncthreads();
         for (int i = 0; i < T.nitems; i++) {
@@ -235,7 +249,7 @@ static cudaError_t go(K kern, int tn, const BatchLaunch &b, const P *params, W *
     if (e != cudaSuccess) return e;
     kern<<<grid, tn, 0, s>>>(params, states, b.tasks, b.ntasks, b.items,
                              static_cast<char *>(b.out), b.counter, static_cast<W *>(b.stage),
-                             b.nwords);
+                             b.polys, b.nwords);
     return cudaGetLastError();
 }
 

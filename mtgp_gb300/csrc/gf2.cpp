@@ -78,8 +78,16 @@ Poly mulmod(const Poly &a, const Poly &b, const Poly &m, int dm) {
     return r;
 }
 
-// Squaring in GF(2)[x] spreads the bits: coefficient i moves to 2i.
+static Poly spread(const Poly &a);
+
 Poly sqrmod(const Poly &a, const Poly &m, int dm) {
+    Poly r = spread(a);
+    reduce(r, m, dm);
+    return r;
+}
+
+// Spread the bits of a: coefficient i moves to 2i (squaring in GF(2)[x]).
+static Poly spread(const Poly &a) {
     Poly r(2 * a.size() + 1, 0);
     for (size_t k = 0; k < a.size(); k++) {
         uint64_t x = a[k];
@@ -93,31 +101,139 @@ Poly sqrmod(const Poly &a, const Poly &m, int dm) {
             r[2 * k + h] = v;
         }
     }
-    reduce(r, m, dm);
     return r;
 }
 
-Poly powxmod(const std::vector<uint32_t> &e, const Poly &m, int dm) {
-    const int W = (dm + 63) / 64;
+Poly mulComb(const Poly &a, const Poly &b) {
+    const size_t tw = b.size() + 1;
+    // t[v] = v(X) * b(X) for every byte v
+    std::vector<uint64_t> t(256 * tw, 0);
+    for (int i = 0; i < 8; i++) {
+        uint64_t *d = &t[(size_t)(1u << i) * tw];
+        for (size_t k = 0; k < b.size(); k++) {
+            d[k] ^= b[k] << i;
+            if (i) d[k + 1] ^= b[k] >> (64 - i);
+        }
+    }
+    for (unsigned v = 3; v < 256; v++) {
+        const unsigned lo = v & (0u - v);
+        if (lo == v) continue;
+        const uint64_t *x = &t[(size_t)lo * tw], *y = &t[(size_t)(v ^ lo) * tw];
+        uint64_t *d = &t[(size_t)v * tw];
+        for (size_t k = 0; k < tw; k++) d[k] = x[k] ^ y[k];
+    }
+    // comb: byte k of every word of a, from the top byte down, shifting the
+    // partial product by 8 between bytes
+    Poly r(a.size() + tw, 0);
+    for (int k = 7; k >= 0; k--) {
+        for (size_t i = 0; i < a.size(); i++) {
+            const unsigned v = (unsigned)(a[i] >> (8 * k)) & 255u;
+            if (!v) continue;
+            const uint64_t *x = &t[(size_t)v * tw];
+            uint64_t *d = &r[i];
+            for (size_t q = 0; q < tw; q++) d[q] ^= x[q];
+        }
+        if (k)
+            for (size_t q = r.size() - 1; q > 0; q--) r[q] = (r[q] << 8) | (r[q - 1] >> 56);
+        if (k) r[0] <<= 8;
+    }
+    return r;
+}
+
+Modulus::Modulus(const Poly &m, int dm) : m_(m), dm_(dm) {
+    m_.resize((size_t)dm / 64 + 1, 0);
+    tw_ = dm / 64 + 2;
+    // coefficients dm-1 .. dm-7 of m: mrev bit 7-i = coefficient dm-i
+    unsigned mrev = 0;
+    for (int i = 0; i <= 7; i++) {
+        const int c = dm - i;
+        if (c >= 0 && ((m_[(size_t)c >> 6] >> (c & 63)) & 1u)) mrev |= 1u << (7 - i);
+    }
+    tab_.assign((size_t)8 * 256 * tw_, 0);
+    for (unsigned b = 1; b < 256; b++) {
+        // quotient q clearing coefficients dm..dm+7 (= b) from the top
+        unsigned res = b, q = 0;
+        for (int k = 7; k >= 0; k--) {
+            if (!((res >> k) & 1u)) continue;
+            q |= 1u << k;
+            res ^= mrev >> (7 - k);  // m * X^k touches window bits k, k-1, ..., 0
+        }
+        uint64_t *d = &tab_[(size_t)b * tw_];  // alignment 0
+        for (int i = 0; i < 8; i++) {
+            if (!((q >> i) & 1u)) continue;
+            for (size_t k = 0; k < m_.size(); k++) {
+                d[k] ^= m_[k] << i;
+                if (i) d[k + 1] ^= m_[k] >> (64 - i);
+            }
+        }
+        for (int a = 1; a < 8; a++) {  // the same entry shifted by 8a bits
+            uint64_t *e = &tab_[((size_t)a * 256 + b) * tw_];
+            const int sh = 8 * a;
+            for (int k = 0; k < tw_; k++) {
+                e[k] = d[k] << sh;
+                if (k) e[k] |= d[k - 1] >> (64 - sh);
+            }
+        }
+    }
+}
+
+void Modulus::reduce(Poly &p) const {
+    const int D = gf2::degree(p);
+    if (D >= dm_) {
+        for (int t = (D - dm_) / 8; t >= 0; t--) {
+            const int j = dm_ + 8 * t;  // window of coefficients j .. j+7
+            const size_t w = (size_t)j >> 6;
+            const int o = j & 63;
+            uint64_t v = p[w] >> o;
+            if (o > 56 && w + 1 < p.size()) v |= p[w + 1] << (64 - o);
+            const unsigned b = (unsigned)v & 255u;
+            if (!b) continue;
+            const int s = 8 * t;  // the entry lands at coefficient s
+            const uint64_t *x = &tab_[((size_t)((s & 63) >> 3) * 256 + b) * tw_];
+            const size_t ws = (size_t)s >> 6;
+            const size_t n = std::min(p.size() - ws, (size_t)tw_);
+            uint64_t *d = &p[ws];
+            for (size_t k = 0; k < n; k++) d[k] ^= x[k];
+        }
+    }
+    p.resize((size_t)words(), 0);
+}
+
+Poly Modulus::mulmod(const Poly &a, const Poly &b) const {
+    Poly r = mulComb(a, b);
+    reduce(r);
+    return r;
+}
+
+Poly Modulus::sqrmod(const Poly &a) const {
+    Poly r = spread(a);
+    reduce(r);
+    return r;
+}
+
+Poly Modulus::powx(const std::vector<uint32_t> &e) const {
+    const int W = words();
     Poly r(W, 0);
     r[0] = 1;
     int top = (int)e.size() * 32 - 1;
     while (top >= 0 && !((e[top / 32] >> (top % 32)) & 1u)) top--;
     for (int i = top; i >= 0; i--) {
-        r = sqrmod(r, m, dm);
-        if ((e[i / 32] >> (i % 32)) & 1u) {
-            // r *= X
+        r = sqrmod(r);
+        if ((e[i / 32] >> (i % 32)) & 1u) {  // r *= X
             Poly t(W + 1, 0);
             for (int k = 0; k < W; k++) {
                 t[k] ^= r[k] << 1;
                 t[k + 1] ^= r[k] >> 63;
             }
-            reduce(t, m, dm);
-            r = t;
+            reduce(t);
+            r.swap(t);
         }
     }
-    r.resize(W);
     return r;
+}
+
+Poly powxmod(const std::vector<uint32_t> &e, const Poly &m, int dm) {
+    return Modulus(m, dm).powx(e);
 }
 
 // Berlekamp-Massey over GF(2) with word-parallel discrepancy: the last L bits

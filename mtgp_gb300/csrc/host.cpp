@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -278,6 +279,10 @@ struct Pool {
     size_t desc_cap = 0;
     std::vector<gf2::Poly> chi;   // characteristic polynomial per parameter set
     std::vector<int> chideg;
+    // Jump arithmetic per parameter set, made on first use: chi's modulus
+    // tables and X^(2^i) mod chi for i < 64.
+    std::vector<std::unique_ptr<gf2::Modulus>> mod;
+    std::vector<std::vector<gf2::Poly>> pow2;
     // X^steps mod chi in word form, keyed by (parameter set, steps); bounded
     std::map<std::pair<int, uint64_t>, std::vector<uint32_t>> jcache;
     int resident = 0, resident_split = 0;
@@ -472,16 +477,43 @@ struct Pool {
 
     int polyWords() const { return sh.mexp / 32 + 1; }
 
-    // X^steps mod chi_k as polyWords() words (host, cached).
+    int modulus(int k, const gf2::Modulus **out) {
+        int rc = characteristic(k);
+        if (rc) return rc;
+        if (mod.size() < hparams.size()) mod.resize(hparams.size());
+        if (!mod[k]) mod[k].reset(new (std::nothrow) gf2::Modulus(chi[k], chideg[k]));
+        if (!mod[k]) return setErr(MTGP_ERR_ALLOC, "jump tables");
+        *out = mod[k].get();
+        return MTGP_OK;
+    }
+
+    // X^steps mod chi_k as polyWords() words (host, cached): the product of
+    // the cached X^(2^i) over the set bits of steps.
     int jumpPoly(int k, uint64_t steps, const std::vector<uint32_t> **out) {
         auto hit = jcache.find({k, steps});
         if (hit == jcache.end()) {
-            int rc = characteristic(k);
+            const gf2::Modulus *M = nullptr;
+            int rc = modulus(k, &M);
             if (rc) return rc;
+            if (pow2.size() < hparams.size()) pow2.resize(hparams.size());
+            std::vector<gf2::Poly> &P2 = pow2[k];
+            if (P2.empty()) {
+                gf2::Poly x((size_t)M->words(), 0);
+                x[0] = 2;  // X (the degree is far above 1)
+                P2.push_back(x);
+                for (int i = 1; i < 64; i++) P2.push_back(M->sqrmod(P2.back()));
+            }
+            gf2::Poly r;
+            for (int i = 0; i < 64; i++) {
+                if (!((steps >> i) & 1u)) continue;
+                r = r.empty() ? P2[i] : M->mulmod(r, P2[i]);
+            }
+            if (r.empty()) {
+                r.assign((size_t)M->words(), 0);
+                r[0] = 1;
+            }
             if (jcache.size() >= 16384) jcache.clear();
-            std::vector<uint32_t> e = {(uint32_t)steps, (uint32_t)(steps >> 32)};
-            gf2::Poly p = gf2::powxmod(e, chi[k], chideg[k]);
-            hit = jcache.emplace(std::make_pair(k, steps), gf2::toWords32(p, polyWords())).first;
+            hit = jcache.emplace(std::make_pair(k, steps), gf2::toWords32(r, polyWords())).first;
         }
         *out = &hit->second;
         return MTGP_OK;
@@ -495,7 +527,10 @@ struct Pool {
         if (rc) return rc;
         std::vector<uint32_t> e = {(uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi,
                                    (uint32_t)(hi >> 32)};
-        gf2::Poly p = gf2::powxmod(e, chi[k], chideg[k]);
+        const gf2::Modulus *M = nullptr;
+        rc = modulus(k, &M);
+        if (rc) return rc;
+        gf2::Poly p = M->powx(e);
         int nw = chideg[k] / 32 + 1;
         std::vector<uint32_t> w = gf2::toWords32(p, nw);
         return jumpArray(i, w.data(), nw, s);
@@ -717,13 +752,27 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     struct Tk {
         BatchTask t;
         std::vector<BatchItem> items;
-        uint64_t total, start;
-        int poly;  // index into the plan's jump polynomials, or -1
+        uint64_t total;
+        uint64_t run, off;  // start = run start + offset in the run
     };
     std::vector<Tk> order;
     std::vector<int32_t> stage_streams;
-    std::map<std::pair<int, uint64_t>, int> poly_at;  // (parameter set, start) -> index
-    std::vector<const std::vector<uint32_t> *> polys;
+    // the plan's jump polynomials: X^steps mod chi for (parameter set, steps)
+    const size_t pw = (size_t)P.polyWords();
+    std::map<std::pair<int, uint64_t>, int> poly_at;
+    std::vector<uint32_t> polys;
+    auto polyIndex = [&](int pidx, uint64_t steps, int32_t *idx) -> int {
+        auto hit = poly_at.find({pidx, steps});
+        if (hit == poly_at.end()) {
+            const std::vector<uint32_t> *w = nullptr;
+            int rc = P.jumpPoly(pidx, steps, &w);
+            if (rc) return rc;
+            hit = poly_at.emplace(std::make_pair(pidx, steps), (int)(polys.size() / pw)).first;
+            polys.insert(polys.end(), w->begin(), w->end());
+        }
+        *idx = hit->second;
+        return MTGP_OK;
+    };
     bool cut = false;
     for (size_t r0 = 0, r1; r0 < runs.size(); r0 = r1) {
         for (r1 = r0; r1 < runs.size() && runs[r1].s == runs[r0].s; r1++) {
@@ -743,9 +792,9 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
                 Tk tk{};
                 tk.t.stream = s;
                 tk.t.pidx = P.hpidx[s];
-                tk.t.jpoly = nullptr;
-                tk.start = R.start + c * (uint64_t)chunk;
-                tk.poly = -1;
+                tk.t.j0 = tk.t.j1 = -1;
+                tk.run = R.start;
+                tk.off = c * (uint64_t)chunk;
                 uint64_t want = (c + 1 == k) ? ~uint64_t(0) : (uint64_t)chunk;
                 while (ii < R.items.size() && (want || R.items[ii].count == used)) {
                     BatchItem bi = R.items[ii];
@@ -769,16 +818,17 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             Tk &tk = order[q];
             tk.t.wb = m == 1 ? kWbStream
                              : (q + 1 == order.size() ? (int32_t)stage_streams.size() : kWbNone);
-            if (!tk.start) continue;
-            auto hit = poly_at.find({tk.t.pidx, tk.start});
-            if (hit == poly_at.end()) {
-                const std::vector<uint32_t> *w = nullptr;
-                int rc = P.jumpPoly(tk.t.pidx, tk.start, &w);
-                if (rc) return rc;
-                hit = poly_at.emplace(std::make_pair(tk.t.pidx, tk.start), (int)polys.size()).first;
-                polys.push_back(w);
+            // X^run then X^off: the run starts (a requested skip) and the
+            // chunk offsets (shared by every long request) are each few,
+            // so few distinct polynomials are needed
+            int rc = MTGP_OK;
+            if (tk.run && tk.off) {
+                rc = polyIndex(tk.t.pidx, tk.run, &tk.t.j0);
+                if (!rc) rc = polyIndex(tk.t.pidx, tk.off, &tk.t.j1);
+            } else if (tk.run || tk.off) {
+                rc = polyIndex(tk.t.pidx, tk.run | tk.off, &tk.t.j0);
             }
-            tk.poly = hit->second;
+            if (rc) return rc;
         }
         if (m > 1) stage_streams.push_back(s);
     }
@@ -786,7 +836,6 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     std::stable_sort(order.begin(), order.end(),
                      [](const Tk &a, const Tk &b) { return a.total > b.total; });
     std::vector<BatchTask> tasks;
-    std::vector<int> task_poly;
     std::vector<BatchItem> bitems;
     int mode = -3;  // the output kind shared by all items, -2 if mixed
     for (Tk &tk : order) {
@@ -797,10 +846,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (bi.count) mode = (mode == -3 || mode == bi.kind) ? bi.kind : -2;
         }
         tasks.push_back(tk.t);
-        task_poly.push_back(tk.poly);
     }
     const bool split = !polys.empty();  // the kernel variant with the jump code
-    const size_t pw = (size_t)P.polyWords();
     // reuse the caller's plan (replan) when given: its device buffers are
     // kept and only grown, so a server can refill plans without freeing
     // device memory (cudaFree would wait for every batch in flight)
@@ -861,15 +908,10 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
                  sizeof(BatchItem) * bitems.size());
     if (e == cudaSuccess && !polys.empty()) {
         e = grow(reinterpret_cast<void **>(&pl->d_polys), &pl->cap_polys,
-                 sizeof(uint32_t) * pw * polys.size());
-        std::vector<uint32_t> flat(pw * polys.size());
-        for (size_t k = 0; k < polys.size(); k++)
-            std::copy(polys[k]->begin(), polys[k]->end(), flat.begin() + k * pw);
+                 sizeof(uint32_t) * polys.size());
         if (e == cudaSuccess)
-            e = cudaMemcpy(pl->d_polys, flat.data(), sizeof(uint32_t) * flat.size(),
+            e = cudaMemcpy(pl->d_polys, polys.data(), sizeof(uint32_t) * polys.size(),
                            cudaMemcpyHostToDevice);
-        for (size_t q = 0; q < tasks.size(); q++)
-            if (task_poly[q] >= 0) tasks[q].jpoly = pl->d_polys + (size_t)task_poly[q] * pw;
     }
     if (e == cudaSuccess && !tasks.empty())
         e = cudaMemcpy(pl->d_tasks, tasks.data(), sizeof(BatchTask) * tasks.size(), cudaMemcpyHostToDevice);
@@ -893,6 +935,7 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     b.mode = pl->mode;
     b.grid = pl->grid;
     b.nwords = P.polyWords();
+    b.polys = pl->d_polys;
     b.split = pl->split;
     b.core = pl->core;
     b.tasks = pl->d_tasks;

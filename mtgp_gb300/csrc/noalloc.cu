@@ -135,7 +135,7 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
         t.nitems = cnt[st];
         t.pidx = param_idx ? param_idx[st] : (nparams == nstreams ? st : 0);
         if (t.pidx < 0 || t.pidx >= nparams) return fail(MTGP_ERR_INVALID, "param_idx out of range");
-        t.jpoly = nullptr;
+        t.j0 = t.j1 = -1;
         t.wb = kWbStream;
         tasks.push_back(t);
     }
@@ -163,6 +163,7 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
     b.core = genCore32();
     b.split = false;
     b.nwords = 0;
+    b.polys = nullptr;
     b.tasks = reinterpret_cast<const BatchTask *>(base + NaLayout::tasks);
     b.ntasks = (int)tasks.size();
     b.items = reinterpret_cast<const BatchItem *>(base + NaLayout::items);

@@ -1,0 +1,78 @@
+"""The library's host GF(2)[x] arithmetic (table reduction, comb products,
+X^e by squaring and by products of X^(2^i)) equals the oracle's bit-serial
+PowerXMod / MulMod on the characteristic polynomials of the shipped
+parameter sets (CPU only)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from mtgp_gb300.params import load_table
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+@pytest.fixture(scope="module")
+def probe(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("gf2") / "gf2_probe.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", so,
+                    os.path.join(HERE, "gf2_probe.cpp"),
+                    os.path.join(ROOT, "mtgp_gb300", "csrc", "gf2.cpp")], check=True)
+    L = ctypes.CDLL(so)
+    vp = ctypes.c_void_p
+    L.probe_powx.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp]
+    L.probe_mulmod.argtypes = [vp, vp, vp, ctypes.c_int, vp]
+    L.probe_pow2_product.argtypes = [vp, ctypes.c_int, ctypes.c_uint64, vp]
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _chi(orc, table):
+    p = load_table(table)[0]
+    seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
+    d, chi = orc.minpoly((seq & 1).astype(np.uint8))
+    assert d == p.mexp
+    m = np.zeros(d // 64 + 1, dtype=np.uint64)
+    m[:min(len(chi), len(m))] = chi[:len(m)]
+    return d, m
+
+
+TABLES = ["mtgp32_fast_11213", "mtgp64dc_fast_11213", "mtgp32_fast_23209"]
+EXPS = [1, 2, 63, 64, 65, 1 << 17, (1 << 40) + 12345, 3 ** 40, (1 << 64) - 1, 3 ** 80]
+
+
+@pytest.mark.parametrize("table", TABLES)
+def test_powx_matches_oracle(orc, probe, table):
+    d, m = _chi(orc, table)
+    for e in EXPS:
+        ew = max(1, (e.bit_length() + 31) // 32)
+        ea = np.array([(e >> (32 * k)) & 0xffffffff for k in range(ew)], dtype=np.uint32)
+        out = np.zeros((d + 63) // 64, dtype=np.uint64)
+        probe.probe_powx(_p(m), d, _p(ea), ew, _p(out))
+        assert np.array_equal(out, orc.powxmod(e, m, d)), e
+        if e < (1 << 64):
+            out2 = np.zeros_like(out)
+            probe.probe_pow2_product(_p(m), d, e, _p(out2))
+            assert np.array_equal(out2, out), e
+
+
+@pytest.mark.parametrize("table", TABLES[:2])
+def test_mulmod_matches_oracle(orc, probe, table):
+    d, m = _chi(orc, table)
+    rng = np.random.default_rng(9)
+    w = (d + 63) // 64
+    top = np.uint64((1 << (d % 64)) - 1)
+    for _ in range(4):
+        a = rng.integers(0, 2 ** 63, w, dtype=np.uint64) * np.uint64(2) + np.uint64(1)
+        b = rng.integers(0, 2 ** 63, w, dtype=np.uint64) * np.uint64(3)
+        a[-1] &= top
+        b[-1] &= top
+        out = np.zeros(w, dtype=np.uint64)
+        probe.probe_mulmod(_p(a), _p(b), _p(m), d, _p(out))
+        assert np.array_equal(out, orc.mulmod(a, b, m, d))
