@@ -18,6 +18,9 @@ Reported (one JSON line on rank 0):
   bank      128-set bank (2^21 uint32 per set, one CTA per set) GB/s
   roofline  batched kernel vs the measured HBM copy bandwidth
   cpu_baseline  the CPU oracle (OpenMP over substreams) on a sample
+  serve     continuous-batching server over resident streams: saturation
+            rate, then p50 / p99 latency and GB/s at 0.3 / 0.6 / 0.9 of it;
+            a check trace whose every response is compared with the oracle
 
     python bench.py [--steps K] [--warmup W] [--impl reference]
 """
@@ -41,6 +44,24 @@ L2_BYTES = 129 * 2 ** 20
 METRIC = "batched MTGP32-11213 output GB/s"
 WORKLOAD = ("batched: mtgp32_params_fast_11213[0], seed 1234, 4096 substreams j*3^162 "
             "(GPU jump), lognormal lengths median 2^16 sigma 1.0 seed 42 clip [2^10,2^22], uint32")
+
+
+SERVE_WORKLOAD = ("serving: 4096 MTGP32-11213 substreams (set 0) + 256 MTGP64-11213 substreams "
+                  "(mtgp64dc set 0), j*3^162 apart, seed 1234; Poisson arrivals; stream uniform; "
+                  "count lognormal median 2^16 sigma 1.0 clip [1,2^26]; types uint32 / float32 "
+                  "[0,1) / uint64 60/30/10; 10% of requests at an offset 2^k, k uniform in "
+                  "17..40 (GF(2) jump on the GPU); 8 GB device budget for in-flight output")
+
+
+def serve_trace(rng, n):
+    """n requests of the serving workload: (pool, stream, kind, count, skip)."""
+    u = rng.random(n)
+    pool = (u >= 0.9).astype(np.int32)
+    kind = np.where((u >= 0.6) & (u < 0.9), 2, 0).astype(np.int32)
+    stream = np.where(pool == 0, rng.integers(0, 4096, n), rng.integers(0, 256, n))
+    count = np.clip(np.rint(rng.lognormal(np.log(2.0 ** 16), 1.0, n)), 1, 2 ** 26)
+    skip = np.where(rng.random(n) < 0.1, np.left_shift(1, rng.integers(17, 41, n)), 0)
+    return pool, stream.astype(np.uint32), kind, count.astype(np.uint64), skip.astype(np.uint64)
 
 
 def lengths(n=N_SUB, seed=42):
@@ -186,6 +207,108 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_serving(args, s, local):
+    """Serving section: a check trace whose responses are kept for the
+    oracle, a burst that finds the saturation rate, then Poisson traces at
+    0.3 / 0.6 / 0.9 of it with p50 / p99 latency (submission to the result
+    resident in device memory)."""
+    import torch
+    from mtgp_gb300.api import Pool, Server, requests
+    from mtgp_gb300.params import jump_table, load_table
+    p32 = load_table("mtgp32_fast_11213")[0]
+    p64 = load_table("mtgp64dc_fast_11213")[0]
+    a = Pool.substreams(p32, SEED, 4096, jump_table(32), stream=s)
+    b = Pool.substreams(p64, SEED, 256, jump_table(64), stream=s)
+    s.synchronize()
+    win_a, win_b = a.windows(), b.windows()
+    srv = Server(a, b, budget_bytes=8 << 30, slots=4, max_batch=2048)
+    # check trace: every response kept for the bit-exact check on the CPU
+    rng = np.random.default_rng(7)
+    pool, stream, kind, count, skip = serve_trace(rng, 256)
+    count = np.minimum(count, 1 << 18)
+    outs = []
+    for k in range(256):
+        dst = torch.empty(int(count[k]), dtype=torch.int32 if pool[k] == 0 else torch.int64,
+                          device="cuda")
+        outs.append(dst)
+        srv.submit(int(pool[k]), int(stream[k]), int(kind[k]), int(count[k]), dst,
+                   skip=int(skip[k]))
+    srv.drain()
+    check = (pool, stream, kind, count, skip, [o.cpu().numpy() for o in outs], win_a, win_b)
+    del outs
+
+    def run(tr, arrivals):
+        c0, b0, k0 = srv.stats()
+        wall = srv.replay(requests(*tr), arrivals)
+        c1, b1, k1 = srv.stats()
+        lat, st = srv.results()
+        assert (st[c0:c1] == 0).all(), "failed requests"
+        return wall, b1 - b0, k1 - k0, lat[c0:c1]
+
+    rng = np.random.default_rng(11)
+    # warm-up: plan buffers, kernels, the jump polynomials of the offsets and
+    # of the chunk multiples
+    for n in (2000, args.serve_burst):
+        run(serve_trace(rng, n), np.zeros(n))
+    run(serve_trace(rng, 20000), np.cumsum(rng.exponential(1e-6, 20000)))
+    out = {"workload": SERVE_WORKLOAD, "slots": 4, "max_batch": 2048,
+           "latency": "submission to the result resident in device memory"}
+    with Clocks(local) as clk:
+        n = args.serve_burst
+        wall, nbytes, batches, lat = run(serve_trace(rng, n), np.zeros(n))
+        sat = n / wall
+        out["saturation"] = {"requests": n, "req_per_s": round(sat, 1),
+                             "GB_per_s": round(nbytes / wall / 1e9, 2), "batches": batches}
+        rates = []
+        for load in (0.3, 0.6, 0.9):
+            rate = load * sat
+            n = max(200, int(rate * args.serve_seconds))
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+            wall, nbytes, batches, lat = run(serve_trace(rng, n), arrivals)
+            rates.append({"load": load, "offered_req_per_s": round(rate, 1), "requests": n,
+                          "req_per_s": round(n / wall, 1),
+                          "GB_per_s": round(nbytes / wall / 1e9, 2),
+                          "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
+                          "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
+                          "batches": batches})
+        out["rates"] = rates
+    out["clocks"] = clk.summary()
+    out["scheduler_s"] = {k: round(v, 3) for k, v in srv.profile().items()}
+    srv.close()
+    return out, check
+
+
+def serve_check(orc, chk):
+    """Every response of the check trace against the oracle: each stream
+    replayed in submission order from the windows the pools started from
+    (offsets of 2^17 or more by X^offset mod chi, as the server does)."""
+    from mtgp_gb300.params import load_table
+    pool, stream, kind, count, skip, outs, win_a, win_b = chk
+    par = {0: load_table("mtgp32_fast_11213")[0], 1: load_table("mtgp64dc_fast_11213")[0]}
+    chis = {}
+    for q, p in par.items():
+        seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
+        chis[q] = orc.minpoly((seq & 1).astype(np.uint8))
+    gens, bad = {}, 0
+    for k in range(len(pool)):
+        q, j = int(pool[k]), int(stream[k])
+        if (q, j) not in gens:
+            o = orc.gen(par[q], seed=1)
+            o.set_window((win_a if q == 0 else win_b)[j])
+            gens[(q, j)] = o
+        o = gens[(q, j)]
+        if int(skip[k]) >= (1 << 17):
+            d, chi = chis[q]
+            o.jump_words(orc.powxmod(int(skip[k]), chi, d).view(np.uint32)[:351])
+        else:
+            o.skip(int(skip[k]))
+        ref = np.ascontiguousarray(o.fill(int(kind[k]), int(count[k])))
+        dt = np.uint32 if q == 0 else np.uint64
+        bad += not np.array_equal(outs[k].view(dt), ref.view(dt))
+    return {"requests": len(pool), "mismatches": int(bad), "bit_exact": bad == 0,
+            "jumped": int((skip >= (1 << 17)).sum())}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -197,8 +320,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--substreams", type=int, default=N_SUB,
                     help="substreams of the batched workload (profiling runs use fewer)")
-    ap.add_argument("--only", default="all", choices=["all", "batched", "bank"],
+    ap.add_argument("--only", default="all", choices=["all", "batched", "bank", "serve"],
                     help="profiling runs: time only one path, no e2e / plain / CPU legs")
+    ap.add_argument("--serve-seconds", type=float, default=3.0,
+                    help="length of each Poisson trace of the serving section")
+    ap.add_argument("--serve-burst", type=int, default=20000,
+                    help="requests of the burst that finds the saturation rate")
+    ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--uniform", type=int, default=0,
                     help="profiling runs: every substream requests this many values "
                          "(steady-state throughput instead of the lognormal workload)")
@@ -262,7 +390,7 @@ def main():
     plan.launch(out, s)
     s.synchronize()
     first_step = out[:int(lens[:256].sum())].cpu().numpy().view(np.uint32).copy()
-    if args.only == "bank":
+    if args.only in ("bank", "serve"):
         args.steps = 0
 
     # --- batched, device-resident, CUDA graph ---
@@ -317,7 +445,7 @@ def main():
         plain_ms = ev0.elapsed_time(ev1) / args.plain_steps
 
     # --- bank: 128 parameter sets, 2^21 uint32 each, one CTA per set ---
-    bank_reps = 0 if args.only == "batched" else 5
+    bank_reps = 0 if args.only in ("batched", "serve") else 5
     tbl = load_table("mtgp32_fast_11213")
     bank = Pool.create([tbl[i] for i in range(128)], np.arange(128) + 1234)
     nb = 1 << 21
@@ -333,12 +461,19 @@ def main():
     bank_ms = max(ev0.elapsed_time(ev1) / max(bank_reps, 1), 1e-6)
     bank_gbs = 128 * nb * 4 / (bank_ms * 1e-3) / 1e9
 
+    # --- serving: continuous batching over resident streams ---
+    serve, serve_chk = None, None
+    if rank == 0 and not args.no_serve and args.only in ("all", "serve"):
+        serve, serve_chk = run_serving(args, s, local)
+
     hbm, peak_kind = peaks()
     state_bytes = 2 * nsub * 351 * 4
     achieved = (total_bytes + state_bytes) / (ms * 1e-3) / 1e9
+    chosen = [l for l in tune_report.splitlines() if l.startswith("chosen:")]
+    kernel = chosen[0][len("chosen:"):].split(", chunk=")[0].strip() if chosen else None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
-                "traffic": None, "kernel": "k_batch32<351,256,1024>"}
+                "traffic": None, "kernel": kernel}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -352,6 +487,8 @@ def main():
                "sample": "first 256 substreams of the workload (%d uint32), %d repetitions"
                          % (words, reps),
                "gpu_first_step_bit_exact": ok}
+        if serve_chk is not None:
+            serve["check"] = serve_check(orc, serve_chk)
 
     if rank == 0:
         line = {
@@ -374,7 +511,8 @@ def main():
             "plan": {"tasks": plan_tasks, "split_chunk": plan_chunk,
                      "autotune_ms": round(plan_ms, 1),
                      "autotune": [l for l in tune_report.strip().splitlines()]},
-            "e2e": {"value": round(e2e, 3), "unit": "GB/s", "h2d_bytes_per_step": 24 * nsub,
+            "serve": serve,
+            "e2e": {"value": round(e2e, 3), "unit": "GB/s", "h2d_bytes_per_step": 32 * nsub,
                     "d2h_bytes_per_step": total_bytes},
             "roofline": roofline,
             "cpu_baseline": cpu,

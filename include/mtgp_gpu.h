@@ -415,16 +415,26 @@ typedef struct mtgp_request {
     uint64_t count;   /* values produced                                   */
     void *dst;        /* device or host destination, or NULL = discard     */
 } mtgp_request_t;
+/* (In a replayed trace a request without destination is discarded when it
+ * completes; mtgp_server_submit keeps such results instead.) */
 
 /* Either pool may be NULL (not both).  The pools must outlive the server. */
 int mtgp_server_create(mtgp_server_t **out, mtgp32_gpu_pool_t *p32,
                        mtgp64_gpu_pool_t *p64, uint64_t budget_bytes,
                        int slots, int max_batch);
 /* Queue a request (thread-safe).  Tickets count from 1.  A request whose
- * output alone exceeds the budget is rejected with MTGP_ERR_BUDGET. */
+ * output alone exceeds the budget is rejected with MTGP_ERR_BUDGET.  With
+ * dst == NULL the result stays in the server's device arena (zero copy):
+ * mtgp_server_result gives its address once the request is done, and
+ * mtgp_server_release returns the space to the budget. */
 int mtgp_server_submit(mtgp_server_t *s, int pool, uint32_t stream, int kind,
                        uint64_t skip, uint64_t count, void *dst,
                        uint64_t *ticket);
+/* Device address and size of a finished request's result kept in the arena
+ * (valid until mtgp_server_release or mtgp_server_destroy). */
+int mtgp_server_result(mtgp_server_t *s, uint64_t ticket, void **dev_ptr,
+                       uint64_t *bytes);
+int mtgp_server_release(mtgp_server_t *s, uint64_t ticket);
 /* Remove a request that has not been admitted yet; its status becomes
  * MTGP_ERR_BUSY.  Fails with MTGP_ERR_INVALID once it is admitted. */
 int mtgp_server_cancel(mtgp_server_t *s, uint64_t ticket);
@@ -440,6 +450,10 @@ int mtgp_server_results(mtgp_server_t *s, double *latency, int *status,
                         uint64_t cap, uint64_t *n);
 int mtgp_server_stats(mtgp_server_t *s, uint64_t *completed, uint64_t *bytes,
                       uint64_t *batches);
+/* Time the scheduler thread spent so far, in seconds: [0] admitting
+ * requests, [1] planning and launching batches, [2] retiring batches,
+ * [3] waiting for work (the first n of these four). */
+int mtgp_server_profile(mtgp_server_t *s, double *seconds, int n);
 /* Submit n requests at their arrival times (seconds after the call starts),
  * then drain; wall_s receives the elapsed time. */
 int mtgp_server_replay(mtgp_server_t *s, const mtgp_request_t *reqs,

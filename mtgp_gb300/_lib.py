@@ -53,10 +53,13 @@ SIGS = {
     "mtgp_server_create": (c_int, [pp, vp, vp, c_u64, c_int, c_int]),
     "mtgp_server_submit": (c_int, [vp, c_int, c_u32, c_int, c_u64, c_u64, vp, vp]),
     "mtgp_server_cancel": (c_int, [vp, c_u64]),
+    "mtgp_server_result": (c_int, [vp, c_u64, vp, vp]),
+    "mtgp_server_release": (c_int, [vp, c_u64]),
     "mtgp_server_wait": (c_int, [vp, c_u64, ctypes.c_double, vp]),
     "mtgp_server_drain": (c_int, [vp, ctypes.c_double]),
     "mtgp_server_results": (c_int, [vp, vp, vp, c_u64, vp]),
     "mtgp_server_stats": (c_int, [vp, vp, vp, vp]),
+    "mtgp_server_profile": (c_int, [vp, vp, c_int]),
     "mtgp_server_replay": (c_int, [vp, vp, vp, c_int, vp]),
     "mtgp_server_destroy": (None, [vp]),
 }

@@ -294,12 +294,29 @@ class Pool:
                                                             w.size))
 
 
+# mtgp_request_t as a numpy record (traces of many requests are built with
+# numpy and handed to the library without per-request Python work)
+REQUEST_DTYPE = np.dtype([("pool", "<i4"), ("stream", "<u4"), ("kind", "<i4"), ("pad_", "<i4"),
+                          ("skip", "<u8"), ("count", "<u8"), ("dst", "<u8")])
+assert REQUEST_DTYPE.itemsize == 40
+
+
+def requests(pools, streams, kinds, counts, skips=None):
+    """A trace of requests (no destinations) as a REQUEST_DTYPE array."""
+    r = np.zeros(len(streams), dtype=REQUEST_DTYPE)
+    r["pool"], r["stream"], r["kind"], r["count"] = pools, streams, kinds, counts
+    if skips is not None:
+        r["skip"] = skips
+    return r
+
+
 class Server:
     """Continuous-batching request loop over resident pools (mtgp_server_t).
 
     `submit` queues a request and returns its ticket; the values land in
-    `dst` (a CUDA or CPU tensor of the pool's word size, or None to discard)
-    once `wait(ticket)` returns."""
+    `dst` (a CUDA or CPU tensor of the pool's word size) once `wait(ticket)`
+    returns.  Without `dst` the result stays in the server's device arena:
+    `result(ticket)` is a zero-copy view of it until `release(ticket)`."""
 
     def __init__(self, pool32=None, pool64=None, budget_bytes=1 << 30, slots=4, max_batch=4096):
         self.pools = (pool32, pool64)  # keep the pools alive
@@ -329,6 +346,24 @@ class Server:
     def cancel(self, ticket):
         check(lib().mtgp_server_cancel(self.h, ticket))
 
+    def result(self, ticket, dtype=torch.int32):
+        """Zero-copy view (CUDA tensor) of a finished request submitted
+        without destination; valid until release(ticket)."""
+        ptr, nbytes = ctypes.c_void_p(), ctypes.c_uint64()
+        check(lib().mtgp_server_result(self.h, ticket, ctypes.byref(ptr), ctypes.byref(nbytes)))
+        esz = torch.tensor([], dtype=dtype).element_size()
+        typestr = {torch.int32: "<i4", torch.float32: "<f4", torch.int64: "<i8",
+                   torch.float64: "<f8"}[dtype]
+
+        class _View:
+            __cuda_array_interface__ = {"shape": (nbytes.value // esz,), "typestr": typestr,
+                                        "data": (ptr.value or 0, False), "version": 3,
+                                        "strides": None}
+        return torch.as_tensor(_View(), device="cuda")
+
+    def release(self, ticket):
+        check(lib().mtgp_server_release(self.h, ticket))
+
     def drain(self, timeout=600.0):
         check(lib().mtgp_server_drain(self.h, timeout))
         self._keep.clear()
@@ -350,13 +385,23 @@ class Server:
         check(lib().mtgp_server_stats(self.h, ctypes.byref(c), ctypes.byref(b), ctypes.byref(k)))
         return c.value, b.value, k.value
 
+    def profile(self):
+        """Scheduler seconds: admitting, planning + launching, retiring, idle."""
+        out = np.zeros(4, dtype=np.float64)
+        check(lib().mtgp_server_profile(self.h, out.ctypes.data_as(ctypes.c_void_p), 4))
+        return {"admit_s": out[0], "launch_s": out[1], "retire_s": out[2], "idle_s": out[3]}
+
     def replay(self, requests, arrivals):
-        """Submit `requests` (an array of Request) at `arrivals` (seconds
-        from now) and drain; returns the wall time in seconds."""
+        """Submit `requests` (a REQUEST_DTYPE array) at `arrivals` (seconds
+        from now) and drain; returns the wall time in seconds.  Results of
+        requests without destination are discarded at completion."""
+        req = np.ascontiguousarray(requests, dtype=REQUEST_DTYPE)
         arr = np.ascontiguousarray(arrivals, dtype=np.float64)
+        assert len(req) == len(arr)
         wall = ctypes.c_double()
-        check(lib().mtgp_server_replay(self.h, requests, arr.ctypes.data_as(ctypes.c_void_p),
-                                       len(arr), ctypes.byref(wall)))
+        check(lib().mtgp_server_replay(self.h, req.ctypes.data_as(ctypes.c_void_p),
+                                       arr.ctypes.data_as(ctypes.c_void_p), len(arr),
+                                       ctypes.byref(wall)))
         return wall.value
 
     def close(self):

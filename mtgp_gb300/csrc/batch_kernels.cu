@@ -20,6 +20,9 @@
 //
 // Plans without split requests use the four-words-per-thread core
 // (mtgp_device4.cuh) for 32-bit streams.
+#include <mutex>
+#include <vector>
+
 #include "batch.h"
 #include "jump_device.cuh"
 #include "mtgp_device4.cuh"
@@ -225,14 +228,35 @@ __global__ void k_unstage(W *__restrict__ states, const W *__restrict__ stage,
     for (int k = threadIdx.x; k < N; k += blockDim.x) dst[k] = src[k];
 }
 
+// Resident CTAs of a kernel on the current device (cached per kernel and
+// device: the occupancy query is not free and servers launch often).
 template <class K>
 static cudaError_t resident(K kern, int tn, int *grid) {
+    struct Entry {
+        const void *fn;
+        int dev, tn, grid;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
     int dev = 0, sms = 0, per = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const void *fn = reinterpret_cast<const void *>(kern);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (const Entry &c : cache)
+            if (c.fn == fn && c.dev == dev && c.tn == tn) {
+                *grid = c.grid;
+                return cudaSuccess;
+            }
+    }
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, tn, 0);
-    if (e == cudaSuccess) *grid = sms * (per > 0 ? per : 1);
-    return e;
+    if (e != cudaSuccess) return e;
+    *grid = sms * (per > 0 ? per : 1);
+    std::lock_guard<std::mutex> lk(mu);
+    cache.push_back({fn, dev, tn, *grid});
+    return cudaSuccess;
 }
 
 // work counter reset -> persistent kernel

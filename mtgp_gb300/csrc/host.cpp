@@ -283,8 +283,8 @@ struct Pool {
     // tables and X^(2^i) mod chi for i < 64.
     std::vector<std::unique_ptr<gf2::Modulus>> mod;
     std::vector<std::vector<gf2::Poly>> pow2;
-    // X^steps mod chi in word form, keyed by (parameter set, steps); bounded
-    std::map<std::pair<int, uint64_t>, std::vector<uint32_t>> jcache;
+    // X^steps mod chi, keyed by (parameter set, steps); bounded
+    std::map<std::pair<int, uint64_t>, gf2::Poly> jcache;
     int resident = 0, resident_split = 0;
 
     ~Pool() {
@@ -487,35 +487,45 @@ struct Pool {
         return MTGP_OK;
     }
 
-    // X^steps mod chi_k as polyWords() words (host, cached): the product of
-    // the cached X^(2^i) over the set bits of steps.
-    int jumpPoly(int k, uint64_t steps, const std::vector<uint32_t> **out) {
+    // X^steps mod chi_k (host, cached): X^(steps - low) * X^low with low the
+    // lowest set bit, X^(2^i) cached per parameter set, so that a sequence of
+    // multiples of one chunk length costs one product each.
+    int jumpPoly(int k, uint64_t steps, const gf2::Poly **out) {
         auto hit = jcache.find({k, steps});
-        if (hit == jcache.end()) {
-            const gf2::Modulus *M = nullptr;
-            int rc = modulus(k, &M);
-            if (rc) return rc;
-            if (pow2.size() < hparams.size()) pow2.resize(hparams.size());
-            std::vector<gf2::Poly> &P2 = pow2[k];
-            if (P2.empty()) {
-                gf2::Poly x((size_t)M->words(), 0);
-                x[0] = 2;  // X (the degree is far above 1)
-                P2.push_back(x);
-                for (int i = 1; i < 64; i++) P2.push_back(M->sqrmod(P2.back()));
-            }
-            gf2::Poly r;
-            for (int i = 0; i < 64; i++) {
-                if (!((steps >> i) & 1u)) continue;
-                r = r.empty() ? P2[i] : M->mulmod(r, P2[i]);
-            }
-            if (r.empty()) {
-                r.assign((size_t)M->words(), 0);
-                r[0] = 1;
-            }
-            if (jcache.size() >= 16384) jcache.clear();
-            hit = jcache.emplace(std::make_pair(k, steps), gf2::toWords32(r, polyWords())).first;
+        if (hit != jcache.end()) {
+            *out = &hit->second;
+            return MTGP_OK;
         }
-        *out = &hit->second;
+        const gf2::Modulus *M = nullptr;
+        int rc = modulus(k, &M);
+        if (rc) return rc;
+        if (pow2.size() < hparams.size()) pow2.resize(hparams.size());
+        std::vector<gf2::Poly> &P2 = pow2[k];
+        if (P2.empty()) {
+            gf2::Poly x((size_t)M->words(), 0);
+            x[0] = 2;  // X (the degree is far above 1)
+            P2.push_back(x);
+            for (int i = 1; i < 64; i++) P2.push_back(M->sqrmod(P2.back()));
+        }
+        gf2::Poly r;
+        if (steps == 0) {
+            r.assign((size_t)M->words(), 0);
+            r[0] = 1;
+        } else {
+            const uint64_t low = steps & (~steps + 1);
+            int b = 0;
+            while ((uint64_t(1) << b) != low) b++;
+            if (steps == low) {
+                r = P2[b];
+            } else {
+                const gf2::Poly *rest = nullptr;
+                rc = jumpPoly(k, steps - low, &rest);
+                if (rc) return rc;
+                r = M->mulmod(*rest, P2[b]);
+            }
+        }
+        if (jcache.size() >= 16384) jcache.clear();
+        *out = &jcache.emplace(std::make_pair(k, steps), std::move(r)).first->second;
         return MTGP_OK;
     }
 
@@ -609,33 +619,37 @@ struct mtgp64_gpu_pool { Pool<T64> pool; };
 struct mtgp_gpu_plan {
     int bits = 32;
     void *pool = nullptr;  // Pool<T32> or Pool<T64>
-    BatchTask *d_tasks = nullptr;
-    BatchItem *d_items = nullptr;
-    unsigned *d_counter = nullptr;
     int ntasks = 0;
     int mode = -2;         // shared output kind of all items, or -2 (mixed)
     uint64_t out_bytes = 0;
     int grid = 0;
     bool split = false;    // some tasks start with an in-kernel jump
     int core = 4;          // 32-bit generation core of unsplit plans
-    size_t cap_tasks = 0, cap_items = 0, cap_stage = 0;  // device buffer capacities
     int64_t chunk = 0;     // chunk length used when splitting
-    void *d_stage = nullptr;
-    int32_t *d_stage_streams = nullptr;
     int nstage = 0;
-    uint32_t *d_polys = nullptr;  // jump polynomials of the tasks that jump
-    size_t cap_polys = 0;
+    // Descriptors (tasks | items | jump polynomials | staged streams), built
+    // in pinned host memory and uploaded by one asynchronous copy on the
+    // stream of the next launch; both buffers are kept and only grown, so a
+    // server can refill plans without allocating (cudaFree and cudaFreeHost
+    // would wait for every batch in flight).
+    unsigned char *h_blob = nullptr, *d_blob = nullptr;
+    size_t cap_h = 0, cap_d = 0, blob_bytes = 0;
+    bool dirty = false;
+    const BatchTask *d_tasks = nullptr;
+    const BatchItem *d_items = nullptr;
+    const uint32_t *d_polys = nullptr;
+    const int32_t *d_stage_streams = nullptr;
+    unsigned *d_counter = nullptr;
+    void *d_stage = nullptr;  // final windows of streams with several tasks
+    size_t cap_stage = 0;
 
     cudaGraphExec_t exec = nullptr;
     void *graph_out = nullptr;
     ~mtgp_gpu_plan() {
         if (exec) cudaGraphExecDestroy(exec);
-
         cudaFree(d_stage);
-        cudaFree(d_stage_streams);
-        cudaFree(d_polys);
-        cudaFree(d_tasks);
-        cudaFree(d_items);
+        cudaFree(d_blob);
+        cudaFreeHost(h_blob);
         cudaFree(d_counter);
     }
 };
@@ -764,11 +778,12 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     auto polyIndex = [&](int pidx, uint64_t steps, int32_t *idx) -> int {
         auto hit = poly_at.find({pidx, steps});
         if (hit == poly_at.end()) {
-            const std::vector<uint32_t> *w = nullptr;
-            int rc = P.jumpPoly(pidx, steps, &w);
+            const gf2::Poly *p = nullptr;
+            int rc = P.jumpPoly(pidx, steps, &p);
             if (rc) return rc;
             hit = poly_at.emplace(std::make_pair(pidx, steps), (int)(polys.size() / pw)).first;
-            polys.insert(polys.end(), w->begin(), w->end());
+            const std::vector<uint32_t> w = gf2::toWords32(*p, (int)pw);
+            polys.insert(polys.end(), w.begin(), w.end());
         }
         *idx = hit->second;
         return MTGP_OK;
@@ -871,57 +886,63 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->core = genCore32();
     pl->chunk = cut ? chunk : 0;
     pl->nstage = (int)stage_streams.size();
-    auto grow = [](void **p, size_t *cap, size_t need) -> cudaError_t {
-        if (need <= *cap) return cudaSuccess;
-        cudaFree(*p);
-        *p = nullptr;
-        *cap = 0;
-        size_t n = need + need / 4;
-        cudaError_t e = cudaMalloc(p, n);
-        if (e == cudaSuccess) *cap = n;
-        return e;
-    };
+    auto align = [](size_t n) { return (n + 255) & ~size_t(255); };
+    const size_t off_items = align(sizeof(BatchTask) * tasks.size());
+    const size_t off_polys = off_items + align(sizeof(BatchItem) * bitems.size());
+    const size_t off_ss = off_polys + align(sizeof(uint32_t) * polys.size());
+    const size_t bytes = off_ss + sizeof(int32_t) * stage_streams.size();
     cudaError_t e = cudaSuccess;
     if (!pl->d_counter) e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
+    if (e == cudaSuccess && bytes > pl->cap_d) {
+        cudaFree(pl->d_blob);
+        pl->d_blob = nullptr;
+        pl->cap_d = 0;
+        e = cudaMalloc(&pl->d_blob, bytes + bytes / 4);
+        if (e == cudaSuccess) pl->cap_d = bytes + bytes / 4;
+    }
+    if (e == cudaSuccess && bytes > pl->cap_h) {
+        cudaFreeHost(pl->h_blob);
+        pl->h_blob = nullptr;
+        pl->cap_h = 0;
+        e = cudaHostAlloc(&pl->h_blob, bytes + bytes / 4, cudaHostAllocDefault);
+        if (e == cudaSuccess) pl->cap_h = bytes + bytes / 4;
+    }
     if (e == cudaSuccess && pl->nstage) {
-        const size_t need = (sizeof(W) * (size_t)P.stride + sizeof(int32_t)) * pl->nstage;
+        const size_t need = sizeof(W) * (size_t)P.stride * pl->nstage;
         if (need > pl->cap_stage) {
             cudaFree(pl->d_stage);
-            cudaFree(pl->d_stage_streams);
             pl->d_stage = nullptr;
-            pl->d_stage_streams = nullptr;
             pl->cap_stage = 0;
-            const int n = pl->nstage + pl->nstage / 4 + 1;
-            e = cudaMalloc(&pl->d_stage, sizeof(W) * (size_t)P.stride * n);
-            if (e == cudaSuccess) e = cudaMalloc(&pl->d_stage_streams, sizeof(int32_t) * n);
-            if (e == cudaSuccess) pl->cap_stage = (sizeof(W) * (size_t)P.stride + sizeof(int32_t)) * n;
+            e = cudaMalloc(&pl->d_stage, need + need / 4);
+            if (e == cudaSuccess) pl->cap_stage = need + need / 4;
         }
-        if (e == cudaSuccess)
-            e = cudaMemcpy(pl->d_stage_streams, stage_streams.data(),
-                           sizeof(int32_t) * pl->nstage, cudaMemcpyHostToDevice);
     }
-    if (e == cudaSuccess)
-        e = grow(reinterpret_cast<void **>(&pl->d_tasks), &pl->cap_tasks,
-                 sizeof(BatchTask) * tasks.size());
-    if (e == cudaSuccess)
-        e = grow(reinterpret_cast<void **>(&pl->d_items), &pl->cap_items,
-                 sizeof(BatchItem) * bitems.size());
-    if (e == cudaSuccess && !polys.empty()) {
-        e = grow(reinterpret_cast<void **>(&pl->d_polys), &pl->cap_polys,
-                 sizeof(uint32_t) * polys.size());
-        if (e == cudaSuccess)
-            e = cudaMemcpy(pl->d_polys, polys.data(), sizeof(uint32_t) * polys.size(),
-                           cudaMemcpyHostToDevice);
-    }
-    if (e == cudaSuccess && !tasks.empty())
-        e = cudaMemcpy(pl->d_tasks, tasks.data(), sizeof(BatchTask) * tasks.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !bitems.empty())
-        e = cudaMemcpy(pl->d_items, bitems.data(), sizeof(BatchItem) * bitems.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         if (fresh) delete pl;
-        return cudaErr(e, "upload plan");
+        return cudaErr(e, "plan buffers");
     }
+    unsigned char *h = pl->h_blob;
+    if (!tasks.empty()) std::memcpy(h, tasks.data(), sizeof(BatchTask) * tasks.size());
+    if (!bitems.empty()) std::memcpy(h + off_items, bitems.data(), sizeof(BatchItem) * bitems.size());
+    if (!polys.empty()) std::memcpy(h + off_polys, polys.data(), sizeof(uint32_t) * polys.size());
+    if (!stage_streams.empty())
+        std::memcpy(h + off_ss, stage_streams.data(), sizeof(int32_t) * stage_streams.size());
+    pl->blob_bytes = bytes;
+    pl->dirty = bytes > 0;
+    pl->d_tasks = reinterpret_cast<const BatchTask *>(pl->d_blob);
+    pl->d_items = reinterpret_cast<const BatchItem *>(pl->d_blob + off_items);
+    pl->d_polys = reinterpret_cast<const uint32_t *>(pl->d_blob + off_polys);
+    pl->d_stage_streams = reinterpret_cast<const int32_t *>(pl->d_blob + off_ss);
     *out = pl;
+    return MTGP_OK;
+}
+
+// The plan's descriptors to the device, ordered before the next launch on s.
+int uploadPlan(mtgp_gpu_plan *pl, void *s) {
+    if (!pl->dirty) return MTGP_OK;
+    CK(cudaMemcpyAsync(pl->d_blob, pl->h_blob, pl->blob_bytes, cudaMemcpyHostToDevice, S(s)),
+       "upload plan");
+    pl->dirty = false;
     return MTGP_OK;
 }
 
@@ -930,6 +951,8 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     Pool<T> &P = *static_cast<Pool<T> *>(pl->pool);
     if (pl->ntasks == 0) return MTGP_OK;
     if (pl->out_bytes && !out) return setErr(MTGP_ERR_INVALID, "null output pointer");
+    int rc = uploadPlan(pl, s);
+    if (rc) return rc;
     BatchLaunch b{};
     b.mexp = P.sh.mexp;
     b.mode = pl->mode;
@@ -1060,6 +1083,18 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
         delete *best;
         *best = nullptr;
         return rc;
+    }
+    if (*best) {
+        const mtgp_gpu_plan *b = *best;
+        const char *kern = T::kBits == 64 ? "k_batch64 (one word per thread)"
+                         : b->split      ? "k_batch32 (one word per thread, in-CTA jumps)"
+                         : b->core == 4  ? "k_batch32x4 (four words per thread, 128-bit stores)"
+                                         : "k_batch32 (one word per thread)";
+        char line[200];
+        std::snprintf(line, sizeof line, "chosen: %s, chunk=%lld, grid=%s, tasks=%d: %.4f ms\n",
+                      kern, (long long)(b->split ? b->chunk : 0),
+                      b->grid > 0 ? "3/4" : "all", b->ntasks, best_ms);
+        rep += line;
     }
     if (report && cap > 0) {
         std::snprintf(report, (size_t)cap, "%s", rep.c_str());
@@ -1398,6 +1433,8 @@ int mtgp_gpu_plan_graph_launch(mtgp_gpu_plan_t *pl, void *out, void *s) {
             pl->exec = nullptr;
         }
         cudaGraph_t g = nullptr;
+        int up = uploadPlan(pl, s);  // before the capture: replays reuse the descriptors
+        if (up) return up;
         CK(cudaStreamBeginCapture(S(s), cudaStreamCaptureModeThreadLocal), "begin capture");
         int rc = planLaunch(pl, out, s);
         cudaError_t e = cudaStreamEndCapture(S(s), &g);

@@ -8,14 +8,16 @@
 //     stream, so a batch admitted while others run overlaps them on the GPU;
 //   - a request is admitted when a slot is free and its output fits in the
 //     device output arena (the memory budget); admission is first-come,
-//     first-served, and a request whose stream is busy waits (requests of one
-//     stream run in submission order, each seeing the stream where the
-//     previous one left it);
+//     first-served; a request whose stream has work on the GPU waits, and
+//     requests of one stream run in submission order (several may share a
+//     batch), each seeing the stream where the previous one left it;
 //   - a request's skip is done by generation when short and by a GF(2) jump
 //     when long (mtgp_work_item_t);
 //   - when a batch completes, results are copied to the callers'
-//     destinations (device or host memory; none = discard), the arena space
-//     is returned and the latency (completion - submission) is recorded.
+//     destinations (device or host memory) and their arena space is
+//     returned; a request without a destination keeps its result in the
+//     arena (zero copy, read through mtgp_server_result) until it is
+//     released; the latency (completion - submission) is recorded.
 // A request's output depends only on its stream's position, so it is the
 // same alone and in any mix.
 #include <algorithm>
@@ -34,6 +36,10 @@
 namespace {
 
 using Clock = std::chrono::steady_clock;
+
+// Skips at least this long are done by a GF(2) jump in the batched kernel
+// (the planner's threshold for MEXP 11213 and 23209).
+constexpr uint64_t kJumpSkip = uint64_t(1) << 17;
 
 // First-fit allocator over the output arena, 256-byte granules.
 class Arena {
@@ -91,6 +97,7 @@ struct Req {
     int kind;
     uint64_t skip, count, bytes, off;
     void *dst;
+    bool keep;  // no destination: the result stays in the arena until released
     Clock::time_point t_submit;
 };
 
@@ -122,7 +129,13 @@ struct mtgp_server {
     uint64_t submitted = 0, completed = 0, bytes_done = 0, batches = 0;
     std::vector<double> latency;  // seconds, by ticket - 1; -1 = not done
     std::vector<int> status;      // MTGP_* by ticket - 1
+    std::map<uint64_t, std::pair<uint64_t, uint64_t>> kept;  // ticket -> (offset, bytes)
+    // scheduler time (s): admission, planning + launch, retiring, idle waits
+    double prof[4] = {0, 0, 0, 0};
     Clock::time_point t0;
+
+    int enqueue(int pool, uint32_t stream, int kind, uint64_t skip, uint64_t count, void *dst,
+                bool keep, uint64_t *ticket);
 
     void loop();
     int launch(Slot &sl, std::vector<Req> &reqs);
@@ -168,6 +181,7 @@ void mtgp_server::loop() {
     std::unique_lock<std::mutex> lk(mu);
     while (!stop.load()) {
         bool progressed = false;
+        const Clock::time_point tr = Clock::now();
         // retire finished batches
         for (Slot &sl : slots) {
             if (!sl.busy) continue;
@@ -177,7 +191,10 @@ void mtgp_server::loop() {
             for (const Req &r : sl.reqs) {
                 latency[r.ticket - 1] = std::chrono::duration<double>(now - r.t_submit).count();
                 status[r.ticket - 1] = q == cudaSuccess ? MTGP_OK : MTGP_ERR_CUDA;
-                arena.release(r.off, r.bytes);
+                if (r.keep && r.bytes && q == cudaSuccess)
+                    kept[r.ticket] = {r.off, r.bytes};
+                else
+                    arena.release(r.off, r.bytes);
                 busy[r.pool][r.stream] = 0;
                 completed++;
                 bytes_done += r.bytes;
@@ -187,6 +204,7 @@ void mtgp_server::loop() {
             progressed = true;
         }
         if (progressed) cv_done.notify_all();
+        prof[2] += std::chrono::duration<double>(Clock::now() - tr).count();
         // admit pending requests into a free slot
         Slot *fs = nullptr;
         for (Slot &sl : slots)
@@ -195,22 +213,39 @@ void mtgp_server::loop() {
                 break;
             }
         if (fs && !pending.empty()) {
+            const Clock::time_point ta = Clock::now();
             std::vector<Req> take;
-            for (auto it = pending.begin(); it != pending.end() && (int)take.size() < max_batch;) {
-                if (busy[it->pool][it->stream]) {
-                    ++it;
+            // one pass: admitted requests move to `take`, requests of busy
+            // streams are compacted towards the front (their order kept)
+            auto w = pending.begin(), it = pending.begin();
+            // A stream whose requests are in a batch on the GPU waits; several
+            // requests of one stream may join the same batch (the plan runs
+            // them in order, jumping ahead where they are long), except that
+            // a long skip only opens a stream's part of a batch: the jump
+            // then starts from the stream's window by X^skip, a polynomial
+            // shared by many requests, instead of from an arbitrary position.
+            for (; it != pending.end() && (int)take.size() < max_batch; ++it) {
+                char &b = busy[it->pool][it->stream];
+                if (b == 2 && it->skip >= kJumpSkip) b = 3;  // next batch
+                if (b == 1 || b == 3) {
+                    if (w != it) *w = *it;
+                    ++w;
                     continue;
                 }
                 uint64_t off = 0;
                 if (!arena.alloc(it->bytes, &off)) break;  // first come, first served
                 it->off = off;
-                busy[it->pool][it->stream] = 1;
+                busy[it->pool][it->stream] = 2;
                 take.push_back(*it);
-                it = pending.erase(it);
             }
+            pending.erase(w, it);
+            for (const Req &r : take) busy[r.pool][r.stream] = 1;
+            prof[0] += std::chrono::duration<double>(Clock::now() - ta).count();
             if (!take.empty()) {
                 lk.unlock();
+                const Clock::time_point tl = Clock::now();
                 const int rc = launch(*fs, take);
+                prof[1] += std::chrono::duration<double>(Clock::now() - tl).count();
                 lk.lock();
                 if (rc) {
                     for (const Req &r : take) {
@@ -229,7 +264,11 @@ void mtgp_server::loop() {
                 progressed = true;
             }
         }
-        if (!progressed) cv.wait_for(lk, std::chrono::microseconds(20));
+        if (!progressed) {
+            const Clock::time_point ti = Clock::now();
+            cv.wait_for(lk, std::chrono::microseconds(20));
+            prof[3] += std::chrono::duration<double>(Clock::now() - ti).count();
+        }
     }
 }
 
@@ -271,18 +310,21 @@ int mtgp_server_create(mtgp_server_t **out, mtgp32_gpu_pool_t *p32, mtgp64_gpu_p
     return MTGP_OK;
 }
 
-int mtgp_server_submit(mtgp_server_t *s, int pool, uint32_t stream, int kind, uint64_t skip,
-                       uint64_t count, void *dst, uint64_t *ticket) {
-    if (!s || !ticket) return mtgp::recordError(MTGP_ERR_INVALID, "null server or ticket");
-    if (pool < 0 || pool > 1 || stream >= (uint32_t)s->nstreams[pool])
+int mtgp_server::enqueue(int pool, uint32_t stream, int kind, uint64_t skip, uint64_t count,
+                         void *dst, bool keep, uint64_t *ticket) {
+    if (!ticket) return mtgp::recordError(MTGP_ERR_INVALID, "null ticket");
+    if (pool < 0 || pool > 1 || stream >= (uint32_t)nstreams[pool])
         return mtgp::recordError(MTGP_ERR_INVALID, "no such pool or stream");
     if (kind < -1 || kind > 4) return mtgp::recordError(MTGP_ERR_INVALID, "unknown output kind");
-    const uint64_t bytes = kind < 0 ? 0 : count * (pool == 0 ? 4u : 8u);
-    if (Arena::round(bytes) > s->arena.size())
+    const uint64_t esz = pool == 0 ? 4u : 8u;
+    if (kind >= 0 && count > ~uint64_t(0) / esz)
         return mtgp::recordError(MTGP_ERR_BUDGET, "request larger than the device budget");
-    std::lock_guard<std::mutex> lk(s->mu);
+    const uint64_t bytes = kind < 0 ? 0 : count * esz;
+    if (Arena::round(bytes) > arena.size())
+        return mtgp::recordError(MTGP_ERR_BUDGET, "request larger than the device budget");
+    std::lock_guard<std::mutex> lk(mu);
     Req r{};
-    r.ticket = ++s->submitted;
+    r.ticket = ++submitted;
     r.pool = pool;
     r.stream = stream;
     r.kind = kind;
@@ -290,11 +332,41 @@ int mtgp_server_submit(mtgp_server_t *s, int pool, uint32_t stream, int kind, ui
     r.count = count;
     r.bytes = bytes;
     r.dst = dst;
+    r.keep = keep && !dst;
     r.t_submit = Clock::now();
-    s->latency.push_back(-1.0);
-    s->status.push_back(1);
-    s->pending.push_back(r);
+    latency.push_back(-1.0);
+    status.push_back(1);
+    pending.push_back(r);
     *ticket = r.ticket;
+    cv.notify_one();
+    return MTGP_OK;
+}
+
+int mtgp_server_submit(mtgp_server_t *s, int pool, uint32_t stream, int kind, uint64_t skip,
+                       uint64_t count, void *dst, uint64_t *ticket) {
+    if (!s) return mtgp::recordError(MTGP_ERR_INVALID, "null server");
+    return s->enqueue(pool, stream, kind, skip, count, dst, true, ticket);
+}
+
+int mtgp_server_result(mtgp_server_t *s, uint64_t ticket, void **dev_ptr, uint64_t *bytes) {
+    if (!s || !dev_ptr) return mtgp::recordError(MTGP_ERR_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->kept.find(ticket);
+    if (it == s->kept.end())
+        return mtgp::recordError(MTGP_ERR_INVALID, "no result held for this ticket");
+    *dev_ptr = s->d_arena + it->second.first;
+    if (bytes) *bytes = it->second.second;
+    return MTGP_OK;
+}
+
+int mtgp_server_release(mtgp_server_t *s, uint64_t ticket) {
+    if (!s) return mtgp::recordError(MTGP_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->kept.find(ticket);
+    if (it == s->kept.end())
+        return mtgp::recordError(MTGP_ERR_INVALID, "no result held for this ticket");
+    s->arena.release(it->second.first, it->second.second);
+    s->kept.erase(it);
     s->cv.notify_one();
     return MTGP_OK;
 }
@@ -355,6 +427,13 @@ int mtgp_server_stats(mtgp_server_t *s, uint64_t *completed, uint64_t *bytes, ui
     return MTGP_OK;
 }
 
+int mtgp_server_profile(mtgp_server_t *s, double *seconds, int n) {
+    if (!s || (n > 0 && !seconds)) return mtgp::recordError(MTGP_ERR_INVALID, "bad profile");
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (int k = 0; k < n && k < 4; k++) seconds[k] = s->prof[k];
+    return MTGP_OK;
+}
+
 int mtgp_server_replay(mtgp_server_t *s, const mtgp_request_t *reqs, const double *arrival_s,
                        int n, double *wall_s) {
     if (!s || n < 0 || (n > 0 && (!reqs || !arrival_s)))
@@ -369,7 +448,7 @@ int mtgp_server_replay(mtgp_server_t *s, const mtgp_request_t *reqs, const doubl
         }
         uint64_t t = 0;
         const mtgp_request_t &r = reqs[k];
-        int rc = mtgp_server_submit(s, r.pool, r.stream, r.kind, r.skip, r.count, r.dst, &t);
+        int rc = s->enqueue(r.pool, r.stream, r.kind, r.skip, r.count, r.dst, false, &t);
         if (rc) return rc;
     }
     int rc = mtgp_server_drain(s, 600.0);

@@ -251,3 +251,31 @@ def test_server_budget_and_host_destination(gpu, orc):
     for k in range(40):
         ref = ga[k % 32].fill(0, 200_000)
         assert np.array_equal(outs[k].numpy().view(np.uint32), ref), k
+
+
+def test_server_zero_copy_result_and_budget_admission(gpu, orc):
+    """A request without destination keeps its result in the device arena
+    (zero-copy view); kept results count against the budget, so a request
+    that does not fit waits until the space is released."""
+    from mtgp_gb300._lib import MTGPError
+    from mtgp_gb300.api import Server
+    a, b, p32, _ = _server_pools()
+    ga = _oracle_streams(orc, a, p32)
+    srv = Server(a, b, budget_bytes=1 << 20, slots=2, max_batch=8)
+    t1 = srv.submit(0, 3, 0, 100_000)
+    assert srv.wait(t1) == 0
+    v = srv.result(t1, torch.int32)
+    assert v.numel() == 100_000
+    assert np.array_equal(v.cpu().numpy().view(np.uint32), ga[3].fill(0, 100_000))
+    t2 = srv.submit(0, 4, 2, 200_000)         # 800 KB: does not fit beside t1
+    with pytest.raises(MTGPError) as e:
+        srv.wait(t2, 0.5)
+    assert e.value.code == -6
+    srv.release(t1)
+    assert srv.wait(t2, 30.0) == 0
+    w = srv.result(t2, torch.float32)
+    assert np.array_equal(w.cpu().numpy(), ga[4].fill(2, 200_000))
+    srv.release(t2)
+    with pytest.raises(MTGPError):
+        srv.release(t2)
+    srv.close()
