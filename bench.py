@@ -213,8 +213,12 @@ def run_serving(args, s, local):
     0.3 / 0.6 / 0.9 of it with p50 / p99 latency (submission to the result
     resident in device memory)."""
     import torch
-    from mtgp_gb300.api import Pool, Server, requests
+    from mtgp_gb300.api import Pool, Server, requests, set_tuning
     from mtgp_gb300.params import jump_table, load_table
+    # the library's default planning (the batched section's tuning is global)
+    set_tuning("core", 4)
+    set_tuning("split_chunk", 0)
+    set_tuning("batch_grid", 0)
     p32 = load_table("mtgp32_fast_11213")[0]
     p64 = load_table("mtgp64dc_fast_11213")[0]
     a = Pool.substreams(p32, SEED, 4096, jump_table(32), stream=s)
@@ -385,6 +389,11 @@ def main():
         plan, tune_report = pool.autotune(items, out, stream=s, reps=2)
     plan_ms = (time.perf_counter() - t0) * 1e3
     plan_tasks, plan_chunk = plan.info()
+    plan_cfg = plan.describe()
+    # plans made later (the e2e leg) use the same configuration
+    set_tuning("core", plan_cfg["core"])
+    set_tuning("split_chunk", plan_cfg["split_chunk"] or -1)
+    set_tuning("batch_grid", plan_cfg["grid"])
 
     # first step, kept for the CPU-baseline leg's bit-exact check
     plan.launch(out, s)
@@ -414,7 +423,9 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * total_bytes / (ms * 1e-3) / 1e9
-    launches = 2 * args.steps  # memset of the work counter + the persistent kernel
+    # the persistent kernel (+ the staged-window copy of split plans) per
+    # step; the work-counter reset is a memset, not a kernel
+    launches = plan_cfg["kernels_per_launch"] * args.steps
 
     if args.only != "all":
         args.plain_steps = 0
@@ -471,9 +482,15 @@ def main():
     achieved = (total_bytes + state_bytes) / (ms * 1e-3) / 1e9
     chosen = [l for l in tune_report.splitlines() if l.startswith("chosen:")]
     kernel = chosen[0][len("chosen:"):].split(", chunk=")[0].strip() if chosen else None
+    # DRAM bytes (read + write) of one launch of the batched kernel on this
+    # workload, measured once with ncu (dram__bytes_read.sum +
+    # dram__bytes_write.sum = 11.58 MB + 1.69 GB); only valid for the full
+    # default workload
+    traffic = 1.70e9 if (nsub == N_SUB and args.uniform <= 0) else None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
-                "traffic": None, "kernel": kernel}
+                "traffic": traffic, "algorithmic_bytes": total_bytes + state_bytes,
+                "kernel": kernel}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -508,7 +525,7 @@ def main():
             "bank": {"value": round(bank_gbs, 2), "unit": "GB/s", "ms": round(bank_ms, 3),
                      "workload": "128 sets x 2^21 uint32, seeds 1234+i, one CTA per set"},
             "jump_setup": {"ms": round(jump_ms, 2), "us_per_substream": round(1e3 * jump_ms / nsub, 2)},
-            "plan": {"tasks": plan_tasks, "split_chunk": plan_chunk,
+            "plan": {"tasks": plan_tasks, "split_chunk": plan_chunk, "config": plan_cfg,
                      "autotune_ms": round(plan_ms, 1),
                      "autotune": [l for l in tune_report.strip().splitlines()]},
             "serve": serve,

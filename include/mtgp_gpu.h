@@ -355,6 +355,13 @@ uint64_t mtgp_gpu_plan_output_bytes(const mtgp_gpu_plan_t *plan);
  * long requests (0 = none split). */
 int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *plan, int64_t *tasks,
                        int64_t *chunk);
+/* The plan's configuration, the first n of: [0] tasks, [1] split chunk
+ * length (0 = none), [2] generation core (1 or 4), [3] grid (0 = all
+ * resident CTAs), [4] kernels one launch runs, [5] 1 if tasks start with
+ * in-kernel jumps.  Passing these to mtgp_gpu_set_tuning ("core",
+ * "split_chunk" (-1 for 0), "batch_grid") makes plans of the same kind. */
+int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
+                           int n);
 /* Process-wide tuning knobs for plans made afterwards (no reference
  * counterpart; the autotuner and tests use them):
  *   "split_chunk"  0 = automatic, < 0 = never split, > 0 = chunk length

@@ -48,6 +48,7 @@ SIGS = {
     "mtgp_gpu_plan_output_bytes": (c_u64, [vp]),
     "mtgp_gpu_plan_free": (None, [vp]),
     "mtgp_gpu_plan_info": (c_int, [vp, vp, vp]),
+    "mtgp_gpu_plan_describe": (c_int, [vp, vp, c_int]),
     "mtgp_gpu_set_tuning": (c_int, [cp, ctypes.c_int64]),
     "mtgp32_gpu_batch_noalloc": (c_int, [P32, c_int, vp, vp, c_int, vp, c_int, vp, vp]),
     "mtgp_server_create": (c_int, [pp, vp, vp, c_u64, c_int, c_int]),

@@ -163,6 +163,14 @@ class Plan:
         check(lib().mtgp_gpu_plan_info(self.h, ctypes.byref(t), ctypes.byref(c)))
         return t.value, c.value
 
+    def describe(self):
+        """Configuration: tasks, split chunk, core, grid, kernels per launch,
+        jumps (see mtgp_gpu_plan_describe)."""
+        v = np.zeros(6, dtype=np.int64)
+        check(lib().mtgp_gpu_plan_describe(self.h, v.ctypes.data_as(ctypes.c_void_p), 6))
+        return {"tasks": int(v[0]), "split_chunk": int(v[1]), "core": int(v[2]),
+                "grid": int(v[3]), "kernels_per_launch": int(v[4]), "jumps": bool(v[5])}
+
     def launch(self, out, stream=None):
         check(lib().mtgp_gpu_plan_launch(self.h, ctypes.c_void_p(out.data_ptr()), _stream(stream)))
 

@@ -40,6 +40,17 @@ template <int N> struct SplitGeo64 { using G = void; };
 template <> struct SplitGeo64<176> { using G = JGeo<176, 7, 128, 128, 1024>; };
 template <> struct SplitGeo64<363> { using G = JGeo<363, 13, 256, 256, 2048>; };
 
+// Words per sub-step of the four-words-per-thread batched kernel (W/4
+// threads per CTA).  It cannot exceed the shape's one-word-per-thread width
+// TN: a sub-step's words are computed in parallel, so none of them may
+// depend on another (y of word i is word i - N + pos, and pos <= N - TN).
+template <int N, int TN> constexpr int kW4 = TN;
+
+// The same for the four-words-per-thread kernel (NT = W/4 threads).
+template <int N> struct SplitGeo32x4 { using G = void; };
+template <> struct SplitGeo32x4<351> { using G = JGeo<351, 11, 64, 64, 1024>; };
+template <> struct SplitGeo32x4<726> { using G = JGeo<726, 23, 128, 128, 2048>; };
+
 template <int N> constexpr bool kSplit32 = (N == 351 || N == 726);
 template <int N> constexpr bool kSplit64 = (N == 176 || N == 363);
 
@@ -115,9 +126,10 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
     }
 }
 
-// Four-words-per-thread core (W/4 threads per CTA), for plans without split
-// requests.
-template <int N, int W, int B, int MODE>
+// Four-words-per-thread core (W/4 threads per CTA).  SPLIT: tasks may start
+// with a jump; the jump works on the window laid out linearly, which is then
+// moved into the four planes of the generation buffer.
+template <int N, int W, int B, int MODE, bool SPLIT>
 __global__ void __launch_bounds__(W / 4, MODE == -2 ? 1 : 1280 / W * 4)
 k_batch32x4(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
             const BatchTask *__restrict__ tasks, int ntasks,
@@ -140,7 +152,33 @@ k_batch32x4(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
         Lane32 L;
         L.load(params[TK.pidx], threadIdx.x & 31);
         const uint32_t *src = states + (size_t)TK.stream * stateStride(N);
-        for (int k = threadIdx.x; k < N; k += T) buf[plane_at<PW>(k)] = src[k];
+        bool planar = true;
+        if constexpr (SPLIT && kSplit32<N>) {
+            using G = typename SplitGeo32x4<N>::G;
+            static_assert(G::NT == T, "jump geometry must use the kernel's threads");
+            static_assert(G::template bytes<uint32_t>(N / 32 + 1) <= sizeof(buf),
+                          "jump buffers must fit the generation buffer");
+            if (TK.j0 >= 0) {
+                for (int k = threadIdx.x; k < N; k += T) buf[k] = src[k];
+                jump_task<Tr32, G>(buf, L, TK, polys, nwords);  // ends with a barrier
+                constexpr int PER = (N + T - 1) / T;
+                uint32_t v[PER];
+#pragma unroll
+                for (int i = 0; i < PER; i++) {
+                    const int k = threadIdx.x + i * T;
+                    if (k < N) v[i] = buf[k];
+                }
+                __syncthreads();
+#pragma unroll
+                for (int i = 0; i < PER; i++) {
+                    const int k = threadIdx.x + i * T;
+                    if (k < N) buf[plane_at<PW>(k)] = v[i];
+                }
+                planar = false;
+            }
+        }
+        if (planar)
+            for (int k = threadIdx.x; k < N; k += T) buf[plane_at<PW>(k)] = src[k];
         __syncthreads();
         for (int i = 0; i < TK.nitems; i++) {
             const BatchItem I = items[TK.first + i];
@@ -291,18 +329,18 @@ static cudaError_t mode32(const BatchLaunch &b, const DevParams32 *p, uint32_t *
     }
 }
 
-template <int N, int W, int B>
+template <int N, int W, int B, bool SPLIT>
 static cudaError_t mode32x4(const BatchLaunch &b, const DevParams32 *p, uint32_t *st,
                             cudaStream_t s) {
     constexpr int T = W / 4;
     switch (b.mode) {
-    case -1: return go<uint32_t>(k_batch32x4<N, W, B, -1>, T, b, p, st, s);
-    case 0: return go<uint32_t>(k_batch32x4<N, W, B, 0>, T, b, p, st, s);
-    case 1: return go<uint32_t>(k_batch32x4<N, W, B, 1>, T, b, p, st, s);
-    case 2: return go<uint32_t>(k_batch32x4<N, W, B, 2>, T, b, p, st, s);
-    case 3: return go<uint32_t>(k_batch32x4<N, W, B, 3>, T, b, p, st, s);
-    case 4: return go<uint32_t>(k_batch32x4<N, W, B, 4>, T, b, p, st, s);
-    default: return go<uint32_t>(k_batch32x4<N, W, B, -2>, T, b, p, st, s);
+    case -1: return go<uint32_t>(k_batch32x4<N, W, B, -1, SPLIT>, T, b, p, st, s);
+    case 0: return go<uint32_t>(k_batch32x4<N, W, B, 0, SPLIT>, T, b, p, st, s);
+    case 1: return go<uint32_t>(k_batch32x4<N, W, B, 1, SPLIT>, T, b, p, st, s);
+    case 2: return go<uint32_t>(k_batch32x4<N, W, B, 2, SPLIT>, T, b, p, st, s);
+    case 3: return go<uint32_t>(k_batch32x4<N, W, B, 3, SPLIT>, T, b, p, st, s);
+    case 4: return go<uint32_t>(k_batch32x4<N, W, B, 4, SPLIT>, T, b, p, st, s);
+    default: return go<uint32_t>(k_batch32x4<N, W, B, -2, SPLIT>, T, b, p, st, s);
     }
 }
 
@@ -325,10 +363,13 @@ static cudaError_t run32x(const BatchLaunch &b, const DevParams32 *p, uint32_t *
                           cudaStream_t s) {
     cudaError_t e;
     if (b.split) {
-        if constexpr (kSplit32<N>) e = mode32<N, TN, B, true>(b, p, st, s);
-        else return cudaErrorInvalidValue;
+        if constexpr (kSplit32<N>)
+            e = b.core == 4 ? mode32x4<N, kW4<N, TN>, B, true>(b, p, st, s)
+                            : mode32<N, TN, B, true>(b, p, st, s);
+        else
+            return cudaErrorInvalidValue;
     } else if (b.core == 4) {
-        e = mode32x4<N, TN, B>(b, p, st, s);
+        e = mode32x4<N, kW4<N, TN>, B, false>(b, p, st, s);
     } else {
         e = mode32<N, TN, B, false>(b, p, st, s);
     }
@@ -379,17 +420,29 @@ cudaError_t launchBatch64(const BatchLaunch &b, const DevParams64 *params, uint6
 bool batchSplits32(int mexp) { return mexp == 11213 || mexp == 23209; }
 bool batchSplits64(int mexp) { return mexp == 11213 || mexp == 23209; }
 
-int batchResident32(int mexp, bool split) {
+// Resident CTAs of the kernel a plan with (or without) split requests uses
+// under the current generation core.
+template <int N, int T, int B>
+static int resident32(bool split) {
     int g = 0;
-#define X(M, N, T, B)                                                              \
-    if (mexp == M) {                                                               \
-        if (split) resident(k_batch32<N, T, B, 0, true>, T, &g);                  \
-        else if (genCore32() == 4) resident(k_batch32x4<N, T, B, 0>, T / 4, &g);   \
-        else resident(k_batch32<N, T, B, 0, false>, T, &g);                        \
+    const bool jumps = split && kSplit32<N>;
+    if (genCore32() == 4) {
+        constexpr int W = kW4<N, T>;
+        if (jumps) resident(k_batch32x4<N, W, B, 0, kSplit32<N>>, W / 4, &g);
+        else resident(k_batch32x4<N, W, B, 0, false>, W / 4, &g);
+    } else {
+        if (jumps) resident(k_batch32<N, T, B, 0, kSplit32<N>>, T, &g);
+        else resident(k_batch32<N, T, B, 0, false>, T, &g);
     }
+    return g;
+}
+
+int batchResident32(int mexp, bool split) {
+#define X(M, N, T, B) \
+    if (mexp == M) return resident32<N, T, B>(split);
     MTGP_SHAPES32(X)
 #undef X
-    return g;
+    return 0;
 }
 
 int batchResident64(int mexp, bool split) {

@@ -752,7 +752,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     }
     int64_t chunk = 0;
     if (can_jump) {
-        if (!P.resident_split) P.resident_split = T::resident(P.sh.mexp, true);
+        P.resident_split = T::resident(P.sh.mexp, true);  // depends on the core; cached below
         if (g_tune.split_chunk > 0) {
             chunk = g_tune.split_chunk;
         } else if (g_tune.split_chunk == 0) {
@@ -985,8 +985,8 @@ int planLaunch(mtgp_gpu_plan *pl, void *out, void *s) {
 // Candidates: generation core (32-bit: four words per thread in 64-thread
 // CTAs with 128-bit stores, or one word per thread in 256-thread CTAs with
 // 32-bit stores), split-chunk length for long requests (none, or 2^17 to
-// 2^20 in steps of 2^17), and grid size (all resident CTAs or three
-// quarters of them).
+// 2^20 in steps of 2^17, with either core), and grid size (all resident
+// CTAs, three quarters or half of them).
 template <class T>
 int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, void *s,
              int reps, mtgp_gpu_plan **best, char *report, int cap) {
@@ -1002,7 +1002,9 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
     const int cores[2] = {4, 1};
     for (int c = 0; c < (T::kBits == 32 ? 2 : 1); c++) cands.push_back({cores[c], -1, 0});
     if (T::splits(P.sh.mexp))
-        for (int64_t ch = 1 << 17; ch <= (1 << 20); ch += 1 << 17) cands.push_back({1, ch, 0});
+        for (int c = 0; c < (T::kBits == 32 ? 2 : 1); c++)
+            for (int64_t ch = 1 << 17; ch <= (1 << 20); ch += 1 << 17)
+                cands.push_back({cores[c], ch, 0});
     const size_t sbytes = sizeof(W) * (size_t)P.stride * P.count;
     W *snap = nullptr;
     CK(cudaMalloc(&snap, sbytes), "cudaMalloc(autotune snapshot)");
@@ -1035,21 +1037,23 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
         return MTGP_OK;
     };
     for (size_t k = 0; k < cands.size() && !rc; k++) {
-        for (int g = 0; g < 2 && !rc; g++) {
+        for (int g = 0; g < 3 && !rc; g++) {
             g_tune.split_chunk = cands[k].chunk;
             g_tune.batch_grid = 0;
             setGenCore32(cands[k].core);
             mtgp_gpu_plan *pl = nullptr;
             rc = makePlan(P, items, nitems, &pl);
             if (rc) break;
-            if (cands[k].chunk > 0 && !pl->split) {  // nothing long enough to split
+            if (cands[k].chunk > 0 && pl->chunk == 0) {  // nothing long enough to split
                 delete pl;
                 break;
             }
-            if (g == 1) {
-                // three quarters of the resident CTAs
+            if (g > 0) {
+                // three quarters or half of the resident CTAs: fewer CTAs
+                // share an SM's data pipe, so each runs its tasks faster,
+                // which pays when the longest tasks set the launch's length
                 const int full = T::resident(P.sh.mexp, pl->split);
-                pl->grid = std::max(1, full * 3 / 4);
+                pl->grid = std::max(1, g == 1 ? full * 3 / 4 : full / 2);
             }
             float ms = 0;
             rc = timeOne(pl, &ms);
@@ -1059,8 +1063,8 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
             }
             char line[160];
             std::snprintf(line, sizeof line, "core=%d chunk=%lld grid=%s tasks=%d: %.4f ms\n",
-                          pl->split ? 1 : pl->core, (long long)(pl->split ? pl->chunk : 0),
-                          g ? "3/4" : "all", pl->ntasks, ms);
+                          T::kBits == 64 ? 1 : pl->core, (long long)pl->chunk,
+                          g == 0 ? "all" : g == 1 ? "3/4" : "1/2", pl->ntasks, ms);
             rep += line;
             if (!*best || ms < best_ms) {
                 delete *best;
@@ -1086,14 +1090,18 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
     }
     if (*best) {
         const mtgp_gpu_plan *b = *best;
-        const char *kern = T::kBits == 64 ? "k_batch64 (one word per thread)"
-                         : b->split      ? "k_batch32 (one word per thread, in-CTA jumps)"
-                         : b->core == 4  ? "k_batch32x4 (four words per thread, 128-bit stores)"
-                                         : "k_batch32 (one word per thread)";
-        char line[200];
+        const char *kern =
+            T::kBits == 64 ? (b->split ? "k_batch64 (one word per thread, in-CTA jumps)"
+                                       : "k_batch64 (one word per thread)")
+            : b->core == 4 ? (b->split ? "k_batch32x4 (four words per thread, in-CTA jumps)"
+                                       : "k_batch32x4 (four words per thread)")
+                           : (b->split ? "k_batch32 (one word per thread, in-CTA jumps)"
+                                       : "k_batch32 (one word per thread)");
+        char grid[32], line[200];
+        if (b->grid > 0) std::snprintf(grid, sizeof grid, "%d CTAs", b->grid);
+        else std::snprintf(grid, sizeof grid, "all resident");
         std::snprintf(line, sizeof line, "chosen: %s, chunk=%lld, grid=%s, tasks=%d: %.4f ms\n",
-                      kern, (long long)(b->split ? b->chunk : 0),
-                      b->grid > 0 ? "3/4" : "all", b->ntasks, best_ms);
+                      kern, (long long)b->chunk, grid, b->ntasks, best_ms);
         rep += line;
     }
     if (report && cap > 0) {
@@ -1458,6 +1466,14 @@ int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *pl, int64_t *tasks, int64_t *chunk
     if (!pl) return setErr(MTGP_ERR_INVALID, "null plan");
     if (tasks) *tasks = pl->ntasks;
     if (chunk) *chunk = pl->chunk;
+    return MTGP_OK;
+}
+
+int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *pl, int64_t *values, int n) {
+    if (!pl || (n > 0 && !values)) return setErr(MTGP_ERR_INVALID, "null plan or values");
+    const int64_t v[6] = {pl->ntasks, pl->chunk, pl->bits == 64 ? 1 : pl->core, pl->grid,
+                          pl->ntasks ? 1 + (pl->nstage > 0) : 0, pl->split ? 1 : 0};
+    for (int k = 0; k < n && k < 6; k++) values[k] = v[k];
     return MTGP_OK;
 }
 

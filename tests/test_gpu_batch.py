@@ -130,11 +130,14 @@ def test_batch_rejects_bad_items(gpu):
 @pytest.mark.parametrize("bits,table", [(32, "mtgp32_fast_11213"), (64, "mtgp64dc_fast_11213"),
                                         (32, "mtgp32_fast_23209"), (64, "mtgp64_fast_23209")])
 @pytest.mark.parametrize("mixed", [False, True])
-def test_batch_split_long_requests(gpu, orc, bits, table, mixed):
+@pytest.mark.parametrize("core", [4, 1])
+def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core):
     """Long requests split into chunks whose start states are GF(2) jumps
-    done inside the batched kernel: bit-exact outputs and final states,
-    across two launches of the same plan."""
+    done inside the batched kernel (either 32-bit generation core): bit-exact
+    outputs and final states, across two launches of the same plan."""
     from mtgp_gb300.api import Pool, set_tuning, work_items
+    if bits == 64 and core == 1:
+        pytest.skip("one 64-bit core")
     tbl = load_table(table)
     rng = np.random.default_rng(bits + mixed + tbl[0].mexp)
     nstreams = 24
@@ -147,16 +150,18 @@ def test_batch_split_long_requests(gpu, orc, bits, table, mixed):
     kinds = rng.integers(0, 5, nstreams) if mixed else np.zeros(nstreams, np.int64)
     esz = bits // 8
     offs = np.concatenate([[0], np.cumsum(counts)[:-1]]) * esz
-    # one stream gets two items (a multi-item task is never split)
+    # one stream gets two items (its run is cut across the item boundary)
     streams = list(range(nstreams)) + [5]
     kinds = list(kinds) + [0]
     counts = list(counts) + [20000]
     offs = list(offs) + [int(sum(counts[:-1])) * esz]
     set_tuning("split_chunk", 1500)
+    set_tuning("core", core)
     try:
         plan = pool.plan(work_items(streams, kinds, counts, offs))
     finally:
         set_tuning("split_chunk", 0)
+        set_tuning("core", 4)
     ntasks, chunk = plan.info()
     assert chunk == 1500 and ntasks > nstreams
     out = torch.zeros(int(sum(counts)) * esz // 4 + 16, dtype=torch.int32, device="cuda")
