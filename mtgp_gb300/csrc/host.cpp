@@ -19,6 +19,7 @@
 #include "batch.h"
 #include "gf2.h"
 #include "internal.h"
+#include "plan_core.h"
 
 namespace mtgp {
 
@@ -285,7 +286,7 @@ struct Pool {
     std::vector<std::vector<gf2::Poly>> pow2;
     // X^steps mod chi, keyed by (parameter set, steps); bounded
     std::map<std::pair<int, uint64_t>, gf2::Poly> jcache;
-    int resident = 0, resident_split = 0;
+    PlanResult plan_scratch;  // reused by every plan of this pool
 
     ~Pool() {
         cudaFree(d_params);
@@ -661,116 +662,23 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     using W = typename T::W;
     if (!out) return setErr(MTGP_ERR_INVALID, "null plan pointer");
     if (*out && (*out)->pool != &P) return setErr(MTGP_ERR_INVALID, "plan belongs to another pool");
-    if (nitems < 0 || (nitems > 0 && !items)) return setErr(MTGP_ERR_INVALID, "bad item list");
-    // group by stream, keeping the caller's order within a stream
-    std::vector<std::vector<int>> by(P.count);
-    uint64_t out_bytes = 0;
-
-    for (int k = 0; k < nitems; k++) {
-        const mtgp_work_item_t &it = items[k];
-        if (it.stream >= (uint32_t)P.count)
-            return setErr(MTGP_ERR_INVALID, "item %d: stream %u out of range", k, it.stream);
-        if (it.kind < -1 || it.kind > 4)
-            return setErr(MTGP_ERR_INVALID, "item %d: unknown kind %d", k, it.kind);
-        if (it.kind >= 0 && it.out_offset % sizeof(W))
-            return setErr(MTGP_ERR_INVALID, "item %d: offset not a multiple of %zu", k, sizeof(W));
-        if (it.count == 0 && it.skip == 0) continue;
-        by[it.stream].push_back(k);
-        if (it.kind >= 0) out_bytes = std::max(out_bytes, it.out_offset + it.count * sizeof(W));
-    }
-    // Each stream's items become one or more tasks.  Positions count steps
-    // from the stream's window at launch.  On exponents whose batched
-    // kernels carry the jump code, a skip of at least kJumpMinSkip (or an
-    // advance-only item that long) is not generated: the work after it is a
-    // new task whose window is the stream's window jumped by X^start mod chi
-    // inside the kernel.  A run of work between jumps much longer than `chunk`
-    // is cut into chunks the same way.  The tasks of one stream all start
-    // from the same window and run in parallel; when there are several, the
-    // last leaves its final window in a staging slot that a second kernel
-    // copies back after the launch (see batch_kernels.cu).
-    struct Run {
-        int s;
-        uint64_t start, total;
-        std::vector<BatchItem> items;
-    };
-    const bool can_jump = T::splits(P.sh.mexp);
-    std::vector<Run> runs;
-    uint64_t grand = 0;
-    for (int s = 0; s < P.count; s++) {
-        if (by[s].empty()) continue;
-        Run cur{s, 0, 0, {}};
-        uint64_t pos = 0;
-        for (int k : by[s]) {
-            const mtgp_work_item_t &it = items[k];
-            uint64_t skip = it.skip, count = it.count;
-            if (it.kind < 0) {  // advance only: all of it is a skip
-                skip += count;
-                count = 0;
-                if (skip < it.skip) return setErr(MTGP_ERR_INVALID, "item %d: skip overflows", k);
-            }
-            if (pos + skip < pos || pos + skip + count < pos + skip)
-                return setErr(MTGP_ERR_INVALID, "item %d: stream position overflows 64 bits", k);
-            if (skip >= kJumpMinSkip && can_jump) {
-                if (!cur.items.empty()) {
-                    grand += cur.total;
-                    runs.push_back(std::move(cur));
-                }
-                pos += skip;
-                cur = Run{s, pos, 0, {}};
-            } else if (skip) {
-                if (skip > kMaxGenSkip)
-                    return setErr(MTGP_ERR_UNSUPPORTED,
-                                  "item %d: skip of %llu values would be generated (no in-kernel "
-                                  "jump for this exponent); jump the stream instead",
-                                  k, (unsigned long long)skip);
-                BatchItem sk{};
-                sk.count = skip;
-                sk.kind = -1;
-                cur.items.push_back(sk);
-                cur.total += skip;
-                pos += skip;
-            }
-            if (count) {
-                BatchItem bi{};
-                bi.out_off = it.out_offset;
-                bi.count = count;
-                bi.kind = it.kind;
-                cur.items.push_back(bi);
-                cur.total += count;
-                pos += count;
-            }
-        }
-        if (!cur.items.empty() || cur.start) {
-            if (cur.items.empty()) {  // ends with a jump: a task that only jumps
-                BatchItem z{};
-                z.kind = -1;
-                cur.items.push_back(z);
-            }
-            grand += cur.total;
-            runs.push_back(std::move(cur));
-        }
-    }
-    int64_t chunk = 0;
-    if (can_jump) {
-        P.resident_split = T::resident(P.sh.mexp, true);  // depends on the core; cached below
-        if (g_tune.split_chunk > 0) {
-            chunk = g_tune.split_chunk;
-        } else if (g_tune.split_chunk == 0) {
-            // a task longer than the average load of one CTA slot would set
-            // the length of the whole launch
-            const uint64_t per = grand / (uint64_t)std::max(P.resident_split, 1);
-            chunk = 1 << 17;
-            while ((uint64_t)chunk < per) chunk <<= 1;
-        }
-    }
-    struct Tk {
-        BatchTask t;
-        std::vector<BatchItem> items;
-        uint64_t total;
-        uint64_t run, off;  // start = run start + offset in the run
-    };
-    std::vector<Tk> order;
-    std::vector<int32_t> stage_streams;
+    PlanOptions o;
+    o.nstreams = P.count;
+    o.word_bytes = sizeof(W);
+    o.can_jump = T::splits(P.sh.mexp);
+    o.jump_min = kJumpMinSkip;
+    o.max_gen_skip = kMaxGenSkip;
+    o.chunk_tune = g_tune.split_chunk;
+    o.resident = o.can_jump ? T::resident(P.sh.mexp, true) : 1;  // depends on the core
+    PlanResult &R = P.plan_scratch;
+    std::string msg;
+    int rc = planCore(items, nitems, o, &R, &msg);
+    if (rc) return setErr(rc, "%s", msg.c_str());
+    const uint64_t out_bytes = R.out_bytes;
+    const int64_t chunk = R.chunk;
+    const bool cut = chunk > 0;
+    const int mode = R.mode;
+    std::vector<int32_t> &stage_streams = R.stage_streams;
     // the plan's jump polynomials: X^steps mod chi for (parameter set, steps)
     const size_t pw = (size_t)P.polyWords();
     std::map<std::pair<int, uint64_t>, int> poly_at;
@@ -779,8 +687,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         auto hit = poly_at.find({pidx, steps});
         if (hit == poly_at.end()) {
             const gf2::Poly *p = nullptr;
-            int rc = P.jumpPoly(pidx, steps, &p);
-            if (rc) return rc;
+            int rc2 = P.jumpPoly(pidx, steps, &p);
+            if (rc2) return rc2;
             hit = poly_at.emplace(std::make_pair(pidx, steps), (int)(polys.size() / pw)).first;
             const std::vector<uint32_t> w = gf2::toWords32(*p, (int)pw);
             polys.insert(polys.end(), w.begin(), w.end());
@@ -788,79 +696,34 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         *idx = hit->second;
         return MTGP_OK;
     };
-    bool cut = false;
-    for (size_t r0 = 0, r1; r0 < runs.size(); r0 = r1) {
-        for (r1 = r0; r1 < runs.size() && runs[r1].s == runs[r0].s; r1++) {
+    std::vector<BatchTask> tasks(R.tasks.size());
+    for (size_t q = 0; q < R.tasks.size(); q++) {
+        const PlanTask &pt = R.tasks[q];
+        BatchTask &t = tasks[q];
+        t = BatchTask{};
+        t.stream = pt.stream;
+        t.first = (int32_t)pt.first;
+        t.nitems = (int32_t)pt.n;
+        t.pidx = P.hpidx[pt.stream];
+        t.j0 = t.j1 = -1;
+        t.wb = pt.wb;
+        // X^run then X^off: the run starts (a requested skip) and the chunk
+        // offsets (shared by every long request) are each few, so few
+        // distinct polynomials are needed
+        if (pt.run && pt.off) {
+            rc = polyIndex(t.pidx, pt.run, &t.j0);
+            if (!rc) rc = polyIndex(t.pidx, pt.off, &t.j1);
+        } else if (pt.run || pt.off) {
+            rc = polyIndex(t.pidx, pt.run | pt.off, &t.j0);
         }
-        const int s = runs[r0].s;
-        const size_t first = order.size();
-        for (size_t r = r0; r < r1; r++) {
-            const Run &R = runs[r];
-            uint64_t k = 1;
-            if (chunk > 0 && R.total > (uint64_t)chunk + (uint64_t)chunk / 4) {
-                k = (R.total + (uint64_t)chunk - 1) / (uint64_t)chunk;
-                cut = true;
-            }
-            size_t ii = 0;      // item of R being cut
-            uint64_t used = 0;  // values of it already taken
-            for (uint64_t c = 0; c < k; c++) {
-                Tk tk{};
-                tk.t.stream = s;
-                tk.t.pidx = P.hpidx[s];
-                tk.t.j0 = tk.t.j1 = -1;
-                tk.run = R.start;
-                tk.off = c * (uint64_t)chunk;
-                uint64_t want = (c + 1 == k) ? ~uint64_t(0) : (uint64_t)chunk;
-                while (ii < R.items.size() && (want || R.items[ii].count == used)) {
-                    BatchItem bi = R.items[ii];
-                    const uint64_t take = std::min(bi.count - used, want);
-                    if (bi.kind >= 0) bi.out_off += used * sizeof(W);
-                    bi.count = take;
-                    tk.items.push_back(bi);
-                    tk.total += take;
-                    want -= take;
-                    used += take;
-                    if (used == R.items[ii].count) {
-                        ii++;
-                        used = 0;
-                    }
-                }
-                order.push_back(std::move(tk));
-            }
-        }
-        const size_t m = order.size() - first;
-        for (size_t q = first; q < order.size(); q++) {
-            Tk &tk = order[q];
-            tk.t.wb = m == 1 ? kWbStream
-                             : (q + 1 == order.size() ? (int32_t)stage_streams.size() : kWbNone);
-            // X^run then X^off: the run starts (a requested skip) and the
-            // chunk offsets (shared by every long request) are each few,
-            // so few distinct polynomials are needed
-            int rc = MTGP_OK;
-            if (tk.run && tk.off) {
-                rc = polyIndex(tk.t.pidx, tk.run, &tk.t.j0);
-                if (!rc) rc = polyIndex(tk.t.pidx, tk.off, &tk.t.j1);
-            } else if (tk.run || tk.off) {
-                rc = polyIndex(tk.t.pidx, tk.run | tk.off, &tk.t.j0);
-            }
-            if (rc) return rc;
-        }
-        if (m > 1) stage_streams.push_back(s);
+        if (rc) return rc;
     }
-    // longest task first
-    std::stable_sort(order.begin(), order.end(),
-                     [](const Tk &a, const Tk &b) { return a.total > b.total; });
-    std::vector<BatchTask> tasks;
-    std::vector<BatchItem> bitems;
-    int mode = -3;  // the output kind shared by all items, -2 if mixed
-    for (Tk &tk : order) {
-        tk.t.first = (int)bitems.size();
-        tk.t.nitems = (int)tk.items.size();
-        for (const BatchItem &bi : tk.items) {
-            bitems.push_back(bi);
-            if (bi.count) mode = (mode == -3 || mode == bi.kind) ? bi.kind : -2;
-        }
-        tasks.push_back(tk.t);
+    std::vector<BatchItem> bitems(R.segs.size());
+    for (size_t q = 0; q < R.segs.size(); q++) {
+        bitems[q].out_off = R.segs[q].out_off;
+        bitems[q].count = R.segs[q].count;
+        bitems[q].kind = R.segs[q].kind;
+        bitems[q].pad_ = 0;
     }
     const bool split = !polys.empty();  // the kernel variant with the jump code
     // reuse the caller's plan (replan) when given: its device buffers are
@@ -879,7 +742,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->bits = T::kBits;
     pl->pool = &P;
     pl->ntasks = (int)tasks.size();
-    pl->mode = mode == -3 ? -1 : mode;
+    pl->mode = mode;
     pl->out_bytes = out_bytes;
     pl->grid = (int)g_tune.batch_grid;
     pl->split = split;

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "server_core.h"
 
 namespace {
 
@@ -41,65 +42,8 @@ using Clock = std::chrono::steady_clock;
 // (the planner's threshold for MEXP 11213 and 23209).
 constexpr uint64_t kJumpSkip = uint64_t(1) << 17;
 
-// First-fit allocator over the output arena, 256-byte granules.
-class Arena {
-  public:
-    void init(uint64_t n) {
-        size_ = n;
-        free_.clear();
-        free_[0] = n;
-    }
-    static uint64_t round(uint64_t n) { return (n + 255) & ~uint64_t(255); }
-    bool alloc(uint64_t n, uint64_t *off) {
-        n = round(n);
-        if (n == 0) {
-            *off = 0;
-            return true;
-        }
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second < n) continue;
-            *off = it->first;
-            const uint64_t rest = it->second - n, at = it->first + n;
-            free_.erase(it);
-            if (rest) free_[at] = rest;
-            return true;
-        }
-        return false;
-    }
-    void release(uint64_t off, uint64_t n) {
-        n = round(n);
-        if (n == 0) return;
-        auto it = free_.emplace(off, n).first;
-        auto nx = std::next(it);
-        if (nx != free_.end() && it->first + it->second == nx->first) {
-            it->second += nx->second;
-            free_.erase(nx);
-        }
-        if (it != free_.begin()) {
-            auto pv = std::prev(it);
-            if (pv->first + pv->second == it->first) {
-                pv->second += it->second;
-                free_.erase(it);
-            }
-        }
-    }
-    uint64_t size() const { return size_; }
-
-  private:
-    uint64_t size_ = 0;
-    std::map<uint64_t, uint64_t> free_;
-};
-
-struct Req {
-    uint64_t ticket;
-    int pool;
-    uint32_t stream;
-    int kind;
-    uint64_t skip, count, bytes, off;
-    void *dst;
-    bool keep;  // no destination: the result stays in the arena until released
-    Clock::time_point t_submit;
-};
+using Req = mtgp::ServeReq;
+using mtgp::Arena;
 
 struct Slot {
     cudaStream_t cs = nullptr;
@@ -195,7 +139,7 @@ void mtgp_server::loop() {
                     kept[r.ticket] = {r.off, r.bytes};
                 else
                     arena.release(r.off, r.bytes);
-                busy[r.pool][r.stream] = 0;
+                busy[r.pool][r.stream] = mtgp::kStreamFree;
                 completed++;
                 bytes_done += r.bytes;
             }
@@ -215,31 +159,7 @@ void mtgp_server::loop() {
         if (fs && !pending.empty()) {
             const Clock::time_point ta = Clock::now();
             std::vector<Req> take;
-            // one pass: admitted requests move to `take`, requests of busy
-            // streams are compacted towards the front (their order kept)
-            auto w = pending.begin(), it = pending.begin();
-            // A stream whose requests are in a batch on the GPU waits; several
-            // requests of one stream may join the same batch (the plan runs
-            // them in order, jumping ahead where they are long), except that
-            // a long skip only opens a stream's part of a batch: the jump
-            // then starts from the stream's window by X^skip, a polynomial
-            // shared by many requests, instead of from an arbitrary position.
-            for (; it != pending.end() && (int)take.size() < max_batch; ++it) {
-                char &b = busy[it->pool][it->stream];
-                if (b == 2 && it->skip >= kJumpSkip) b = 3;  // next batch
-                if (b == 1 || b == 3) {
-                    if (w != it) *w = *it;
-                    ++w;
-                    continue;
-                }
-                uint64_t off = 0;
-                if (!arena.alloc(it->bytes, &off)) break;  // first come, first served
-                it->off = off;
-                busy[it->pool][it->stream] = 2;
-                take.push_back(*it);
-            }
-            pending.erase(w, it);
-            for (const Req &r : take) busy[r.pool][r.stream] = 1;
+            mtgp::admitBatch(pending, busy, arena, max_batch, kJumpSkip, &take);
             prof[0] += std::chrono::duration<double>(Clock::now() - ta).count();
             if (!take.empty()) {
                 lk.unlock();
@@ -252,7 +172,7 @@ void mtgp_server::loop() {
                         latency[r.ticket - 1] = 0;
                         status[r.ticket - 1] = rc;
                         arena.release(r.off, r.bytes);
-                        busy[r.pool][r.stream] = 0;
+                        busy[r.pool][r.stream] = mtgp::kStreamFree;
                         completed++;
                     }
                     cv_done.notify_all();
