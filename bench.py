@@ -64,6 +64,28 @@ def serve_trace(rng, n):
     return pool, stream.astype(np.uint32), kind, count.astype(np.uint64), skip.astype(np.uint64)
 
 
+def replica_seed(rank):
+    """Replicas are independent jobs: rank r seeds its substreams with
+    SEED + r, so no two ranks produce the same numbers."""
+    return SEED + rank
+
+
+def max_over_ranks(x, world, device="cuda"):
+    """The slowest rank's time (the job ends when its last rank does)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, bytes_per_rank, ms):
+    """Whole-job GB/s: every rank's output over the slowest rank's time."""
+    return world * bytes_per_rank / (ms * 1e-3) / 1e9
+
+
 def lengths(n=N_SUB, seed=42):
     rng = np.random.default_rng(seed)
     x = rng.lognormal(mean=np.log(2.0 ** 16), sigma=1.0, size=n)
@@ -373,7 +395,7 @@ def main():
     # --- substream setup (GPU jumps), timed separately ---
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    pool = Pool.substreams(p, SEED + rank, nsub, jump_table(32), stream=s)
+    pool = Pool.substreams(p, replica_seed(rank), nsub, jump_table(32), stream=s)
     torch.cuda.synchronize()
     jump_ms = (time.perf_counter() - t0) * 1e3
     start_windows = pool.windows()
@@ -417,12 +439,8 @@ def main():
         s.synchronize()
         torch.cuda.synchronize()
         barrier()
-    ms = max(ev0.elapsed_time(ev1) / max(args.steps, 1), 1e-6)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * total_bytes / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(max(ev0.elapsed_time(ev1) / max(args.steps, 1), 1e-6), world)
+    value = job_value(world, total_bytes, ms)
     # the persistent kernel (+ the staged-window copy of split plans) per
     # step; the work-counter reset is a memset, not a kernel
     launches = plan_cfg["kernels_per_launch"] * args.steps
@@ -434,14 +452,15 @@ def main():
     e2e_steps = 0 if args.only != "all" else max(3, min(args.steps, 10))
     host_out = torch.empty(total_bytes // 4, dtype=torch.int32, pin_memory=True)
     torch.cuda.synchronize()
+    barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         with torch.cuda.stream(s):
             pool.submit(items, out, s)
             host_out.copy_(out, non_blocking=True)
         s.synchronize()
-    e2e_s = (time.perf_counter() - t0) / max(e2e_steps, 1)
-    e2e = world * total_bytes / e2e_s / 1e9
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / max(e2e_steps, 1), world)
+    e2e = job_value(world, total_bytes, e2e_s * 1e3)
 
     # --- plain: one launch (one CTA) per substream ---
     plain_ms = None
