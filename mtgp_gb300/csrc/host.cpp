@@ -101,33 +101,6 @@ Tuning g_tune;
 // Seeding (host).  Same integer arithmetic as the reference.
 // ------------------------------------------------------------------------
 
-// mtgp32-fast.c:119-137
-void seed32(const mtgp32_params_fast_t &p, uint32_t seed, uint32_t *a) {
-    const int size = p.mexp / 32 + 1;
-    const uint32_t hidden = p.tbl[4] ^ (p.tbl[8] << 16);
-    uint32_t b = hidden;
-    b += b >> 16;
-    b += b >> 8;
-    std::fill(a, a + size, (b & 0xffu) * 0x01010101u);
-    a[0] = seed;
-    a[1] = hidden;
-    for (int i = 1; i < size; i++) a[i] ^= 1812433253u * (a[i - 1] ^ (a[i - 1] >> 30)) + (uint32_t)i;
-}
-
-// mtgp64-fast.c:124-142
-void seed64(const mtgp64_params_fast_t &p, uint64_t seed, uint64_t *a) {
-    const int size = p.mexp / 64 + 1;
-    const uint64_t hidden = p.tbl[4] ^ (p.tbl[8] << 16);
-    uint64_t b = hidden >> 32;
-    b += b >> 16;
-    b += b >> 8;
-    std::fill(a, a + size, (b & 0xffu) * 0x0101010101010101ULL);
-    a[0] = seed;
-    a[1] = hidden;
-    for (int i = 1; i < size; i++)
-        a[i] ^= 6364136223846793005ULL * (a[i - 1] ^ (a[i - 1] >> 62)) + (uint64_t)i;
-}
-
 // Key-schedule seeding shared by init_by_array and init_by_str
 // (mtgp32-fast.c:151-235 / 250-334, mtgp64-fast.c:156-239 / 255-339).
 // `keyAt(j)` returns key word j as the reference adds it: array words
@@ -202,7 +175,10 @@ struct T32 {
     }
     static int resident(int mexp, bool split) { return batchResident32(mexp, split); }
     static bool splits(int mexp) { return batchSplits32(mexp); }
-    static void seed(const HP &p, W s, W *a) { seed32(p, s, a); }
+    static cudaError_t seed(const DP *p, const int *pi, const W *seeds, W *st, int n, int size,
+                            int stride) {
+        return launchSeed32(p, pi, seeds, st, n, size, stride, nullptr);
+    }
     static void byArray(const HP &p, const W *key, int len, W *a) {
         keyed<W>(a, p.mexp / 32 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
                  [&](int j, int i) { return (W)(key[j] + (W)i); }, 1664525u, 1566083941u, 27);
@@ -234,7 +210,10 @@ struct T64 {
     }
     static int resident(int mexp, bool split) { return batchResident64(mexp, split); }
     static bool splits(int mexp) { return batchSplits64(mexp); }
-    static void seed(const HP &p, W s, W *a) { seed64(p, s, a); }
+    static cudaError_t seed(const DP *p, const int *pi, const W *seeds, W *st, int n, int size,
+                            int stride) {
+        return launchSeed64(p, pi, seeds, st, n, size, stride, nullptr);
+    }
     static void byArray(const HP &p, const W *key, int len, W *a) {
         keyed<W>(a, p.mexp / 64 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
                  [&](int j, int i) { return (W)(key[j] + (W)i); }, 2173292883993ULL,
@@ -353,10 +332,18 @@ struct Pool {
         return MTGP_OK;
     }
 
+    // Integer seeds, seeded on the device (mtgp32-fast.c:119-137).
     int seedAll(const W *seeds) {
-        std::vector<W> win((size_t)count * size);
-        for (int i = 0; i < count; i++) T::seed(hparams[hpidx[i]], seeds[i], &win[(size_t)i * size]);
-        return setWindows(win.data(), win.size());
+        W *d_seeds = nullptr;
+        CK(cudaMalloc(&d_seeds, sizeof(W) * count), "cudaMalloc(seeds)");
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e == cudaSuccess)
+            e = cudaMemcpy(d_seeds, seeds, sizeof(W) * count, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = T::seed(d_params, d_pidx, d_seeds, d_states, count, size, stride);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        cudaFree(d_seeds);
+        if (e != cudaSuccess) return cudaErr(e, "device seeding");
+        return MTGP_OK;
     }
 
     static int checkKind(int kind) {
@@ -999,6 +986,20 @@ int initSingle(Obj **out, const typename T::HP *para, const typename T::W *win) 
     return rc;
 }
 
+// A single generator from an integer seed, seeded on the device.
+template <class T, class Obj>
+int initSeeded(Obj **out, const typename T::HP *para, typename T::W seed) {
+    int rc = newObj(out);
+    if (rc) return rc;
+    rc = (*out)->pool.init(para, 1, nullptr, 1);
+    if (!rc) rc = (*out)->pool.seedAll(&seed);
+    if (rc) {
+        delete *out;
+        *out = nullptr;
+    }
+    return rc;
+}
+
 template <class T, class Obj>
 int importSingle(Obj *h, const typename T::Fast *src) {
     using W = typename T::W;
@@ -1041,9 +1042,7 @@ int mtgp32_gpu_init(mtgp32_gpu_t **out, const mtgp32_params_fast_t *para, uint32
     Shape sh;
     int rc = checkParams<T32>(*para, &sh);
     if (rc) return rc;
-    std::vector<uint32_t> w(sh.n);
-    T32::seed(*para, seed, w.data());
-    return initSingle<T32>(out, para, w.data());
+    return initSeeded<T32>(out, para, seed);
 }
 int mtgp32_gpu_init_by_array(mtgp32_gpu_t **out, const mtgp32_params_fast_t *para,
                              const uint32_t *array, int length) {
@@ -1115,9 +1114,7 @@ int mtgp64_gpu_init(mtgp64_gpu_t **out, const mtgp64_params_fast_t *para, uint64
     Shape sh;
     int rc = checkParams<T64>(*para, &sh);
     if (rc) return rc;
-    std::vector<uint64_t> w(sh.n);
-    T64::seed(*para, seed, w.data());
-    return initSingle<T64>(out, para, w.data());
+    return initSeeded<T64>(out, para, seed);
 }
 int mtgp64_gpu_init_by_array(mtgp64_gpu_t **out, const mtgp64_params_fast_t *para,
                              const uint64_t *array, int length) {

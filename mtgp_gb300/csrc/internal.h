@@ -70,6 +70,13 @@ void toDev(const mtgp64_params_fast_t &p, DevParams64 *d);
 // ngen generators, generator g uses params[pidx ? pidx[g] : g] (device
 // arrays), its window at states + g*stateStride(N), and writes n values of
 // `kind` at out + g*outStride elements.  kind < 0 = skip (no output).
+// Integer seeding of `count` windows (size words each, `stride` apart) on
+// the device: stream i from seeds[i] with parameter set pidx[i].
+cudaError_t launchSeed32(const DevParams32 *params, const int *pidx, const uint32_t *seeds,
+                         uint32_t *states, int count, int size, int stride, cudaStream_t s);
+cudaError_t launchSeed64(const DevParams64 *params, const int *pidx, const uint64_t *seeds,
+                         uint64_t *states, int count, int size, int stride, cudaStream_t s);
+
 cudaError_t launchGen32(int mexp, int kind, const DevParams32 *params,
                         const int *pidx, uint32_t *states, int ngen,
                         void *out, uint64_t n, uint64_t outStride,
