@@ -366,8 +366,9 @@ int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
  * counterpart; the autotuner and tests use them):
  *   "split_chunk"  0 = automatic, < 0 = never split, > 0 = chunk length
  *   "batch_grid"   0 = one CTA per resident slot, > 0 = that many CTAs
- *   "core"         32-bit generation core for plans without split requests:
- *                  4 = four adjacent words per thread (default), 1 = one */
+ *   "core"         32-bit generation core: 4 = four adjacent words per
+ *                  thread (default), 1 = one word per thread; plans whose
+ *                  items mix output kinds use the one-word core */
 int mtgp_gpu_set_tuning(const char *key, int64_t value);
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
 

@@ -59,8 +59,9 @@ cudaError_t launchBatch32(const BatchLaunch &b, const DevParams32 *params, uint3
                           cudaStream_t s);
 cudaError_t launchBatch64(const BatchLaunch &b, const DevParams64 *params, uint64_t *states,
                           cudaStream_t s);
-// Number of CTAs of the batched kernel resident at once on the device.
-int batchResident32(int mexp, bool split);
+// Number of CTAs of the batched kernel resident at once on the device
+// (32-bit: for the given generation core, 1 or 4).
+int batchResident32(int mexp, bool split, int core);
 int batchResident64(int mexp, bool split);
 // Whether split requests are supported for this exponent.
 bool batchSplits32(int mexp);

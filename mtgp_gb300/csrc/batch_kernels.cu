@@ -71,17 +71,48 @@ __device__ __forceinline__ void jump_task(typename Tr::W *buf, const typename Tr
         nwords);
 }
 
+// The one-word kernels with mixed output kinds (MODE == -2) keep their
+// generation buffer in dynamic shared memory and call each kind's loop out
+// of line, addressing the buffer by this symbol (so the accesses stay
+// shared-memory instructions).  Inlined together, the six loops' registers
+// add up (63 instead of 32) and the resident CTAs halve.
+extern __shared__ __align__(16) uint32_t g_mix32[];
+extern __shared__ __align__(16) uint64_t g_mix64[];
+
+// Resident CTAs that fix a mixed kernel's register budget: as many as its
+// shared memory allows, at most `blocks`.
+constexpr int mixBlocks(int blocks, size_t smem) {
+    const int by_smem = (int)(204800 / smem) > 0 ? (int)(204800 / smem) : 1;
+    return blocks < by_smem ? blocks : by_smem;
+}
+
+template <int N, int TN, int B, int KIND>
+__device__ __noinline__ void mix32(Lane32 L, uint64_t n, char *o) {
+    using OT = typename Out32<(KIND < 0 ? 0 : KIND)>::T;
+    run32<N, TN, B, KIND>(g_mix32, L, L.otab(KIND < 0 ? 0 : KIND), n, (OT *)o);
+}
+
+template <int N, int TN, int B, int KIND>
+__device__ __noinline__ void mix64(Lane64 L, uint64_t n, char *o) {
+    using OT = typename Out64<(KIND < 0 ? 0 : KIND)>::T;
+    run64<N, TN, B, KIND>(g_mix64, L, L.otab_lo(KIND < 0 ? 0 : KIND),
+                          L.otab_hi(KIND < 0 ? 0 : KIND), n, (OT *)o);
+}
+
 // MODE >= -1: every item has output kind MODE (-1 = skip); MODE == -2:
-// items of any kind (the kind is switched per item).  SPLIT: tasks may
-// start with a jump.
+// items of any kind (the kind is switched per item; dynamic shared memory of
+// B words).  SPLIT: tasks may start with a jump.
 template <int N, int TN, int B, int MODE, bool SPLIT>
-__global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1280 : 2048) / TN)
+__global__ void __launch_bounds__(TN, MODE == -2
+                                         ? mixBlocks((SPLIT ? 1280 : 2048) / TN, sizeof(uint32_t) * B)
+                                         : (SPLIT ? 1280 : 2048) / TN)
 k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
           unsigned *__restrict__ counter, uint32_t *__restrict__ stage,
           const uint32_t *__restrict__ polys, int nwords) {
-    __shared__ __align__(16) uint32_t buf[B];
+    __shared__ __align__(16) uint32_t sbuf[MODE == -2 ? 4 : B];
+    uint32_t *const buf = MODE == -2 ? g_mix32 : sbuf;
     __shared__ int s_task;
     for (;;) {
         if (threadIdx.x == 0) s_task = (int)atomicAdd(counter, 1u);
@@ -110,12 +141,12 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
                 run32<N, TN, B, MODE>(buf, L, L.otab(MODE < 0 ? 0 : MODE), I.count, (OT *)o);
             } else {
                 switch (I.kind) {
-                case 0: run32<N, TN, B, 0>(buf, L, L.tmp, I.count, (uint32_t *)o); break;
-                case 1: run32<N, TN, B, 1>(buf, L, L.flt, I.count, (float *)o); break;
-                case 2: run32<N, TN, B, 2>(buf, L, L.flt, I.count, (float *)o); break;
-                case 3: run32<N, TN, B, 3>(buf, L, L.flt, I.count, (float *)o); break;
-                case 4: run32<N, TN, B, 4>(buf, L, L.flt, I.count, (float *)o); break;
-                default: run32<N, TN, B, -1>(buf, L, L.tmp, I.count, nullptr); break;
+                case 0: mix32<N, TN, B, 0>(L, I.count, o); break;
+                case 1: mix32<N, TN, B, 1>(L, I.count, o); break;
+                case 2: mix32<N, TN, B, 2>(L, I.count, o); break;
+                case 3: mix32<N, TN, B, 3>(L, I.count, o); break;
+                case 4: mix32<N, TN, B, 4>(L, I.count, o); break;
+                default: mix32<N, TN, B, -1>(L, I.count, nullptr); break;
                 }
             }
         }
@@ -205,13 +236,16 @@ k_batch32x4(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
 }
 
 template <int N, int TN, int B, int MODE, bool SPLIT>
-__global__ void __launch_bounds__(TN, MODE == -2 ? 1 : (SPLIT ? 1280 : 2048) / TN)
+__global__ void __launch_bounds__(TN, MODE == -2
+                                         ? mixBlocks((SPLIT ? 1280 : 2048) / TN, sizeof(uint64_t) * B)
+                                         : (SPLIT ? 1280 : 2048) / TN)
 k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
           unsigned *__restrict__ counter, uint64_t *__restrict__ stage,
           const uint32_t *__restrict__ polys, int nwords) {
-    __shared__ __align__(16) uint64_t buf[B];
+    __shared__ __align__(16) uint64_t sbuf[MODE == -2 ? 4 : B];
+    uint64_t *const buf = MODE == -2 ? g_mix64 : sbuf;
     __shared__ int s_task;
     for (;;) {
         if (threadIdx.x == 0) s_task = (int)atomicAdd(counter, 1u);
@@ -241,12 +275,12 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
                                       L.otab_hi(MODE < 0 ? 0 : MODE), I.count, (OT *)o);
             } else {
                 switch (I.kind) {
-                case 0: run64<N, TN, B, 0>(buf, L, L.tmp_lo, L.tmp_hi, I.count, (uint64_t *)o); break;
-                case 1: run64<N, TN, B, 1>(buf, L, L.dbl_lo, L.dbl_hi, I.count, (double *)o); break;
-                case 2: run64<N, TN, B, 2>(buf, L, L.dbl_lo, L.dbl_hi, I.count, (double *)o); break;
-                case 3: run64<N, TN, B, 3>(buf, L, L.dbl_lo, L.dbl_hi, I.count, (double *)o); break;
-                case 4: run64<N, TN, B, 4>(buf, L, L.dbl_lo, L.dbl_hi, I.count, (double *)o); break;
-                default: run64<N, TN, B, -1>(buf, L, L.tmp_lo, L.tmp_hi, I.count, nullptr); break;
+                case 0: mix64<N, TN, B, 0>(L, I.count, o); break;
+                case 1: mix64<N, TN, B, 1>(L, I.count, o); break;
+                case 2: mix64<N, TN, B, 2>(L, I.count, o); break;
+                case 3: mix64<N, TN, B, 3>(L, I.count, o); break;
+                case 4: mix64<N, TN, B, 4>(L, I.count, o); break;
+                default: mix64<N, TN, B, -1>(L, I.count, nullptr); break;
                 }
             }
         }
@@ -269,7 +303,7 @@ __global__ void k_unstage(W *__restrict__ states, const W *__restrict__ stage,
 // Resident CTAs of a kernel on the current device (cached per kernel and
 // device: the occupancy query is not free and servers launch often).
 template <class K>
-static cudaError_t resident(K kern, int tn, int *grid) {
+static cudaError_t resident(K kern, int tn, int *grid, size_t smem = 0) {
     struct Entry {
         const void *fn;
         int dev, tn, grid;
@@ -289,7 +323,7 @@ static cudaError_t resident(K kern, int tn, int *grid) {
             }
     }
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, tn, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, tn, smem);
     if (e != cudaSuccess) return e;
     *grid = sms * (per > 0 ? per : 1);
     std::lock_guard<std::mutex> lk(mu);
@@ -300,16 +334,16 @@ static cudaError_t resident(K kern, int tn, int *grid) {
 // work counter reset -> persistent kernel
 template <typename W, class K, class P>
 static cudaError_t go(K kern, int tn, const BatchLaunch &b, const P *params, W *states,
-                      cudaStream_t s) {
+                      cudaStream_t s, size_t smem = 0) {
     int grid = b.grid;
     if (grid <= 0) {
-        cudaError_t e = resident(kern, tn, &grid);
+        cudaError_t e = resident(kern, tn, &grid, smem);
         if (e != cudaSuccess) return e;
     }
     if (grid > b.ntasks) grid = b.ntasks;
     cudaError_t e = cudaMemsetAsync(b.counter, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
-    kern<<<grid, tn, 0, s>>>(params, states, b.tasks, b.ntasks, b.items,
+    kern<<<grid, tn, smem, s>>>(params, states, b.tasks, b.ntasks, b.items,
                              static_cast<char *>(b.out), b.counter, static_cast<W *>(b.stage),
                              b.polys, b.nwords);
     return cudaGetLastError();
@@ -325,7 +359,9 @@ static cudaError_t mode32(const BatchLaunch &b, const DevParams32 *p, uint32_t *
     case 2: return go<uint32_t>(k_batch32<N, TN, B, 2, SPLIT>, TN, b, p, st, s);
     case 3: return go<uint32_t>(k_batch32<N, TN, B, 3, SPLIT>, TN, b, p, st, s);
     case 4: return go<uint32_t>(k_batch32<N, TN, B, 4, SPLIT>, TN, b, p, st, s);
-    default: return go<uint32_t>(k_batch32<N, TN, B, -2, SPLIT>, TN, b, p, st, s);
+    default:
+        return go<uint32_t>(k_batch32<N, TN, B, -2, SPLIT>, TN, b, p, st, s,
+                            sizeof(uint32_t) * B);
     }
 }
 
@@ -354,7 +390,9 @@ static cudaError_t mode64(const BatchLaunch &b, const DevParams64 *p, uint64_t *
     case 2: return go<uint64_t>(k_batch64<N, TN, B, 2, SPLIT>, TN, b, p, st, s);
     case 3: return go<uint64_t>(k_batch64<N, TN, B, 3, SPLIT>, TN, b, p, st, s);
     case 4: return go<uint64_t>(k_batch64<N, TN, B, 4, SPLIT>, TN, b, p, st, s);
-    default: return go<uint64_t>(k_batch64<N, TN, B, -2, SPLIT>, TN, b, p, st, s);
+    default:
+        return go<uint64_t>(k_batch64<N, TN, B, -2, SPLIT>, TN, b, p, st, s,
+                            sizeof(uint64_t) * B);
     }
 }
 
@@ -421,12 +459,12 @@ bool batchSplits32(int mexp) { return mexp == 11213 || mexp == 23209; }
 bool batchSplits64(int mexp) { return mexp == 11213 || mexp == 23209; }
 
 // Resident CTAs of the kernel a plan with (or without) split requests uses
-// under the current generation core.
+// with the given generation core.
 template <int N, int T, int B>
-static int resident32(bool split) {
+static int resident32(bool split, int core) {
     int g = 0;
     const bool jumps = split && kSplit32<N>;
-    if (genCore32() == 4) {
+    if (core == 4) {
         constexpr int W = kW4<N, T>;
         if (jumps) resident(k_batch32x4<N, W, B, 0, kSplit32<N>>, W / 4, &g);
         else resident(k_batch32x4<N, W, B, 0, false>, W / 4, &g);
@@ -437,9 +475,9 @@ static int resident32(bool split) {
     return g;
 }
 
-int batchResident32(int mexp, bool split) {
+int batchResident32(int mexp, bool split, int core) {
 #define X(M, N, T, B) \
-    if (mexp == M) return resident32<N, T, B>(split);
+    if (mexp == M) return resident32<N, T, B>(split, core);
     MTGP_SHAPES32(X)
 #undef X
     return 0;

@@ -173,7 +173,9 @@ struct T32 {
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch32(b, p, st, s);
     }
-    static int resident(int mexp, bool split) { return batchResident32(mexp, split); }
+    static int resident(int mexp, bool split, int core) {
+        return batchResident32(mexp, split, core);
+    }
     static bool splits(int mexp) { return batchSplits32(mexp); }
     static cudaError_t seed(const DP *p, const int *pi, const W *seeds, W *st, int n, int size,
                             int stride) {
@@ -208,7 +210,7 @@ struct T64 {
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch64(b, p, st, s);
     }
-    static int resident(int mexp, bool split) { return batchResident64(mexp, split); }
+    static int resident(int mexp, bool split, int) { return batchResident64(mexp, split); }
     static bool splits(int mexp) { return batchSplits64(mexp); }
     static cudaError_t seed(const DP *p, const int *pi, const W *seeds, W *st, int n, int size,
                             int stride) {
@@ -656,7 +658,25 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     o.jump_min = kJumpMinSkip;
     o.max_gen_skip = kMaxGenSkip;
     o.chunk_tune = g_tune.split_chunk;
-    o.resident = o.can_jump ? T::resident(P.sh.mexp, true) : 1;  // depends on the core
+    // Plans whose generated values mix kinds (a generated skip counts as
+    // kind -1) run on the one-word core, whose per-kind loops are out of line
+    // at no cost.  The same rule as planCore's mode, decided up front because
+    // the chunk length depends on the core's resident CTAs.
+    int kinds = -3;
+    auto addKind = [&kinds](int k) { kinds = (kinds == -3 || kinds == k) ? k : -2; };
+    auto jumped = [&o](uint64_t v) { return o.can_jump && v >= o.jump_min; };
+    for (int k = 0; k < nitems && items; k++) {
+        const mtgp_work_item_t &it = items[k];
+        if (it.kind < 0) {
+            const uint64_t adv = it.skip + it.count;
+            if (adv && !jumped(adv)) addKind(-1);
+        } else {
+            if (it.skip && !jumped(it.skip)) addKind(-1);
+            if (it.count) addKind(it.kind);
+        }
+    }
+    const int core = (T::kBits == 32 && kinds == -2) ? 1 : genCore32();
+    o.resident = o.can_jump ? T::resident(P.sh.mexp, true, core) : 1;
     PlanResult &R = P.plan_scratch;
     std::string msg;
     int rc = planCore(items, nitems, o, &R, &msg);
@@ -733,7 +753,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->out_bytes = out_bytes;
     pl->grid = (int)g_tune.batch_grid;
     pl->split = split;
-    pl->core = genCore32();
+    pl->core = pl->mode == -2 ? 1 : core;
     pl->chunk = cut ? chunk : 0;
     pl->nstage = (int)stage_streams.size();
     auto align = [](size_t n) { return (n + 255) & ~size_t(255); };
@@ -902,7 +922,7 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
                 // three quarters or half of the resident CTAs: fewer CTAs
                 // share an SM's data pipe, so each runs its tasks faster,
                 // which pays when the longest tasks set the launch's length
-                const int full = T::resident(P.sh.mexp, pl->split);
+                const int full = T::resident(P.sh.mexp, pl->split, pl->core);
                 pl->grid = std::max(1, g == 1 ? full * 3 / 4 : full / 2);
             }
             float ms = 0;

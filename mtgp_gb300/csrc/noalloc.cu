@@ -160,7 +160,7 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
     b.mexp = sh.mexp;
     b.mode = mode == -3 ? -1 : mode;
     b.grid = 0;
-    b.core = genCore32();
+    b.core = b.mode == -2 ? 1 : genCore32();  // mixed kinds: the one-word core
     b.split = false;
     b.nwords = 0;
     b.polys = nullptr;
