@@ -126,7 +126,7 @@ typedef struct mtgp32_gpu mtgp32_gpu_t;
 typedef struct mtgp64_gpu mtgp64_gpu_t;
 
 /* Replaces mtgp32_init (mtgp32-fast.c:94-104) + mtgp32_init_state (:119-137).
- * Allocates the device-resident state; the seeding is done on the host with
+ * Allocates the device-resident state and seeds it on the device with
  * the reference's exact arithmetic. */
 int mtgp32_gpu_init(mtgp32_gpu_t **out, const mtgp32_params_fast_t *para,
                     uint32_t seed);
@@ -156,7 +156,12 @@ int mtgp32_gpu_fill_open_close(mtgp32_gpu_t *h, float *dev_out, size_t n,
 /* n successive mtgp32_genrand_open_open (mtgp32-fast.h:330-346). */
 int mtgp32_gpu_fill_open_open(mtgp32_gpu_t *h, float *dev_out, size_t n,
                               void *stream);
-/* Generic form of the five fills above; kind is an MTGP_KIND_* value. */
+/* Generic form of the five fills above; kind is an MTGP_KIND_* value.
+ * Fills of 2^20 values or more (MEXP 11213 and 23209) are split into chunks
+ * that start with a GF(2) jump and run on many CTAs; such a fill may first
+ * wait for the split fill issued two calls earlier on the same handle, and
+ * the first one of a parameter set computes its jump tables (tens of ms).
+ * Fills issued during stream capture always run on one CTA. */
 int mtgp32_gpu_fill(mtgp32_gpu_t *h, int kind, void *dev_out, size_t n,
                     void *stream);
 /* Advance the state by n steps without writing output. */

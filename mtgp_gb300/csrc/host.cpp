@@ -601,8 +601,22 @@ struct Pool {
 // ==========================================================================
 // Public structs
 // ==========================================================================
-struct mtgp32_gpu { Pool<T32> pool; };
-struct mtgp64_gpu { Pool<T64> pool; };
+// Large fills of a single generator run as split plans (see fillSingle);
+// two plans are used in turn, so a fill never refills a plan whose previous
+// launch the GPU may still be reading.
+struct SingleFill {
+    mtgp_gpu_plan *plan[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    int next = 0;
+};
+struct mtgp32_gpu {
+    Pool<T32> pool;
+    SingleFill fill;
+};
+struct mtgp64_gpu {
+    Pool<T64> pool;
+    SingleFill fill;
+};
 struct mtgp32_gpu_pool { Pool<T32> pool; };
 struct mtgp64_gpu_pool { Pool<T64> pool; };
 
@@ -647,7 +661,8 @@ struct mtgp_gpu_plan {
 namespace {
 
 template <class T>
-int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_plan **out) {
+int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_plan **out,
+             int force_core = 0, int64_t force_chunk = 0) {
     using W = typename T::W;
     if (!out) return setErr(MTGP_ERR_INVALID, "null plan pointer");
     if (*out && (*out)->pool != &P) return setErr(MTGP_ERR_INVALID, "plan belongs to another pool");
@@ -657,7 +672,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     o.can_jump = T::splits(P.sh.mexp);
     o.jump_min = kJumpMinSkip;
     o.max_gen_skip = kMaxGenSkip;
-    o.chunk_tune = g_tune.split_chunk;
+    o.chunk_tune = force_chunk ? force_chunk : g_tune.split_chunk;
     // Plans whose generated values mix kinds (a generated skip counts as
     // kind -1) run on the one-word core, whose per-kind loops are out of line
     // at no cost.  The same rule as planCore's mode, decided up front because
@@ -675,7 +690,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (it.count) addKind(it.kind);
         }
     }
-    const int core = (T::kBits == 32 && kinds == -2) ? 1 : genCore32();
+    const int core = force_core ? force_core : (T::kBits == 32 && kinds == -2) ? 1 : genCore32();
     o.resident = o.can_jump ? T::resident(P.sh.mexp, true, core) : 1;
     PlanResult &R = P.plan_scratch;
     std::string msg;
@@ -843,8 +858,69 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     return MTGP_OK;
 }
 
+// n successive values of one generator.  A fill of at least kSplitFillMin
+// values, on an exponent with the in-kernel jump, runs as a split plan: chunks
+// of the request start from the window jumped by X^(c*chunk) and run on many
+// CTAs at once (one CTA alone generates about 2.6 G values/s), on the
+// one-word core, whose CTAs run a single task fastest.  Smaller fills, and
+// fills issued while the stream is being captured, run on one CTA.  The first
+// split fill of a parameter set also computes its characteristic polynomial
+// and jump polynomials (tens of milliseconds, and a device synchronisation).
+constexpr size_t kSplitFillMin = size_t(1) << 20;
+
+template <class T, class Obj>
+int fillSingle(Obj *h, int kind, void *out, size_t n, void *s);
+
 int planLaunch(mtgp_gpu_plan *pl, void *out, void *s) {
     return pl->bits == 32 ? launchPlan<T32>(pl, out, s) : launchPlan<T64>(pl, out, s);
+}
+
+template <class T, class Obj>
+int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
+    Pool<T> &P = h->pool;
+    if (n < kSplitFillMin || !T::splits(P.sh.mexp)) return P.fillAll(kind, out, n, s);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(S(s), &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        return P.fillAll(kind, out, n, s);
+    int rc = P.checkKind(kind);
+    if (!rc) rc = P.checkOut(out, n);
+    if (rc) return rc;
+    SingleFill &F = h->fill;
+    const int i = F.next;
+    if (F.done[i])
+        CK(cudaEventSynchronize(F.done[i]), "wait for an earlier fill");
+    else
+        CK(cudaEventCreateWithFlags(&F.done[i], cudaEventDisableTiming), "cudaEventCreate");
+    mtgp_work_item_t it{};
+    it.stream = 0;
+    it.kind = kind;
+    it.count = n;
+    // about two chunks per SM: more chunks make the in-CTA jumps (tens of
+    // microseconds of integer work each) the larger cost
+    int64_t chunk = g_tune.split_chunk;
+    if (chunk == 0) {
+        int dev = 0, sms = 152;
+        if (cudaGetDevice(&dev) == cudaSuccess)
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        chunk = 1 << 17;
+        while ((uint64_t)chunk * 2 * (uint64_t)sms < n) chunk <<= 1;
+    }
+    rc = makePlan(P, &it, 1, &F.plan[i], 1, chunk);
+    if (!rc) rc = launchPlan<T>(F.plan[i], out, s);
+    if (rc) return rc;
+    CK(cudaEventRecord(F.done[i], S(s)), "record fill");
+    F.next ^= 1;
+    return MTGP_OK;
+}
+
+template <class Obj>
+void freeSingle(Obj *h) {
+    cudaDeviceSynchronize();
+    for (int i = 0; i < 2; i++) {
+        delete h->fill.plan[i];
+        if (h->fill.done[i]) cudaEventDestroy(h->fill.done[i]);
+    }
+    delete h;
 }
 
 // Autotuner: build one plan per candidate configuration, time each on the
@@ -1086,12 +1162,11 @@ int mtgp32_gpu_init_by_str(mtgp32_gpu_t **out, const mtgp32_params_fast_t *para,
 }
 void mtgp32_gpu_free(mtgp32_gpu_t *h) {
     if (!h) return;
-    cudaDeviceSynchronize();
-    delete h;
+    freeSingle(h);
 }
 int mtgp32_gpu_fill(mtgp32_gpu_t *h, int kind, void *out, size_t n, void *s) {
     if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
-    return h->pool.fillAll(kind, out, n, s);
+    return fillSingle<T32>(h, kind, out, n, s);
 }
 int mtgp32_gpu_fill_uint32(mtgp32_gpu_t *h, uint32_t *o, size_t n, void *s) { return mtgp32_gpu_fill(h, 0, o, n, s); }
 int mtgp32_gpu_fill_close1_open2(mtgp32_gpu_t *h, float *o, size_t n, void *s) { return mtgp32_gpu_fill(h, 1, o, n, s); }
@@ -1158,12 +1233,11 @@ int mtgp64_gpu_init_by_str(mtgp64_gpu_t **out, const mtgp64_params_fast_t *para,
 }
 void mtgp64_gpu_free(mtgp64_gpu_t *h) {
     if (!h) return;
-    cudaDeviceSynchronize();
-    delete h;
+    freeSingle(h);
 }
 int mtgp64_gpu_fill(mtgp64_gpu_t *h, int kind, void *out, size_t n, void *s) {
     if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
-    return h->pool.fillAll(kind, out, n, s);
+    return fillSingle<T64>(h, kind, out, n, s);
 }
 int mtgp64_gpu_fill_uint64(mtgp64_gpu_t *h, uint64_t *o, size_t n, void *s) { return mtgp64_gpu_fill(h, 0, o, n, s); }
 int mtgp64_gpu_fill_close1_open2(mtgp64_gpu_t *h, double *o, size_t n, void *s) { return mtgp64_gpu_fill(h, 1, o, n, s); }
