@@ -187,9 +187,14 @@ int planCore(const mtgp_work_item_t *items, int nitems, const PlanOptions &o, Pl
         if (m > 1) r->stage_streams.push_back(runs[r0].stream);
     }
     r->chunk = cut ? chunk : 0;
-    // longest task first
+    // longest task first, a jump counted as jump_min generated values (about
+    // its cost)
+    const uint64_t jw = o.can_jump ? o.jump_min : 0;
+    auto cost = [jw](const PlanTask &t) {
+        return t.total + jw * ((t.run ? 1u : 0u) + (t.off ? 1u : 0u));
+    };
     std::stable_sort(r->tasks.begin(), r->tasks.end(),
-                     [](const PlanTask &a, const PlanTask &b) { return a.total > b.total; });
+                     [&cost](const PlanTask &a, const PlanTask &b) { return cost(a) > cost(b); });
     int mode = -3;
     for (const PlanSeg &g : r->segs)
         if (g.count) mode = (mode == -3 || mode == g.kind) ? g.kind : -2;

@@ -18,7 +18,8 @@
 //     parallel.  A stream with one task writes its window back directly; with
 //     several, the last one (in stream order) writes to a staging slot that is
 //     copied back after the launch, the others write nothing.
-//   - Tasks are ordered longest first.
+//   - Tasks are ordered longest first, a start jump counting as `jump_min`
+//     values (about its cost).
 // The kernel-side jump of a task is X^run then X^off (either may be 0).
 #pragma once
 #include <cstddef>

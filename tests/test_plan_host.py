@@ -3,7 +3,7 @@ for random item lists, the tasks it produces step every stream through
 exactly the positions the items ask for, write every requested value once
 at its offset, generate no long skip when jumps are available, cut long runs
 at the chunk length, write each stream's final window back exactly once, and
-come longest first; malformed items are rejected."""
+come longest first (a jump counting as 2^17 values); malformed items are rejected."""
 import ctypes
 import os
 import subprocess
@@ -101,8 +101,9 @@ def check(items, res, nstreams, esz, can_jump, chunk_tune):
         else:
             assert wb >= 0 and stage[wb] == s
     assert sorted(stage.tolist()) == sorted(set(stage.tolist()))
-    totals = tasks[:, 4]
-    assert np.all(totals[:-1] >= totals[1:]), "not longest first"
+    jumps = (tasks[:, 2] > 0).astype(np.int64) + (tasks[:, 3] > 0).astype(np.int64)
+    cost = tasks[:, 4] + (JUMP_MIN * jumps if can_jump else 0)
+    assert np.all(cost[:-1] >= cost[1:]), "not longest first"
     assert not can_jump or chunk_tune >= 0 or chunk == 0
     if chunk_tune > 0 and chunk:
         assert chunk == chunk_tune
