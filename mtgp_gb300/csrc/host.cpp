@@ -467,12 +467,33 @@ struct Pool {
 
     int polyWords() const { return sh.mexp / 32 + 1; }
 
+    // chi_k's reduction tables (2.9 MB for MEXP 11213).  At most kMaxModuli
+    // are kept per pool; the least recently used is dropped (and rebuilt in
+    // about 2 ms if needed again), so pools with many parameter sets stay
+    // small.  A pointer handed out stays valid until the next call for
+    // another parameter set.
+    static constexpr int kMaxModuli = 16;
+    std::vector<uint64_t> mod_used;
+    uint64_t mod_clock = 0;
     int modulus(int k, const gf2::Modulus **out) {
         int rc = characteristic(k);
         if (rc) return rc;
-        if (mod.size() < hparams.size()) mod.resize(hparams.size());
-        if (!mod[k]) mod[k].reset(new (std::nothrow) gf2::Modulus(chi[k], chideg[k]));
+        if (mod.size() < hparams.size()) {
+            mod.resize(hparams.size());
+            mod_used.resize(hparams.size(), 0);
+        }
+        if (!mod[k]) {
+            int live = 0, lru = -1;
+            for (size_t j = 0; j < mod.size(); j++)
+                if (mod[j]) {
+                    live++;
+                    if (lru < 0 || mod_used[j] < mod_used[(size_t)lru]) lru = (int)j;
+                }
+            if (live >= kMaxModuli) mod[(size_t)lru].reset();
+            mod[k].reset(new (std::nothrow) gf2::Modulus(chi[k], chideg[k]));
+        }
         if (!mod[k]) return setErr(MTGP_ERR_ALLOC, "jump tables");
+        mod_used[k] = ++mod_clock;
         *out = mod[k].get();
         return MTGP_OK;
     }

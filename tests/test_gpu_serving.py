@@ -279,3 +279,31 @@ def test_server_zero_copy_result_and_budget_admission(gpu, orc):
     with pytest.raises(MTGPError):
         srv.release(t2)
     srv.close()
+
+
+def test_jumps_across_many_parameter_sets(gpu, orc):
+    """Twenty parameter sets that all need in-kernel jumps (more than the
+    pool keeps reduction tables for at once, so some are dropped and
+    rebuilt): every split request and skip is still bit-exact."""
+    from mtgp_gb300.api import Pool, set_tuning, work_items
+    tbl = load_table("mtgp32_fast_11213")
+    n = 20
+    plist = [tbl[i] for i in range(n)]
+    seeds = np.arange(n) + 900
+    pool = Pool.create(plist, seeds, np.arange(n))
+    counts = np.full(n, 5000)
+    skips = np.where(np.arange(n) % 3 == 0, 1 << 17, 0)
+    offs = np.arange(n) * 5000 * 4
+    set_tuning("split_chunk", 1200)
+    try:
+        for rep in range(2):
+            out = torch.zeros(n * 5000, dtype=torch.int32, device="cuda")
+            pool.submit(work_items(np.arange(n), np.zeros(n), counts, offs, skips), out)
+            torch.cuda.synchronize()
+            got = out.cpu().numpy().view(np.uint32)
+            for k in range(n):
+                o = orc.gen(plist[k], seed=int(seeds[k]))
+                o.skip(int(skips[k]) * (rep + 1) + 5000 * rep)
+                assert np.array_equal(got[k * 5000:(k + 1) * 5000], o.fill(0, 5000)), (rep, k)
+    finally:
+        set_tuning("split_chunk", 0)
