@@ -953,7 +953,7 @@ void freeSingle(Obj *h) {
 // CTAs with 128-bit stores, or one word per thread in 256-thread CTAs with
 // 32-bit stores), split-chunk length for long requests (none, or 2^17 to
 // 2^20 in steps of 2^17, with either core), and grid size (all resident
-// CTAs, three quarters or half of them).
+// CTAs, or 7/8, 3/4, 5/8, 1/2 of them).
 template <class T>
 int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, void *s,
              int reps, mtgp_gpu_plan **best, char *report, int cap) {
@@ -1004,7 +1004,8 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
         return MTGP_OK;
     };
     for (size_t k = 0; k < cands.size() && !rc; k++) {
-        for (int g = 0; g < 3 && !rc; g++) {
+        static const int kGridEighths[] = {8, 7, 6, 5, 4};  // of the resident CTAs
+        for (int g = 0; g < 5 && !rc; g++) {
             g_tune.split_chunk = cands[k].chunk;
             g_tune.batch_grid = 0;
             setGenCore32(cands[k].core);
@@ -1016,11 +1017,11 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
                 break;
             }
             if (g > 0) {
-                // three quarters or half of the resident CTAs: fewer CTAs
-                // share an SM's data pipe, so each runs its tasks faster,
-                // which pays when the longest tasks set the launch's length
+                // fewer CTAs than resident: fewer share an SM's data pipe,
+                // so each runs its tasks faster, which pays when the longest
+                // tasks set the launch's length
                 const int full = T::resident(P.sh.mexp, pl->split, pl->core);
-                pl->grid = std::max(1, g == 1 ? full * 3 / 4 : full / 2);
+                pl->grid = std::max(1, full * kGridEighths[g] / 8);
             }
             float ms = 0;
             rc = timeOne(pl, &ms);
@@ -1031,7 +1032,8 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
             char line[160];
             std::snprintf(line, sizeof line, "core=%d chunk=%lld grid=%s tasks=%d: %.4f ms\n",
                           T::kBits == 64 ? 1 : pl->core, (long long)pl->chunk,
-                          g == 0 ? "all" : g == 1 ? "3/4" : "1/2", pl->ntasks, ms);
+                          g == 0 ? "all" : g == 1 ? "7/8" : g == 2 ? "3/4" : g == 3 ? "5/8" : "1/2",
+                          pl->ntasks, ms);
             rep += line;
             if (!*best || ms < best_ms) {
                 delete *best;
