@@ -452,7 +452,8 @@ int mtgp_server_release(mtgp_server_t *s, uint64_t ticket);
  * MTGP_ERR_BUSY.  Fails with MTGP_ERR_INVALID once it is admitted. */
 int mtgp_server_cancel(mtgp_server_t *s, uint64_t ticket);
 /* Wait until a request is done (its destination holds the result);
- * `status` receives MTGP_OK or the error it ended with. */
+ * `status` receives MTGP_OK or the error it ended with (a request whose batch
+ * failed may still have advanced its stream). */
 int mtgp_server_wait(mtgp_server_t *s, uint64_t ticket, double timeout_s,
                      int *status);
 /* Wait until every submitted request is done. */

@@ -824,7 +824,14 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         }
     }
     if (e != cudaSuccess) {
-        if (fresh) delete pl;
+        if (fresh) {
+            delete pl;
+        } else {  // a refilled plan that could not grow launches nothing
+            pl->ntasks = 0;
+            pl->nstage = 0;
+            pl->out_bytes = 0;
+            pl->dirty = false;
+        }
         return cudaErr(e, "plan buffers");
     }
     unsigned char *h = pl->h_blob;

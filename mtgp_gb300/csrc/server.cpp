@@ -83,9 +83,18 @@ struct mtgp_server {
 
     void loop();
     int launch(Slot &sl, std::vector<Req> &reqs);
+    int launchBatch(Slot &sl, std::vector<Req> &reqs);
 };
 
 int mtgp_server::launch(Slot &sl, std::vector<Req> &reqs) {
+    const int rc = launchBatch(sl, reqs);
+    // work already queued for this batch must end before its arena space is
+    // handed to another batch
+    if (rc) cudaStreamSynchronize(sl.cs);
+    return rc;
+}
+
+int mtgp_server::launchBatch(Slot &sl, std::vector<Req> &reqs) {
     std::vector<mtgp_work_item_t> items[2];
     for (const Req &r : reqs) {
         mtgp_work_item_t it{};
