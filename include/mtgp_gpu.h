@@ -164,7 +164,9 @@ int mtgp32_gpu_fill_open_open(mtgp32_gpu_t *h, float *dev_out, size_t n,
  * Fills issued during stream capture always run on one CTA. */
 int mtgp32_gpu_fill(mtgp32_gpu_t *h, int kind, void *dev_out, size_t n,
                     void *stream);
-/* Advance the state by n steps without writing output. */
+/* Advance the state by n steps without writing output.  From 2^22 steps on
+ * this is a GF(2) jump (X^n mod chi), not n generated steps; the state then
+ * matches stepping except in the bits of word 0 that never reach an output. */
 int mtgp32_gpu_skip(mtgp32_gpu_t *h, uint64_t n, void *stream);
 
 /* Replaces mtgp32_fast_jump (mtgp32-fast-jump.c:51-79): jump_string is the

@@ -941,6 +941,21 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
     return MTGP_OK;
 }
 
+// Advance one generator by n steps: generated (and discarded) below
+// kSkipJumpMin steps, a GF(2) jump by X^n mod chi above (the polynomial from
+// the pool's cache; one jump kernel instead of n steps).
+constexpr uint64_t kSkipJumpMin = uint64_t(1) << 22;
+
+template <class T>
+int skipSingle(Pool<T> &P, uint64_t n, void *s) {
+    if (n < kSkipJumpMin) return P.fillOne(0, -1, nullptr, n, s);
+    const gf2::Poly *p = nullptr;
+    int rc = P.jumpPoly(P.hpidx[0], n, &p);
+    if (rc) return rc;
+    const std::vector<uint32_t> w = gf2::toWords32(*p, P.polyWords());
+    return P.jumpArray(0, w.data(), (int)w.size(), s);
+}
+
 template <class Obj>
 void freeSingle(Obj *h) {
     cudaDeviceSynchronize();
@@ -1205,7 +1220,7 @@ int mtgp32_gpu_fill_open_close(mtgp32_gpu_t *h, float *o, size_t n, void *s) { r
 int mtgp32_gpu_fill_open_open(mtgp32_gpu_t *h, float *o, size_t n, void *s) { return mtgp32_gpu_fill(h, 4, o, n, s); }
 int mtgp32_gpu_skip(mtgp32_gpu_t *h, uint64_t n, void *s) {
     if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
-    return h->pool.fillOne(0, -1, nullptr, n, s);
+    return skipSingle(h->pool, n, s);
 }
 int mtgp32_gpu_fast_jump(mtgp32_gpu_t *h, const char *js, void *s) {
     if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
@@ -1276,7 +1291,7 @@ int mtgp64_gpu_fill_open_close(mtgp64_gpu_t *h, double *o, size_t n, void *s) { 
 int mtgp64_gpu_fill_open_open(mtgp64_gpu_t *h, double *o, size_t n, void *s) { return mtgp64_gpu_fill(h, 4, o, n, s); }
 int mtgp64_gpu_skip(mtgp64_gpu_t *h, uint64_t n, void *s) {
     if (!h) return setErr(MTGP_ERR_INVALID, "null handle");
-    return h->pool.fillOne(0, -1, nullptr, n, s);
+    return skipSingle(h->pool, n, s);
 }
 int mtgp64_gpu_fast_jump(mtgp64_gpu_t *h, const char *js, void *s) {
     if (!h) return setErr(MTGP_ERR_INVALID, "null handle");

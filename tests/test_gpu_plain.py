@@ -86,7 +86,7 @@ def test_skip_matches_stepping(gpu, orc):
         p = load_table(table)[0]
         g = _gen(bits, p, seed=7)
         o = orc.gen(p, seed=7)
-        for n in (1, 300, 100003):
+        for n in (1, 300, 100003, (1 << 22) + 5):   # the last one is a jump
             g.skip(n)
             o.skip(n)
             assert np.array_equal(_run(g, 0, 500, bits), o.fill(0, 500))
