@@ -1,5 +1,5 @@
 """Generator banks (one CTA per parameter set): configs 2 and 3 at reduced
-length, bit-exact per stream, plus a full-length check of config 2."""
+length and at full length, bit-exact per stream."""
 import numpy as np
 import pytest
 import torch
@@ -46,6 +46,12 @@ def test_config3_bank_reduced(gpu, orc):
 def test_config2_bank_full_length(gpu, orc):
     """128 sets x 2^21 uint32, then 2^21 float [0,1) each: full size."""
     _bank(orc, 32, "mtgp32_fast_11213", 1234, 128, 1 << 21, (0, 2))
+
+
+def test_config3_bank_full_length(gpu, orc):
+    """200 sets of the OpenCL mtgp64dc table x 2^20 uint64, then 2^20 double
+    [1,2) each (mantissa bit-packing): full size."""
+    _bank(orc, 64, "mtgp64dc_fast_11213", 5678, 200, 1 << 20, (0, 1))
 
 
 def test_other_mexp_banks(gpu, orc):
