@@ -14,7 +14,9 @@
 //     recursion (GW words per sub-step, GW <= the shape's lanes);
 //   - each chunk's taps are split over the warps; lane l of a warp owns R
 //     consecutive outputs and slides an R-word register window along seq,
-//     so a tap costs one shared load and R masked XORs;
+//     so a tap costs one shared load and, when its coefficient is set, R
+//     XORs (the coefficient is the same for a whole warp, so a zero tap is a
+//     uniform branch past them);
 //   - the warps' partial sums are combined with shared-memory atomicXor.
 // A chain of polynomials is applied in order.
 #pragma once
@@ -30,7 +32,6 @@ struct Tr32 {
         uint32_t yy = rec32_pre(x1, x2, y, L.mask, L.sh1, L.sh2);
         return yy ^ lut(L.tbl, yy);
     }
-    __device__ static __forceinline__ W andm(W v, uint32_t m) { return v & m; }
     __device__ static __forceinline__ void axor(W *p, W v) { atomicXor(p, v); }
 };
 
@@ -41,9 +42,6 @@ struct Tr64 {
     __device__ static __forceinline__ W rec(W x1, W x2, W y, const Lane &L) {
         uint64_t yy = rec64_pre(x1, x2, y, L.mask, L.sh1, L.sh2);
         return yy ^ lut64(L.tbl_lo, L.tbl_hi, (uint32_t)yy);
-    }
-    __device__ static __forceinline__ W andm(W v, uint32_t m) {
-        return v & (uint64_t)(int64_t)(int32_t)m;
     }
     __device__ static __forceinline__ void axor(W *p, W v) {
         atomicXor(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
@@ -133,9 +131,12 @@ __device__ __forceinline__ void jump_chain_impl(typename Tr::W *smem, const type
 #pragma unroll
                     for (int j = 0; j < R; j++) {
                         const uint32_t bj = j < 32 ? bits_lo : bits_hi;
-                        const uint32_t m = (uint32_t)((int32_t)(bj << (31 - (j & 31))) >> 31);
+                        // the tap's coefficient is the same for the whole warp:
+                        // a zero skips the R XORs instead of masking them
+                        if ((bj >> (j & 31)) & 1u) {
 #pragma unroll
-                        for (int r = 0; r < R; r++) acc[r] ^= Tr::andm(win[(j + r) % R], m);
+                            for (int r = 0; r < R; r++) acc[r] ^= win[(j + r) % R];
+                        }
                         win[j] = ring[(uint32_t)(p + l0 + R + j) & M];
                     }
                 }
@@ -217,9 +218,12 @@ __device__ void jump_part(typename Tr::W *smem, const typename Tr::Lane &L, cons
 #pragma unroll
                     for (int j = 0; j < R; j++) {
                         const uint32_t bj = j < 32 ? bits_lo : bits_hi;
-                        const uint32_t m = (uint32_t)((int32_t)(bj << (31 - (j & 31))) >> 31);
+                        // the tap's coefficient is the same for the whole warp:
+                        // a zero skips the R XORs instead of masking them
+                        if ((bj >> (j & 31)) & 1u) {
 #pragma unroll
-                        for (int r = 0; r < R; r++) acc[r] ^= Tr::andm(win[(j + r) % R], m);
+                            for (int r = 0; r < R; r++) acc[r] ^= win[(j + r) % R];
+                        }
                         win[j] = ring[(uint32_t)(p + l0 + R + j) & M];
                     }
                 }
