@@ -408,7 +408,7 @@ def main():
     if args.no_autotune:
         plan, tune_report = pool.plan(items), "autotuner off"
     else:
-        plan, tune_report = pool.autotune(items, out, stream=s, reps=2)
+        plan, tune_report = pool.autotune(items, out, stream=s, reps=5)
     plan_ms = (time.perf_counter() - t0) * 1e3
     plan_tasks, plan_chunk = plan.info()
     plan_cfg = plan.describe()
@@ -517,7 +517,7 @@ def main():
         bitems = work_items(np.arange(128), np.zeros(128), np.full(128, nb),
                             np.arange(128) * nb * 4)
         t0 = time.perf_counter()
-        bplan, _ = bank.autotune(bitems, bout, stream=s, reps=2)
+        bplan, _ = bank.autotune(bitems, bout, stream=s, reps=3)
         setup_s = time.perf_counter() - t0
         for _ in range(3):
             bplan.launch(bout, s)

@@ -339,7 +339,7 @@ int mtgp64_gpu_pool_export(mtgp64_gpu_pool_t *p, int s, mtgp64_fast_t *dst);
  * configuration -- generation core (four words per thread in 64-thread CTAs
  * with 128-bit stores, or one word per thread in 256-thread CTAs), the chunk
  * length used to split long requests, and the grid size -- times each on
- * these items and this output buffer (best of `reps` launches on `stream`),
+ * these items and this output buffer (median of `reps` launches on `stream`),
  * and returns the fastest.  The pool's windows are restored before every
  * trial and at the end, so the pool is left unchanged.  `report` (optional)
  * receives one line per candidate. */

@@ -968,7 +968,7 @@ void freeSingle(Obj *h) {
 
 // Autotuner: build one plan per candidate configuration, time each on the
 // caller's own items and output buffer (CUDA events on the caller's stream,
-// best of `reps` launches after one warm-up), and keep the fastest.  The
+// median of `reps` launches after one warm-up), and keep the fastest.  The
 // stream windows are restored from a snapshot before every launch, so every
 // candidate does exactly the same work and the pool ends where it started.
 // Candidates: generation core (32-bit: four words per thread in 64-thread
@@ -1007,8 +1007,11 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
     int rc = MTGP_OK;
     cudaError_t ce = cudaMemcpyAsync(snap, P.d_states, sbytes, cudaMemcpyDeviceToDevice, S(s));
     if (ce != cudaSuccess) rc = cudaErr(ce, "autotune snapshot");
+    // median of `reps` launches after one warm-up: a persistent launch's
+    // length varies with the order its CTAs happen to take tasks in, and the
+    // minimum would favour plans whose length varies most
     auto timeOne = [&](mtgp_gpu_plan *pl, float *ms) -> int {
-        float bestt = 1e30f;
+        std::vector<float> ts;
         for (int r = 0; r <= reps; r++) {
             cudaError_t e = cudaMemcpyAsync(P.d_states, snap, sbytes, cudaMemcpyDeviceToDevice, S(s));
             if (e == cudaSuccess) e = cudaEventRecord(e0, S(s));
@@ -1020,9 +1023,10 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
             float t = 0;
             if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
             if (e != cudaSuccess) return cudaErr(e, "autotune timing");
-            if (r > 0 && t < bestt) bestt = t;
+            if (r > 0) ts.push_back(t);
         }
-        *ms = bestt;
+        std::sort(ts.begin(), ts.end());
+        *ms = ts[ts.size() / 2];
         return MTGP_OK;
     };
     for (size_t k = 0; k < cands.size() && !rc; k++) {

@@ -21,6 +21,14 @@ int fail(std::string *err, int code, const char *fmt, ...) {
     return code;
 }
 
+// Piece lengths of cut runs are multiples of a grain: the largest power of
+// two <= chunk / 8, at most 2^16 values.
+uint64_t pieceGrain(uint64_t chunk) {
+    uint64_t g = 1;
+    while (g * 2 <= chunk / 8 && g < (uint64_t(1) << 16)) g *= 2;
+    return g;
+}
+
 // A run: consecutive generated work of one stream starting at `start`.
 struct Run {
     int32_t stream;
@@ -138,6 +146,7 @@ int planCore(const mtgp_work_item_t *items, int nitems, const PlanOptions &o, Pl
         }
     }
     // cut runs into tasks; per stream, mark write-back
+    const uint64_t grain = chunk > 0 ? pieceGrain((uint64_t)chunk) : 1;
     r->segs.reserve(rseg.size() + runs.size());
     bool cut = false;
     for (size_t r0 = 0, r1; r0 < runs.size(); r0 = r1) {
@@ -146,10 +155,17 @@ int planCore(const mtgp_work_item_t *items, int nitems, const PlanOptions &o, Pl
         const size_t first_task = r->tasks.size();
         for (size_t ri = r0; ri < r1; ri++) {
             const Run &R = runs[ri];
-            uint64_t k = 1;
-            if (chunk > 0 && R.total > (uint64_t)chunk + (uint64_t)chunk / 4) {
+            // a run longer than one chunk becomes k = ceil(total / chunk)
+            // near-equal pieces, rounded up to a multiple of the grain so
+            // that the pieces' offsets (and jump polynomials) recur across
+            // requests; the last piece takes the rest
+            uint64_t k = 1, piece = R.total;
+            if (chunk > 0 && R.total > (uint64_t)chunk) {
                 k = (R.total + (uint64_t)chunk - 1) / (uint64_t)chunk;
-                cut = true;
+                piece = (R.total + k - 1) / k;
+                piece = (piece + grain - 1) / grain * grain;
+                k = (R.total + piece - 1) / piece;
+                if (k > 1) cut = true;
             }
             uint32_t si = R.first;     // segment of R being cut
             const uint32_t se = R.first + R.n;
@@ -158,9 +174,9 @@ int planCore(const mtgp_work_item_t *items, int nitems, const PlanOptions &o, Pl
                 PlanTask t{};
                 t.stream = R.stream;
                 t.run = R.start;
-                t.off = c * (uint64_t)chunk;
+                t.off = c * piece;
                 t.first = (uint32_t)r->segs.size();
-                uint64_t want = (c + 1 == k) ? ~uint64_t(0) : (uint64_t)chunk;
+                uint64_t want = (c + 1 == k) ? ~uint64_t(0) : piece;
                 while (si < se && (want || rseg[si].count == used)) {
                     PlanSeg g = rseg[si];
                     const uint64_t take = std::min(g.count - used, want);

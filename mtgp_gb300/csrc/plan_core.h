@@ -9,8 +9,10 @@
 //     is a new run that starts at that position, reached by jumping the
 //     window inside the kernel.  Shorter skips are generated (advance items);
 //     generated skips above `max_gen_skip` are rejected.
-//   - A run longer than 1.25 x `chunk` is cut into chunks of `chunk` values
-//     (the last takes the rest); chunk c starts at run start + c * chunk.
+//   - A run longer than `chunk` is cut into k = ceil(length / chunk)
+//     near-equal pieces whose length is rounded up to a multiple of the
+//     largest power of two <= chunk / 8 (at most 2^16; the last piece takes
+//     the rest); piece c starts at run start + c * piece.
 //   - The chunk length is `chunk_tune` when > 0, none when < 0, and
 //     otherwise the next power of two >= (all generated values / resident
 //     CTAs), at least 2^17.

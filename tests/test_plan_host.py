@@ -108,16 +108,23 @@ def check(items, res, nstreams, esz, can_jump, chunk_tune):
     if chunk_tune > 0 and chunk:
         assert chunk == chunk_tune
     if chunk:
-        # pieces of a cut run: all but the last are exactly one chunk long
+        # pieces of a cut run: near-equal, a multiple of the grain (largest
+        # power of two <= chunk / 8, at most 2^16), at most chunk + grain,
+        # the last taking the rest; uncut runs are at most one chunk
+        grain = 1
+        while grain * 2 <= chunk // 8 and grain < (1 << 16):
+            grain *= 2
         by_run = {}
         for s, wb, run, off, total, first, n in tasks:
             by_run.setdefault((s, run), []).append((off, total))
         for pieces in by_run.values():
             pieces.sort()
             if len(pieces) > 1:
-                assert all(t == chunk for _, t in pieces[:-1])
-                assert pieces[-1][1] <= chunk
-                assert [o for o, _ in pieces] == [k * chunk for k in range(len(pieces))]
+                piece = pieces[0][1]
+                assert piece % grain == 0 and piece < chunk + grain
+                assert all(t == piece for _, t in pieces[:-1])
+                assert 0 <= pieces[-1][1] <= piece
+                assert [o for o, _ in pieces] == [k * piece for k in range(len(pieces))]
     ob = max([off + count * esz for s, kind, count, off, skip in items if kind >= 0 and count],
              default=0)
     assert out_bytes == ob
@@ -186,7 +193,9 @@ def test_plan_automatic_chunk(probe):
     rc, res = plan(probe, items, 4, resident=2)
     assert rc == 0 and res[3] == 0 and len(res[0]) == 4   # 2^20 chunks: nothing to cut
     rc, res = plan(probe, items, 4, resident=8)
-    assert rc == 0 and res[3] == 0       # 150 k per slot -> 2^18: 300 k <= 1.25 x 2^18
+    assert rc == 0 and res[3] == 1 << 18   # 150 k per slot -> 2^18 < 300 k: two pieces
+    assert len(res[0]) == 8 and set(res[0][:, 4].tolist()) == {163840, 136160}  # grain 2^15
+    check(items, res, 4, 4, True, 0)
     rc, res = plan(probe, items, 4, resident=16)
     assert rc == 0 and res[3] == 1 << 17                   # 75 k per slot -> 2^17, cut
     check(items, res, 4, 4, True, 0)
