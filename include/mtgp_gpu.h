@@ -299,6 +299,14 @@ int mtgp32_gpu_pool_replan(mtgp32_gpu_pool_t *p, const mtgp_work_item_t *items,
 /* Jump stream s by a polynomial (uint32-array form). */
 int mtgp32_gpu_pool_jump_array(mtgp32_gpu_pool_t *p, int s,
                                const uint32_t *poly, int nwords, void *stream);
+/* X^steps[j] mod chi of parameter set `param_set`, for j < n, computed on the
+ * GPU (one CTA each, many at once) in the uint32-array form of
+ * jump_array: mexp/32 + 1 words each at dev_out + j * (mexp/32 + 1).
+ * steps is host memory.  Replaces NTL's PowerXMod (mtgp-calc-jump.hpp:135-162)
+ * for many exponents; batched work items with uncached long skips use it. */
+int mtgp32_gpu_pool_jump_polys(mtgp32_gpu_pool_t *p, int param_set,
+                               const uint64_t *steps, int n, uint32_t *dev_out,
+                               void *stream);
 /* All windows, count * size words, stream-major (synchronous). */
 int mtgp32_gpu_pool_get_windows_host(mtgp32_gpu_pool_t *p, uint32_t *win,
                                      size_t nwords);
@@ -329,6 +337,9 @@ int mtgp64_gpu_pool_replan(mtgp64_gpu_pool_t *p, const mtgp_work_item_t *items,
                            int nitems, mtgp_gpu_plan_t *plan);
 int mtgp64_gpu_pool_jump_array(mtgp64_gpu_pool_t *p, int s,
                                const uint32_t *poly, int nwords, void *stream);
+int mtgp64_gpu_pool_jump_polys(mtgp64_gpu_pool_t *p, int param_set,
+                               const uint64_t *steps, int n, uint32_t *dev_out,
+                               void *stream);
 int mtgp64_gpu_pool_get_windows_host(mtgp64_gpu_pool_t *p, uint64_t *win,
                                      size_t nwords);
 int mtgp64_gpu_pool_set_windows_host(mtgp64_gpu_pool_t *p,

@@ -90,6 +90,7 @@ for B, P, W in ((32, P32, c_u32), (64, P64, c_u64)):
         pre + "pool_plan": (c_int, [vp, vp, c_int, pp]),
         pre + "pool_replan": (c_int, [vp, vp, c_int, vp]),
         pre + "pool_jump_array": (c_int, [vp, c_int, vp, c_int, vp]),
+        pre + "pool_jump_polys": (c_int, [vp, c_int, vp, c_int, vp, vp]),
         pre + "pool_get_windows_host": (c_int, [vp, vp, c_size_t]),
         pre + "pool_set_windows_host": (c_int, [vp, vp, c_size_t]),
         pre + "pool_export": (c_int, [vp, c_int, vp]),

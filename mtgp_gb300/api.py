@@ -211,11 +211,12 @@ def work_items(streams, kinds, counts, offsets, skips=None):
 class Pool:
     """Many device-resident streams (mtgp32_gpu_pool_t / mtgp64_gpu_pool_t)."""
 
-    def __init__(self, bits, handle, size_words):
+    def __init__(self, bits, handle, mexp):
         self.bits = bits
         self.pre = "mtgp%d_gpu_pool_" % bits
         self.h = handle
-        self.size = size_words
+        self.mexp = mexp
+        self.size = mexp // bits + 1  # words of a window
         self.count = getattr(lib(), self.pre + "size")(handle)
 
     @classmethod
@@ -230,7 +231,7 @@ class Pool:
             ctypes.byref(h), arr, len(params_list),
             None if pidx is None else pidx.ctypes.data_as(ctypes.c_void_p),
             sd.ctypes.data_as(ctypes.c_void_p), len(sd)))
-        return cls(bits, h, params_list[0].mexp // bits + 1)
+        return cls(bits, h, params_list[0].mexp)
 
     @classmethod
     def substreams(cls, params, seed, count, table, stream=None):
@@ -240,7 +241,7 @@ class Pool:
         check(getattr(lib(), "mtgp%d_gpu_pool_create_substreams" % bits)(
             ctypes.byref(h), ctypes.byref(params), seed, count,
             t.ctypes.data_as(ctypes.c_void_p), t.shape[0], t.shape[1], _stream(stream)))
-        return cls(bits, h, params.mexp // bits + 1)
+        return cls(bits, h, params.mexp)
 
     def close(self):
         if self.h:
@@ -284,6 +285,16 @@ class Pool:
     def submit(self, items, out, stream=None):
         check(getattr(lib(), self.pre + "submit")(self.h, items, len(items),
                                                   ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+
+    def jump_polys(self, param_set, steps, stream=None):
+        """X^steps[j] mod chi of a parameter set, computed on the GPU: a
+        (len(steps), mexp/32 + 1) CUDA tensor of uint32 words (as int32)."""
+        st = np.ascontiguousarray(steps, dtype=np.uint64)
+        out = torch.empty((len(st), self.mexp // 32 + 1), dtype=torch.int32, device="cuda")
+        check(getattr(lib(), self.pre + "jump_polys")(
+            self.h, int(param_set), st.ctypes.data_as(ctypes.c_void_p), len(st),
+            ctypes.c_void_p(out.data_ptr()), _stream(stream)))
+        return out
 
     def jump_array(self, s, words, stream=None):
         w = np.ascontiguousarray(words, dtype=np.uint32)

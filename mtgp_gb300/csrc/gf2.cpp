@@ -232,6 +232,26 @@ Poly Modulus::powx(const std::vector<uint32_t> &e) const {
     return r;
 }
 
+Poly divXpow(int e, const Poly &m, int dm) {
+    // remainder r starts as X^e; clear its bits from the top with shifted m
+    Poly r((size_t)e / 64 + 1, 0), q((size_t)(e - dm) / 64 + 1, 0);
+    r[(size_t)e >> 6] = uint64_t(1) << (e & 63);
+    const int mw = dm / 64 + 1;
+    for (int b = e; b >= dm; b--) {
+        if (!((r[(size_t)b >> 6] >> (b & 63)) & 1u)) continue;
+        const int sh = b - dm;
+        q[(size_t)sh >> 6] |= uint64_t(1) << (sh & 63);
+        const int ws = sh >> 6, bs = sh & 63;
+        for (int k = 0; k < mw; k++) {
+            const size_t d = (size_t)(k + ws);
+            if (d >= r.size()) break;
+            r[d] ^= m[(size_t)k] << bs;
+            if (bs && d + 1 < r.size()) r[d + 1] ^= m[(size_t)k] >> (64 - bs);
+        }
+    }
+    return q;
+}
+
 Poly powxmod(const std::vector<uint32_t> &e, const Poly &m, int dm) {
     return Modulus(m, dm).powx(e);
 }

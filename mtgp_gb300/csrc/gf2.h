@@ -43,6 +43,9 @@ class Modulus {
     std::vector<uint64_t> tab_;
 };
 Poly mulComb(const Poly &a, const Poly &b);  // a * b, 8-bit comb
+// floor(X^e / m) for m of degree dm <= e (long division), e.g. the Barrett
+// constant floor(X^(2 dm) / m).
+Poly divXpow(int e, const Poly &m, int dm);
 
 // Minimal polynomial of the bit sequence s (Berlekamp-Massey); returns the
 // degree L and writes chi (monic, degree L).

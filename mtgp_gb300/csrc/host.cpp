@@ -270,6 +270,7 @@ struct Pool {
     PlanResult plan_scratch;  // reused by every plan of this pool
 
     ~Pool() {
+        for (auto &kv : gpow) cudaFree(kv.second);
         cudaFree(d_params);
         cudaFree(d_pidx);
         cudaFree(d_states);
@@ -498,6 +499,85 @@ struct Pool {
         return MTGP_OK;
     }
 
+    // X^(2^i) mod chi_k for i < 64, by squaring (once per parameter set).
+    int ensurePow2(int k) {
+        if (pow2.size() < hparams.size()) pow2.resize(hparams.size());
+        std::vector<gf2::Poly> &P2 = pow2[k];
+        if (!P2.empty()) return MTGP_OK;
+        const gf2::Modulus *M = nullptr;
+        int rc = modulus(k, &M);
+        if (rc) return rc;
+        gf2::Poly x((size_t)M->words(), 0);
+        x[0] = 2;  // X (the degree is far above 1)
+        P2.push_back(x);
+        for (int i = 1; i < 64; i++) P2.push_back(M->sqrmod(P2.back()));
+        return MTGP_OK;
+    }
+
+    // Device tables for computing X^e mod chi_k on the GPU (launchPowX):
+    // chi, mu = floor(X^(2D) / chi) and X^(2^i) for i < 64, polyWords()
+    // words each, made on first use.
+    std::map<int, uint32_t *> gpow;
+    int gpuPowTables(int k, const uint32_t **out) {
+        auto hit = gpow.find(k);
+        if (hit != gpow.end()) {
+            *out = hit->second;
+            return MTGP_OK;
+        }
+        int rc = ensurePow2(k);
+        if (rc) return rc;
+        const int W = polyWords(), D = chideg[k];
+        std::vector<uint32_t> h((size_t)66 * W);
+        auto put = [&](const gf2::Poly &p, int slot) {
+            const std::vector<uint32_t> w = gf2::toWords32(p, W);
+            std::copy(w.begin(), w.end(), h.begin() + (size_t)slot * W);
+        };
+        put(chi[k], 0);
+        put(gf2::divXpow(2 * D, chi[k], D), 1);
+        for (int i = 0; i < 64; i++) put(pow2[k][i], 2 + i);
+        uint32_t *d = nullptr;
+        CK(cudaMalloc(&d, sizeof(uint32_t) * h.size()), "cudaMalloc(jump tables)");
+        cudaError_t e = cudaMemcpy(d, h.data(), sizeof(uint32_t) * h.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            return cudaErr(e, "upload jump tables");
+        }
+        gpow[k] = d;
+        *out = d;
+        return MTGP_OK;
+    }
+
+    // X^steps[j] mod chi_k on the GPU, one CTA each, into out + j * polyWords().
+    int gpuJumpPolys(int k, const uint64_t *d_steps, int n, uint32_t *out, void *s) {
+        const uint32_t *t = nullptr;
+        int rc = gpuPowTables(k, &t);
+        if (rc) return rc;
+        const int W = polyWords();
+        CK(launchPowX(t, t + W, t + 2 * W, chideg[k], W, d_steps, n, out, S(s)), "jump polynomials");
+        return MTGP_OK;
+    }
+
+    // Public form: host exponents, device output (mtgp*_gpu_pool_jump_polys).
+    int jumpPolysApi(int k, const uint64_t *steps, int n, uint32_t *out, void *s) {
+        if (k < 0 || k >= nparams) return setErr(MTGP_ERR_INVALID, "parameter set %d out of range", k);
+        if (n < 0 || (n > 0 && (!steps || !out))) return setErr(MTGP_ERR_INVALID, "bad arguments");
+        if (n == 0) return MTGP_OK;
+        const uint32_t *t = nullptr;
+        int rc = gpuPowTables(k, &t);  // before any stream work
+        if (rc) return rc;
+        uint64_t *d = nullptr;
+        CK(cudaMallocAsync(reinterpret_cast<void **>(&d), sizeof(uint64_t) * n, S(s)),
+           "cudaMallocAsync(exponents)");
+        cudaError_t e =
+            cudaMemcpyAsync(d, steps, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, S(s));
+        if (e == cudaSuccess) rc = gpuJumpPolys(k, d, n, out, s);
+        cudaError_t f = cudaFreeAsync(d, S(s));
+        if (e != cudaSuccess) return cudaErr(e, "upload exponents");
+        if (rc) return rc;
+        if (f != cudaSuccess) return cudaErr(f, "cudaFreeAsync");
+        return MTGP_OK;
+    }
+
     // X^steps mod chi_k (host, cached): X^(steps - low) * X^low with low the
     // lowest set bit, X^(2^i) cached per parameter set, so that a sequence of
     // multiples of one chunk length costs one product each.
@@ -509,15 +589,9 @@ struct Pool {
         }
         const gf2::Modulus *M = nullptr;
         int rc = modulus(k, &M);
+        if (!rc) rc = ensurePow2(k);
         if (rc) return rc;
-        if (pow2.size() < hparams.size()) pow2.resize(hparams.size());
-        std::vector<gf2::Poly> &P2 = pow2[k];
-        if (P2.empty()) {
-            gf2::Poly x((size_t)M->words(), 0);
-            x[0] = 2;  // X (the degree is far above 1)
-            P2.push_back(x);
-            for (int i = 1; i < 64; i++) P2.push_back(M->sqrmod(P2.back()));
-        }
+        const std::vector<gf2::Poly> &P2 = pow2[k];
         gf2::Poly r;
         if (steps == 0) {
             r.assign((size_t)M->words(), 0);
@@ -665,6 +739,14 @@ struct mtgp_gpu_plan {
     const uint32_t *d_polys = nullptr;
     const int32_t *d_stage_streams = nullptr;
     unsigned *d_counter = nullptr;
+    // jump polynomials computed on the GPU before each launch, after the
+    // host-computed ones: groups of (parameter set, first job, jobs)
+    struct JobGroup {
+        int pidx, first, n;
+    };
+    std::vector<JobGroup> gpu_jobs;
+    uint32_t *gpu_polys = nullptr;
+    const uint64_t *gpu_steps = nullptr;
     void *d_stage = nullptr;  // final windows of streams with several tasks
     size_t cap_stage = 0;
 
@@ -680,6 +762,13 @@ struct mtgp_gpu_plan {
 };
 
 namespace {
+
+// A jump polynomial X^steps mod chi_pidx computed on the GPU at launch.
+struct GpuJob {
+    int pidx;
+    uint64_t steps;
+    int32_t slot;
+};
 
 template <class T>
 int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_plan **out,
@@ -725,16 +814,34 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     // the plan's jump polynomials: X^steps mod chi for (parameter set, steps)
     const size_t pw = (size_t)P.polyWords();
     std::map<std::pair<int, uint64_t>, int> poly_at;
-    std::vector<uint32_t> polys;
-    auto polyIndex = [&](int pidx, uint64_t steps, int32_t *idx) -> int {
+    std::vector<uint32_t> polys;  // computed here, in index order
+    // A requested skip (a run start) that the host has not cached and would
+    // need two or more products for is computed on the GPU at launch
+    // (GpuJob): arbitrary offsets then cost the host nothing.  Chunk offsets
+    // recur from plan to plan and stay on the host, cached.  Until the
+    // indices are final, GPU polynomials carry kGpuSlot + job number.
+    constexpr int32_t kGpuSlot = 1 << 29;
+    std::vector<GpuJob> gjobs;
+    auto polyIndex = [&](int pidx, uint64_t steps, int32_t *idx, bool gpu_ok) -> int {
         auto hit = poly_at.find({pidx, steps});
         if (hit == poly_at.end()) {
-            const gf2::Poly *p = nullptr;
-            int rc2 = P.jumpPoly(pidx, steps, &p);
-            if (rc2) return rc2;
-            hit = poly_at.emplace(std::make_pair(pidx, steps), (int)(polys.size() / pw)).first;
-            const std::vector<uint32_t> w = gf2::toWords32(*p, (int)pw);
-            polys.insert(polys.end(), w.begin(), w.end());
+            int slot;
+            if (gpu_ok && P.jcache.find({pidx, steps}) == P.jcache.end() &&
+                __builtin_popcountll(steps) >= 3) {
+                const uint32_t *t = nullptr;
+                int rc2 = P.gpuPowTables(pidx, &t);  // made now, never during a launch
+                if (rc2) return rc2;
+                slot = kGpuSlot + (int)gjobs.size();
+                gjobs.push_back(GpuJob{pidx, steps, slot});
+            } else {
+                const gf2::Poly *p = nullptr;
+                int rc2 = P.jumpPoly(pidx, steps, &p);
+                if (rc2) return rc2;
+                slot = (int)(polys.size() / pw);
+                const std::vector<uint32_t> w = gf2::toWords32(*p, (int)pw);
+                polys.insert(polys.end(), w.begin(), w.end());
+            }
+            hit = poly_at.emplace(std::make_pair(pidx, steps), slot).first;
         }
         *idx = hit->second;
         return MTGP_OK;
@@ -754,10 +861,10 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         // offsets (shared by every long request) are each few, so few
         // distinct polynomials are needed
         if (pt.run && pt.off) {
-            rc = polyIndex(t.pidx, pt.run, &t.j0);
-            if (!rc) rc = polyIndex(t.pidx, pt.off, &t.j1);
+            rc = polyIndex(t.pidx, pt.run, &t.j0, true);
+            if (!rc) rc = polyIndex(t.pidx, pt.off, &t.j1, false);
         } else if (pt.run || pt.off) {
-            rc = polyIndex(t.pidx, pt.run | pt.off, &t.j0);
+            rc = polyIndex(t.pidx, pt.run | pt.off, &t.j0, pt.run != 0);
         }
         if (rc) return rc;
     }
@@ -768,7 +875,23 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         bitems[q].kind = R.segs[q].kind;
         bitems[q].pad_ = 0;
     }
-    const bool split = !polys.empty();  // the kernel variant with the jump code
+    // final indices of the GPU-computed polynomials: after the host's,
+    // grouped by parameter set so that each group is one launch
+    const int nhost = (int)(polys.size() / pw);
+    std::stable_sort(gjobs.begin(), gjobs.end(),
+                     [](const GpuJob &a, const GpuJob &b) { return a.pidx < b.pidx; });
+    std::vector<int32_t> remap(gjobs.size());
+    std::vector<uint64_t> job_steps(gjobs.size());
+    for (size_t q = 0; q < gjobs.size(); q++) {
+        remap[(size_t)(gjobs[q].slot - kGpuSlot)] = nhost + (int32_t)q;
+        job_steps[q] = gjobs[q].steps;
+    }
+    for (BatchTask &t : tasks) {
+        if (t.j0 >= kGpuSlot) t.j0 = remap[(size_t)(t.j0 - kGpuSlot)];
+        if (t.j1 >= kGpuSlot) t.j1 = remap[(size_t)(t.j1 - kGpuSlot)];
+    }
+    const size_t npolys = (size_t)nhost + gjobs.size();
+    const bool split = npolys > 0;  // the kernel variant with the jump code
     // reuse the caller's plan (replan) when given: its device buffers are
     // kept and only grown, so a server can refill plans without freeing
     // device memory (cudaFree would wait for every batch in flight)
@@ -795,7 +918,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     auto align = [](size_t n) { return (n + 255) & ~size_t(255); };
     const size_t off_items = align(sizeof(BatchTask) * tasks.size());
     const size_t off_polys = off_items + align(sizeof(BatchItem) * bitems.size());
-    const size_t off_ss = off_polys + align(sizeof(uint32_t) * polys.size());
+    const size_t off_steps = off_polys + align(sizeof(uint32_t) * pw * npolys);
+    const size_t off_ss = off_steps + align(sizeof(uint64_t) * job_steps.size());
     const size_t bytes = off_ss + sizeof(int32_t) * stage_streams.size();
     cudaError_t e = cudaSuccess;
     if (!pl->d_counter) e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
@@ -838,6 +962,16 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     if (!tasks.empty()) std::memcpy(h, tasks.data(), sizeof(BatchTask) * tasks.size());
     if (!bitems.empty()) std::memcpy(h + off_items, bitems.data(), sizeof(BatchItem) * bitems.size());
     if (!polys.empty()) std::memcpy(h + off_polys, polys.data(), sizeof(uint32_t) * polys.size());
+    if (!job_steps.empty())
+        std::memcpy(h + off_steps, job_steps.data(), sizeof(uint64_t) * job_steps.size());
+    pl->gpu_jobs.clear();
+    for (size_t q = 0; q < gjobs.size(); q++) {  // (parameter set, first job, jobs)
+        if (q == 0 || gjobs[q].pidx != gjobs[q - 1].pidx)
+            pl->gpu_jobs.push_back({gjobs[q].pidx, (int)q, 0});
+        pl->gpu_jobs.back().n++;
+    }
+    pl->gpu_polys = reinterpret_cast<uint32_t *>(pl->d_blob + off_polys) + (size_t)nhost * pw;
+    pl->gpu_steps = reinterpret_cast<const uint64_t *>(pl->d_blob + off_steps);
     if (!stage_streams.empty())
         std::memcpy(h + off_ss, stage_streams.data(), sizeof(int32_t) * stage_streams.size());
     pl->blob_bytes = bytes;
@@ -866,6 +1000,12 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     if (pl->out_bytes && !out) return setErr(MTGP_ERR_INVALID, "null output pointer");
     int rc = uploadPlan(pl, s);
     if (rc) return rc;
+    const size_t pw = (size_t)P.polyWords();
+    for (const mtgp_gpu_plan::JobGroup &g : pl->gpu_jobs) {
+        rc = P.gpuJumpPolys(g.pidx, pl->gpu_steps + g.first, g.n,
+                            pl->gpu_polys + (size_t)g.first * pw, s);
+        if (rc) return rc;
+    }
     BatchLaunch b{};
     b.mexp = P.sh.mexp;
     b.mode = pl->mode;
@@ -1394,6 +1534,11 @@ int mtgp64_gpu_set_window_host(mtgp64_gpu_t *h, const uint64_t *w, int size) {
         delete pl;                                                                               \
         if (!rc && e != cudaSuccess) rc = cudaErr(e, "batched launch");                          \
         return rc;                                                                               \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_jump_polys(mtgp##B##_gpu_pool_t *p, int param_set,                   \
+                                      const uint64_t *steps, int n, uint32_t *dev_out, void *s) { \
+        if (!p) return setErr(MTGP_ERR_INVALID, "null pool");                                   \
+        return p->pool.jumpPolysApi(param_set, steps, n, dev_out, s);                           \
     }                                                                                            \
     int mtgp##B##_gpu_pool_jump_array(mtgp##B##_gpu_pool_t *p, int i, const uint32_t *poly,      \
                                       int nw, void *s) {                                         \

@@ -77,6 +77,12 @@ cudaError_t launchSeed32(const DevParams32 *params, const int *pidx, const uint3
 cudaError_t launchSeed64(const DevParams64 *params, const int *pidx, const uint64_t *seeds,
                          uint64_t *states, int count, int size, int stride, cudaStream_t s);
 
+// X^steps[k] mod chi for k < n, one CTA each, into out + k * W (chi, mu =
+// floor(X^(2D) / chi) and p2[i] = X^(2^i) mod chi for i < 64: W = D/32 + 1
+// words each, bit i of the words = coefficient of X^i).
+cudaError_t launchPowX(const uint32_t *chi, const uint32_t *mu, const uint32_t *p2, int D, int W,
+                       const uint64_t *steps, int n, uint32_t *out, cudaStream_t s);
+
 cudaError_t launchGen32(int mexp, int kind, const DevParams32 *params,
                         const int *pidx, uint32_t *states, int ngen,
                         void *out, uint64_t n, uint64_t outStride,

@@ -46,3 +46,10 @@ int probe_pow2_product(const uint64_t *m, int dm, uint64_t e, uint64_t *out) {
     return 0;
 }
 }
+
+// floor(X^e / m): quotient words into out ((e - dm) / 64 + 1 words).
+extern "C" int probe_divxpow(const uint64_t *m, int dm, int e, uint64_t *out) {
+    Poly q = mtgp::gf2::divXpow(e, take(m, dm / 64 + 1), dm);
+    std::memcpy(out, q.data(), sizeof(uint64_t) * q.size());
+    return (int)q.size();
+}

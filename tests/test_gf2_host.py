@@ -76,3 +76,30 @@ def test_mulmod_matches_oracle(orc, probe, table):
         out = np.zeros(w, dtype=np.uint64)
         probe.probe_mulmod(_p(a), _p(b), _p(m), d, _p(out))
         assert np.array_equal(out, orc.mulmod(a, b, m, d))
+
+
+def test_barrett_constant(orc, probe):
+    """mu = floor(X^(2d) / chi) satisfies X^(2d) = mu * chi + rho with
+    deg rho < d (checked with the oracle's products)."""
+    probe.probe_divxpow.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    d, m = _chi(orc, "mtgp32_fast_11213")
+    mu = np.zeros(d // 64 + 2, dtype=np.uint64)
+    n = probe.probe_divxpow(_p(m), d, 2 * d, _p(mu))
+    assert n == d // 64 + 1
+    # the bit-serial product mu * chi, then X^(2d) xor it must have degree < d
+    prod = np.zeros(2 * d // 64 + 3, dtype=np.uint64)
+    for i in range(d + 1):
+        if (int(mu[i >> 6]) >> (i & 63)) & 1:
+            for k in range(len(m)):
+                w = int(m[k])
+                if not w:
+                    continue
+                lo = (w << (i & 63)) & (2 ** 64 - 1)
+                hi = w >> (64 - (i & 63)) if i & 63 else 0
+                prod[k + (i >> 6)] ^= np.uint64(lo)
+                if hi:
+                    prod[k + (i >> 6) + 1] ^= np.uint64(hi)
+    prod[(2 * d) >> 6] ^= np.uint64(1 << ((2 * d) & 63))
+    top = max((64 * k + int(prod[k]).bit_length() - 1 for k in range(len(prod)) if prod[k]),
+              default=-1)
+    assert top < d

@@ -149,3 +149,25 @@ def test_substreams(gpu, orc, bits, table):
         assert (int(w[0]) ^ int(win[j][0])) & int(p.mask) == 0, j
         assert np.array_equal(w[1:], win[j][1:]), j
         chain.fast_jump(js)
+
+
+@pytest.mark.parametrize("bits,table,idx", [(32, "mtgp32_fast_11213", 0),
+                                            (64, "mtgp64dc_fast_11213", 1),
+                                            (32, "mtgp32_fast_23209", 2)])
+def test_gpu_jump_polys_match_oracle(gpu, orc, bits, table, idx):
+    """X^e mod chi computed on the GPU (one CTA per exponent: word-parallel
+    products, Barrett reduction) equals the oracle's bit-serial PowerXMod."""
+    from mtgp_gb300.api import Pool
+    tbl = load_table(table)
+    pool = Pool.create([tbl[0], tbl[idx]], [1, 2], [0, 1])
+    p = tbl[idx]
+    rng = np.random.default_rng(31 + idx)
+    steps = [0, 1, 2, 3, 1 << 17, (1 << 40) + 12345, (1 << 64) - 1, 3 ** 40]
+    steps += [int(x) for x in rng.integers(0, 2 ** 63, 8, dtype=np.int64)]
+    got = pool.jump_polys(1, steps).cpu().numpy().view(np.uint32)
+    seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
+    d, chi = orc.minpoly((seq & 1).astype(np.uint8))
+    nw = p.mexp // 32 + 1
+    for k, e in enumerate(steps):
+        ref = orc.powxmod(e, chi, d).view(np.uint32)[:nw]
+        assert np.array_equal(got[k], ref), e

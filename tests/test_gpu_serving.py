@@ -307,3 +307,37 @@ def test_jumps_across_many_parameter_sets(gpu, orc):
                 assert np.array_equal(got[k * 5000:(k + 1) * 5000], o.fill(0, 5000)), (rep, k)
     finally:
         set_tuning("split_chunk", 0)
+
+
+@pytest.mark.parametrize("bits,table", CASES)
+def test_arbitrary_skips_use_gpu_polynomials(gpu, orc, bits, table):
+    """Skips at arbitrary (not power-of-two) offsets: their jump polynomials
+    are computed on the GPU at launch; outputs and windows match the oracle
+    jumped by the same X^skip, over two launches of the plan."""
+    from mtgp_gb300.api import work_items
+    pool, plist, pidx, seeds = _pool(bits, table, 8)
+    rng = np.random.default_rng(77 + bits)
+    skips = [int(x) for x in rng.integers(1 << 17, 1 << 40, 8, dtype=np.int64)]
+    skips[3] = (1 << 20) + 1          # popcount 2: stays on the host
+    counts = [1000 + 37 * k for k in range(8)]
+    esz = bits // 8
+    offs = list(np.concatenate([[0], np.cumsum(counts)[:-1]]) * esz)
+    items = work_items(list(range(8)), [0] * 8, counts, offs, skips)
+    plan = pool.plan(items)
+    chis = {}
+    gens = [orc.gen(plist[pidx[s]], seed=int(seeds[s])) for s in range(8)]
+    nw = plist[0].mexp // 32 + 1
+    for rep in range(2):
+        out = torch.zeros(sum(counts) * esz // 4 + 4, dtype=torch.int32, device="cuda")
+        plan.launch(out)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().view(np.uint8)
+        for s in range(8):
+            p = plist[pidx[s]]
+            if s % 3 not in chis:
+                seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
+                chis[s % 3] = orc.minpoly((seq & 1).astype(np.uint8))
+            d, chi = chis[s % 3]
+            gens[s].jump_words(orc.powxmod(skips[s], chi, d).view(np.uint32)[:nw])
+            ref = np_bits(gens[s].fill(0, counts[s]), bits).view(np.uint8)
+            assert np.array_equal(got[offs[s]:offs[s] + ref.size], ref), (rep, s)
