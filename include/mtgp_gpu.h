@@ -386,7 +386,10 @@ int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
  *   "batch_grid"   0 = one CTA per resident slot, > 0 = that many CTAs
  *   "core"         32-bit generation core: 4 = four adjacent words per
  *                  thread (default), 1 = one word per thread; plans whose
- *                  items mix output kinds use the one-word core */
+ *                  items mix output kinds use the one-word core
+ *   "poly_window"  bits per table window of the GPU's polynomial products
+ *                  (jump polynomials): 0 = automatic (4 where the table
+ *                  fits in shared memory, else 2), 2 or 4 */
 int mtgp_gpu_set_tuning(const char *key, int64_t value);
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
 

@@ -20,6 +20,7 @@
 #include "gf2.h"
 #include "internal.h"
 #include "plan_core.h"
+#include "pow_sched.h"
 
 namespace mtgp {
 
@@ -268,6 +269,8 @@ struct Pool {
     // X^steps mod chi, keyed by (parameter set, steps); bounded
     std::map<std::pair<int, uint64_t>, gf2::Poly> jcache;
     PlanResult plan_scratch;  // reused by every plan of this pool
+    PowSchedule pow_scratch;
+    std::vector<PowOp> powop_scratch;
 
     ~Pool() {
         for (auto &kv : gpow) cudaFree(kv.second);
@@ -514,9 +517,11 @@ struct Pool {
         return MTGP_OK;
     }
 
-    // Device tables for computing X^e mod chi_k on the GPU (launchPowX):
-    // chi, mu = floor(X^(2D) / chi) and X^(2^i) for i < 64, polyWords()
-    // words each, made on first use.
+    // Device tables for computing X^e mod chi_k on the GPU (pow_sched.h):
+    // chi | mu = floor(X^(2D) / chi) | slot 256 m + k = X^(k 2^(8m)) mod chi,
+    // polyWords() words each (5.8 MB for MEXP 11213), made on first use:
+    // the slots X^(2^i) come from the host's squarings, the others from
+    // 1,976 products on the GPU (seven launches, about a millisecond).
     std::map<int, uint32_t *> gpow;
     int gpuPowTables(int k, const uint32_t **out) {
         auto hit = gpow.find(k);
@@ -524,37 +529,80 @@ struct Pool {
             *out = hit->second;
             return MTGP_OK;
         }
+        const int W = polyWords();
+        if (!powOpsFits(W)) return setErr(MTGP_ERR_UNSUPPORTED, "polynomials too long for the GPU");
         int rc = ensurePow2(k);
         if (rc) return rc;
-        const int W = polyWords(), D = chideg[k];
-        std::vector<uint32_t> h((size_t)66 * W);
-        auto put = [&](const gf2::Poly &p, int slot) {
+        const int D = chideg[k];
+        const size_t words = (size_t)(2 + kPowSlots) * W;
+        std::vector<uint32_t> h(words, 0u);
+        auto put = [&](const gf2::Poly &p, size_t slot) {
             const std::vector<uint32_t> w = gf2::toWords32(p, W);
-            std::copy(w.begin(), w.end(), h.begin() + (size_t)slot * W);
+            std::copy(w.begin(), w.end(), h.begin() + (std::ptrdiff_t)(slot * W));
         };
         put(chi[k], 0);
         put(gf2::divXpow(2 * D, chi[k], D), 1);
-        for (int i = 0; i < 64; i++) put(pow2[k][i], 2 + i);
+        for (int i = 0; i < 64; i++) put(pow2[k][i], 2 + (size_t)powSlot(i / 8, 1 << (i % 8)));
+        PowSchedule sch;
+        tableSchedule(sch);
+        std::vector<PowOp> ops;
         uint32_t *d = nullptr;
-        CK(cudaMalloc(&d, sizeof(uint32_t) * h.size()), "cudaMalloc(jump tables)");
-        cudaError_t e = cudaMemcpy(d, h.data(), sizeof(uint32_t) * h.size(), cudaMemcpyHostToDevice);
+        PowOp *d_ops = nullptr;
+        cudaStream_t st = nullptr;
+        cudaError_t e = cudaMalloc(&d, sizeof(uint32_t) * words);
+        if (e == cudaSuccess) e = cudaMalloc(&d_ops, sizeof(PowOp) * (size_t)sch.steps());
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d, h.data(), sizeof(uint32_t) * words, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            powOps(sch, [&](int) { return d; }, d + 2 * W, nullptr, D, ops);
+            e = cudaMemcpyAsync(d_ops, ops.data(), sizeof(PowOp) * ops.size(),
+                                cudaMemcpyHostToDevice, st);
+        }
+        size_t first = 0;
+        for (size_t l = 0; e == cudaSuccess && l < sch.levels.size(); l++) {
+            const int n = (int)sch.levels[l].size();
+            e = launchPowOps(d_ops + first, n, nullptr, W, st);
+            first += (size_t)n;
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (st) cudaStreamDestroy(st);
+        cudaFree(d_ops);
         if (e != cudaSuccess) {
             cudaFree(d);
-            return cudaErr(e, "upload jump tables");
+            return cudaErr(e, "jump tables on the GPU");
         }
         gpow[k] = d;
         *out = d;
         return MTGP_OK;
     }
 
-    // X^steps[j] mod chi_k on the GPU, one CTA each, into out + j * polyWords().
-    int gpuJumpPolys(int k, const uint64_t *d_steps, int n, uint32_t *out, void *s) {
-        const uint32_t *t = nullptr;
-        int rc = gpuPowTables(k, &t);
-        if (rc) return rc;
-        const int W = polyWords();
-        CK(launchPowX(t, t + W, t + 2 * W, chideg[k], W, d_steps, n, out, S(s)), "jump polynomials");
-        return MTGP_OK;
+    // Device form of a schedule, level by level: table slots of tab(job),
+    // scratch slots of `scratch`, outputs at dst_base + index * W.
+    template <class Tab>
+    void powOps(const PowSchedule &sch, Tab tab, uint32_t *dst_base, uint32_t *scratch, int D,
+                std::vector<PowOp> &ops) const {
+        const size_t W = (size_t)polyWords();
+        ops.clear();
+        for (const auto &lev : sch.levels)
+            for (const PowStep &st : lev) {
+                PowOp o{};
+                o.tab = tab(st.job);
+                o.dst = st.dst >= 0 ? dst_base + (size_t)st.dst * W
+                                    : scratch + (size_t)(-1 - st.dst) * W;
+                o.D = D;
+                o.nsrc = st.nsrc;
+                for (int q = 0; q < kPowMaxSrc; q++) o.src[q] = st.src[q];
+                ops.push_back(o);
+            }
+    }
+
+    // CTAs of the product kernel that run at once (one per SM).
+    int powWidth() const {
+        int dev = 0, sms = 152;
+        if (cudaGetDevice(&dev) == cudaSuccess)
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        return sms;
     }
 
     // Public form: host exponents, device output (mtgp*_gpu_pool_jump_polys).
@@ -565,15 +613,26 @@ struct Pool {
         const uint32_t *t = nullptr;
         int rc = gpuPowTables(k, &t);  // before any stream work
         if (rc) return rc;
-        uint64_t *d = nullptr;
-        CK(cudaMallocAsync(reinterpret_cast<void **>(&d), sizeof(uint64_t) * n, S(s)),
-           "cudaMallocAsync(exponents)");
-        cudaError_t e =
-            cudaMemcpyAsync(d, steps, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, S(s));
-        if (e == cudaSuccess) rc = gpuJumpPolys(k, d, n, out, s);
+        const int W = polyWords();
+        PowSchedule sch;
+        powSchedule(steps, n, powWidth(), sch);
+        unsigned char *d = nullptr;
+        const size_t ops_bytes = (sizeof(PowOp) * (size_t)sch.steps() + 255) & ~size_t(255);
+        const size_t bytes = ops_bytes + sizeof(uint32_t) * (size_t)sch.nscratch * W;
+        CK(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, S(s)), "cudaMallocAsync(products)");
+        uint32_t *scratch = reinterpret_cast<uint32_t *>(d + ops_bytes);
+        std::vector<PowOp> ops;
+        powOps(sch, [t](int) { return t; }, out, scratch, chideg[k], ops);
+        cudaError_t e = cudaMemcpyAsync(d, ops.data(), sizeof(PowOp) * ops.size(),
+                                        cudaMemcpyHostToDevice, S(s));
+        size_t first = 0;
+        for (size_t l = 0; e == cudaSuccess && l < sch.levels.size(); l++) {
+            const int m = (int)sch.levels[l].size();
+            e = launchPowOps(reinterpret_cast<const PowOp *>(d) + first, m, scratch, W, S(s));
+            first += (size_t)m;
+        }
         cudaError_t f = cudaFreeAsync(d, S(s));
-        if (e != cudaSuccess) return cudaErr(e, "upload exponents");
-        if (rc) return rc;
+        if (e != cudaSuccess) return cudaErr(e, "jump polynomials");
         if (f != cudaSuccess) return cudaErr(f, "cudaFreeAsync");
         return MTGP_OK;
     }
@@ -740,13 +799,12 @@ struct mtgp_gpu_plan {
     const int32_t *d_stage_streams = nullptr;
     unsigned *d_counter = nullptr;
     // jump polynomials computed on the GPU before each launch, after the
-    // host-computed ones: groups of (parameter set, first job, jobs)
-    struct JobGroup {
-        int pidx, first, n;
-    };
-    std::vector<JobGroup> gpu_jobs;
-    uint32_t *gpu_polys = nullptr;
-    const uint64_t *gpu_steps = nullptr;
+    // host-computed ones: the product levels of pow_sched.h (steps per
+    // level, one launch each), their scratch polynomials kept and grown
+    std::vector<int> pow_levels;
+    const PowOp *d_powops = nullptr;
+    uint32_t *d_pscratch = nullptr;
+    size_t cap_pscratch = 0;
     void *d_stage = nullptr;  // final windows of streams with several tasks
     size_t cap_stage = 0;
 
@@ -755,6 +813,7 @@ struct mtgp_gpu_plan {
     ~mtgp_gpu_plan() {
         if (exec) cudaGraphExecDestroy(exec);
         cudaFree(d_stage);
+        cudaFree(d_pscratch);
         cudaFree(d_blob);
         cudaFreeHost(h_blob);
         cudaFree(d_counter);
@@ -816,10 +875,10 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     std::map<std::pair<int, uint64_t>, int> poly_at;
     std::vector<uint32_t> polys;  // computed here, in index order
     // A requested skip (a run start) that the host has not cached and would
-    // need two or more products for is computed on the GPU at launch
-    // (GpuJob): arbitrary offsets then cost the host nothing.  Chunk offsets
-    // recur from plan to plan and stay on the host, cached.  Until the
-    // indices are final, GPU polynomials carry kGpuSlot + job number.
+    // need a product for (two or more set bits) is computed on the GPU at
+    // launch (GpuJob): arbitrary offsets then cost the host nothing.  Chunk
+    // offsets recur from plan to plan and stay on the host, cached.  Until
+    // the indices are final, GPU polynomials carry kGpuSlot + job number.
     constexpr int32_t kGpuSlot = 1 << 29;
     std::vector<GpuJob> gjobs;
     auto polyIndex = [&](int pidx, uint64_t steps, int32_t *idx, bool gpu_ok) -> int {
@@ -827,7 +886,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         if (hit == poly_at.end()) {
             int slot;
             if (gpu_ok && P.jcache.find({pidx, steps}) == P.jcache.end() &&
-                __builtin_popcountll(steps) >= 3) {
+                __builtin_popcountll(steps) >= 2) {
                 const uint32_t *t = nullptr;
                 int rc2 = P.gpuPowTables(pidx, &t);  // made now, never during a launch
                 if (rc2) return rc2;
@@ -886,6 +945,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         remap[(size_t)(gjobs[q].slot - kGpuSlot)] = nhost + (int32_t)q;
         job_steps[q] = gjobs[q].steps;
     }
+    PowSchedule &sch = P.pow_scratch;
+    powSchedule(job_steps.data(), (int)job_steps.size(), P.powWidth(), sch);
     for (BatchTask &t : tasks) {
         if (t.j0 >= kGpuSlot) t.j0 = remap[(size_t)(t.j0 - kGpuSlot)];
         if (t.j1 >= kGpuSlot) t.j1 = remap[(size_t)(t.j1 - kGpuSlot)];
@@ -918,8 +979,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     auto align = [](size_t n) { return (n + 255) & ~size_t(255); };
     const size_t off_items = align(sizeof(BatchTask) * tasks.size());
     const size_t off_polys = off_items + align(sizeof(BatchItem) * bitems.size());
-    const size_t off_steps = off_polys + align(sizeof(uint32_t) * pw * npolys);
-    const size_t off_ss = off_steps + align(sizeof(uint64_t) * job_steps.size());
+    const size_t off_ops = off_polys + align(sizeof(uint32_t) * pw * npolys);
+    const size_t off_ss = off_ops + align(sizeof(PowOp) * (size_t)sch.steps());
     const size_t bytes = off_ss + sizeof(int32_t) * stage_streams.size();
     cudaError_t e = cudaSuccess;
     if (!pl->d_counter) e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
@@ -936,6 +997,14 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         pl->cap_h = 0;
         e = cudaHostAlloc(&pl->h_blob, bytes + bytes / 4, cudaHostAllocDefault);
         if (e == cudaSuccess) pl->cap_h = bytes + bytes / 4;
+    }
+    if (e == cudaSuccess && (size_t)sch.nscratch * pw > pl->cap_pscratch) {
+        const size_t need = (size_t)sch.nscratch * pw;
+        cudaFree(pl->d_pscratch);
+        pl->d_pscratch = nullptr;
+        pl->cap_pscratch = 0;
+        e = cudaMalloc(&pl->d_pscratch, sizeof(uint32_t) * (need + need / 4));
+        if (e == cudaSuccess) pl->cap_pscratch = need + need / 4;
     }
     if (e == cudaSuccess && pl->nstage) {
         const size_t need = sizeof(W) * (size_t)P.stride * pl->nstage;
@@ -962,16 +1031,18 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     if (!tasks.empty()) std::memcpy(h, tasks.data(), sizeof(BatchTask) * tasks.size());
     if (!bitems.empty()) std::memcpy(h + off_items, bitems.data(), sizeof(BatchItem) * bitems.size());
     if (!polys.empty()) std::memcpy(h + off_polys, polys.data(), sizeof(uint32_t) * polys.size());
-    if (!job_steps.empty())
-        std::memcpy(h + off_steps, job_steps.data(), sizeof(uint64_t) * job_steps.size());
-    pl->gpu_jobs.clear();
-    for (size_t q = 0; q < gjobs.size(); q++) {  // (parameter set, first job, jobs)
-        if (q == 0 || gjobs[q].pidx != gjobs[q - 1].pidx)
-            pl->gpu_jobs.push_back({gjobs[q].pidx, (int)q, 0});
-        pl->gpu_jobs.back().n++;
+    pl->pow_levels.clear();
+    if (sch.steps()) {  // GPU job q writes polynomial nhost + q
+        std::vector<PowOp> &ops = P.powop_scratch;
+        uint32_t *dst = reinterpret_cast<uint32_t *>(pl->d_blob + off_polys) + (size_t)nhost * pw;
+        std::vector<const uint32_t *> tabs(gjobs.size());
+        for (size_t q = 0; q < gjobs.size(); q++) tabs[q] = P.gpow.at(gjobs[q].pidx);
+        P.powOps(sch, [&tabs](int j) { return tabs[(size_t)j]; }, dst, pl->d_pscratch,
+                 P.sh.mexp, ops);
+        std::memcpy(h + off_ops, ops.data(), sizeof(PowOp) * ops.size());
+        for (const auto &lev : sch.levels) pl->pow_levels.push_back((int)lev.size());
     }
-    pl->gpu_polys = reinterpret_cast<uint32_t *>(pl->d_blob + off_polys) + (size_t)nhost * pw;
-    pl->gpu_steps = reinterpret_cast<const uint64_t *>(pl->d_blob + off_steps);
+    pl->d_powops = reinterpret_cast<const PowOp *>(pl->d_blob + off_ops);
     if (!stage_streams.empty())
         std::memcpy(h + off_ss, stage_streams.data(), sizeof(int32_t) * stage_streams.size());
     pl->blob_bytes = bytes;
@@ -1001,10 +1072,11 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     int rc = uploadPlan(pl, s);
     if (rc) return rc;
     const size_t pw = (size_t)P.polyWords();
-    for (const mtgp_gpu_plan::JobGroup &g : pl->gpu_jobs) {
-        rc = P.gpuJumpPolys(g.pidx, pl->gpu_steps + g.first, g.n,
-                            pl->gpu_polys + (size_t)g.first * pw, s);
-        if (rc) return rc;
+    size_t first = 0;
+    for (int n : pl->pow_levels) {
+        CK(launchPowOps(pl->d_powops + first, n, pl->d_pscratch, (int)pw, S(s)),
+           "jump polynomials");
+        first += (size_t)n;
     }
     BatchLaunch b{};
     b.mexp = P.sh.mexp;
@@ -1632,6 +1704,10 @@ int mtgp_gpu_set_tuning(const char *key, int64_t value) {
     } else if (!std::strcmp(key, "core")) {
         if (value != 1 && value != 4) return setErr(MTGP_ERR_INVALID, "core must be 1 or 4");
         setGenCore32((int)value);
+    } else if (!std::strcmp(key, "poly_window")) {
+        if (value != 0 && value != 2 && value != 4)
+            return setErr(MTGP_ERR_INVALID, "poly_window must be 0, 2 or 4");
+        setPowWindow((int)value);
     } else if (!std::strcmp(key, "batch_grid")) {
         if (value < 0) return setErr(MTGP_ERR_INVALID, "batch_grid must be >= 0");
         g_tune.batch_grid = value;

@@ -77,11 +77,25 @@ cudaError_t launchSeed32(const DevParams32 *params, const int *pidx, const uint3
 cudaError_t launchSeed64(const DevParams64 *params, const int *pidx, const uint64_t *seeds,
                          uint64_t *states, int count, int size, int stride, cudaStream_t s);
 
-// X^steps[k] mod chi for k < n, one CTA each, into out + k * W (chi, mu =
-// floor(X^(2D) / chi) and p2[i] = X^(2^i) mod chi for i < 64: W = D/32 + 1
-// words each, bit i of the words = coefficient of X^i).
-cudaError_t launchPowX(const uint32_t *chi, const uint32_t *mu, const uint32_t *p2, int D, int W,
-                       const uint64_t *steps, int n, uint32_t *out, cudaStream_t s);
+// One product of a jump-polynomial schedule (pow_sched.h): dst = product
+// of the nsrc sources mod chi (nsrc = 0: the polynomial 1).  tab points at
+// chi | mu = floor(X^(2 D) / chi) | table slots, W words each (bit i of the
+// words = coefficient of X^i); a source code >= 0 is a table slot, < 0 the
+// scratch slot -1 - code.
+struct PowOp {
+    const uint32_t *tab;
+    uint32_t *dst;
+    int32_t D;  // degree of chi; W >= D / 32 + 1
+    int32_t nsrc;
+    int32_t src[8];
+};
+
+// The n independent products ops[0..n), one CTA each (W words per
+// polynomial); smem limits: powOpsFits(W).
+bool powOpsFits(int W);
+void setPowWindow(int bits);  // comb window: 0 automatic, 2 or 4 bits
+cudaError_t launchPowOps(const PowOp *ops, int n, const uint32_t *scratch, int W,
+                         cudaStream_t s);
 
 cudaError_t launchGen32(int mexp, int kind, const DevParams32 *params,
                         const int *pidx, uint32_t *states, int ngen,

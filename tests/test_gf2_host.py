@@ -103,3 +103,29 @@ def test_barrett_constant(orc, probe):
     top = max((64 * k + int(prod[k]).bit_length() - 1 for k in range(len(prod)) if prod[k]),
               default=-1)
     assert top < d
+
+
+def test_pow_schedules_match_oracle(orc, probe):
+    """The GPU's product schedules (byte-window table, then per exponent a
+    serial chain or a pairwise tree), executed here with the host's
+    products, give the oracle's X^e mod chi; the tree is picked for few
+    exponents (depth 3 for eight factors), the chain for many."""
+    L = probe
+    vp = ctypes.c_void_p
+    L.probe_pow_schedule.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp, vp]
+    d, m = _chi(orc, "mtgp32_fast_11213")
+    w = (d + 63) // 64
+    rng = np.random.default_rng(5)
+    exps = np.array([0, 1, 255, 256, 257, (1 << 64) - 1, 1 << 63, 0x0101010101010101,
+                     *rng.integers(0, 2 ** 63, 6, dtype=np.uint64)], dtype=np.uint64)
+    for width, want in ((152, "tree"), (1, "serial")):
+        out = np.zeros((len(exps), w), dtype=np.uint64)
+        shape = np.zeros(3, dtype=np.int32)
+        assert L.probe_pow_schedule(_p(m), d, _p(exps), len(exps), width, _p(out), _p(shape)) == 0
+        for j, e in enumerate(exps):
+            assert np.array_equal(out[j], orc.powxmod(int(e), m, d)), (width, int(e))
+        levels, steps, nscratch = shape
+        if want == "tree":
+            assert levels == 3 and nscratch > 0
+        else:
+            assert levels == 1 and steps == len(exps) and nscratch == 0

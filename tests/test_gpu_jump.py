@@ -151,23 +151,50 @@ def test_substreams(gpu, orc, bits, table):
         chain.fast_jump(js)
 
 
-@pytest.mark.parametrize("bits,table,idx", [(32, "mtgp32_fast_11213", 0),
-                                            (64, "mtgp64dc_fast_11213", 1),
-                                            (32, "mtgp32_fast_23209", 2)])
-def test_gpu_jump_polys_match_oracle(gpu, orc, bits, table, idx):
-    """X^e mod chi computed on the GPU (one CTA per exponent: word-parallel
-    products, Barrett reduction) equals the oracle's bit-serial PowerXMod."""
-    from mtgp_gb300.api import Pool
+@pytest.mark.parametrize("bits,table,idx,window", [(32, "mtgp32_fast_11213", 0, 0),
+                                                   (32, "mtgp32_fast_11213", 3, 2),
+                                                   (64, "mtgp64dc_fast_11213", 1, 0),
+                                                   (32, "mtgp32_fast_23209", 2, 0),
+                                                   (32, "mtgp32_fast_44497", 1, 0)])
+def test_gpu_jump_polys_match_oracle(gpu, orc, bits, table, idx, window):
+    """X^e mod chi computed on the GPU (byte-window tables made on the GPU,
+    then a tree of comb products with Barrett reduction) equals the oracle's
+    bit-serial PowerXMod; window 2 is the variant for long polynomials."""
+    from mtgp_gb300.api import Pool, set_tuning
     tbl = load_table(table)
-    pool = Pool.create([tbl[0], tbl[idx]], [1, 2], [0, 1])
-    p = tbl[idx]
-    rng = np.random.default_rng(31 + idx)
-    steps = [0, 1, 2, 3, 1 << 17, (1 << 40) + 12345, (1 << 64) - 1, 3 ** 40]
-    steps += [int(x) for x in rng.integers(0, 2 ** 63, 8, dtype=np.int64)]
-    got = pool.jump_polys(1, steps).cpu().numpy().view(np.uint32)
+    set_tuning("poly_window", window)
+    try:
+        pool = Pool.create([tbl[0], tbl[idx]], [1, 2], [0, 1])
+        p = tbl[idx]
+        rng = np.random.default_rng(31 + idx)
+        steps = [0, 1, 2, 3, 255, 256, 1 << 17, (1 << 40) + 12345, (1 << 64) - 1, 3 ** 40]
+        nrand = 2 if p.mexp > 40000 else 8
+        steps += [int(x) for x in rng.integers(0, 2 ** 63, nrand, dtype=np.int64)]
+        got = pool.jump_polys(1, steps).cpu().numpy().view(np.uint32)
+    finally:
+        set_tuning("poly_window", 0)
     seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
     d, chi = orc.minpoly((seq & 1).astype(np.uint8))
     nw = p.mexp // 32 + 1
     for k, e in enumerate(steps):
         ref = orc.powxmod(e, chi, d).view(np.uint32)[:nw]
         assert np.array_equal(got[k], ref), e
+
+
+def test_gpu_jump_polys_many(gpu, orc):
+    """600 exponents at once (one chain of products per CTA instead of the
+    tree): 40 distinct exponents, each repeated, against the oracle."""
+    from mtgp_gb300.api import Pool
+    tbl = load_table("mtgp32_fast_11213")
+    p = tbl[5]
+    pool = Pool.create([p], [3], [0])
+    rng = np.random.default_rng(8)
+    distinct = [int(x) for x in rng.integers(0, 2 ** 63, 40, dtype=np.int64)]
+    steps = [distinct[(7 * k) % 40] for k in range(600)]
+    got = pool.jump_polys(0, steps).cpu().numpy().view(np.uint32)
+    seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
+    d, chi = orc.minpoly((seq & 1).astype(np.uint8))
+    nw = p.mexp // 32 + 1
+    refs = {e: orc.powxmod(e, chi, d).view(np.uint32)[:nw] for e in distinct}
+    for k, e in enumerate(steps):
+        assert np.array_equal(got[k], refs[e]), (k, e)

@@ -318,7 +318,8 @@ def test_arbitrary_skips_use_gpu_polynomials(gpu, orc, bits, table):
     pool, plist, pidx, seeds = _pool(bits, table, 8)
     rng = np.random.default_rng(77 + bits)
     skips = [int(x) for x in rng.integers(1 << 17, 1 << 40, 8, dtype=np.int64)]
-    skips[3] = (1 << 20) + 1          # popcount 2: stays on the host
+    skips[3] = 1 << 33                # a power of two: stays on the host
+    skips[5] = (1 << 20) + 1          # two factors from one table
     counts = [1000 + 37 * k for k in range(8)]
     esz = bits // 8
     offs = list(np.concatenate([[0], np.cumsum(counts)[:-1]]) * esz)
