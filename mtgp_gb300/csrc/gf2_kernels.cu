@@ -10,33 +10,49 @@
 // only below X^W.
 //
 // Products use the comb method.  The right operand B becomes a table of
-// its 2^WIN multiples v * B (v < 2^WIN, WIN = 4 bits) in shared memory; the
-// word A[i] of the left operand contributes, for each WIN-bit window w of
-// A[i] with value v, the table row v shifted by 32 i + WIN w bits.  A warp
-// takes a tile of 32 output words x 32 words of A: lane l owns output word
-// o = 32 ob + l and keeps one accumulator per window position, so that each
-// (A word, window) costs one table load (consecutive words across the
-// lanes: no bank conflicts) and one XOR; the window shifts are applied once
-// per tile, the bits that cross into word o + 1 pass to the next lane with a
-// shuffle, and the tile adds its words to the result with shared-memory
-// XOR atomics.  Tiles that touch no table word are never visited: a tile
-// (ob, ib) contributes only if 0 <= ob - ib <= (lb + 31) / 32.  Table rows
-// carry 32 zero words before and 64 after so that a tile's lanes never need
-// a bounds test.  There is no carry-less multiply instruction; a table load
-// stands for WIN shifted XORs.
+// its 2^WIN multiples v * B (v < 2^WIN; WIN = 4 bits, 2 for polynomials too
+// long for that table) in shared memory; the word A[i] of the left operand
+// contributes, for each WIN-bit window w of A[i] with value v, the table row
+// v shifted by 32 i + WIN w bits.  A warp takes a tile of 32 K output words
+// x 32 words of A: lane l owns word l of each of K blocks of 32 output words
+// and keeps one accumulator per (block, window position), so that one
+// window extraction serves K table loads (consecutive words across the
+// lanes: no bank conflicts) and two loads share one three-input XOR.  The
+// kernel is then bound by shared-memory bandwidth (one 128-byte wavefront per
+// warp-wide load).  The window shifts are applied once per tile, the bits
+// that cross into the next word pass one lane up with a shuffle, and the
+// tile adds its words to the result with shared-memory XOR atomics.  Table
+// rows carry zero padding (32 words before, 32 K + 32 after) so that no
+// lane of a visited tile needs a bounds test.  There is no carry-less
+// multiply instruction; a table load stands for WIN shifted XORs.
 #include "internal.h"
 
 namespace mtgp {
 namespace {
 
 constexpr int kPowThreads = 1024;
-constexpr int kPadLo = 32, kPadHi = 64;
 
-__host__ __device__ constexpr int rowStride(int W) { return kPadLo + W + 1 + kPadHi; }
+// Output words per lane: K blocks of 32 words (one window extraction serves
+// K table loads); the K x NB accumulators of a lane take 32 registers.  A
+// tile covers IL words of A.
+template <int WIN>
+struct Comb {
+    static constexpr int NB = 32 / WIN;  // windows per word
+    static constexpr int K = NB == 8 ? 4 : 2;
+    static constexpr int IL = 32;
+    static constexpr int kPadLo = 32, kPadHi = 32 * K + 32;
+};
+
+template <int WIN>
+__host__ __device__ constexpr int rowStride(int W) {
+    return Comb<WIN>::kPadLo + W + 1 + Comb<WIN>::kPadHi;
+}
 
 // shared words: table (2^WIN rows), R (W), P (2W + 2), Q (W + 1), U (2W + 2)
-__host__ __device__ constexpr size_t powSmemWords(int win, int W) {
-    return (size_t)(1 << win) * rowStride(W) + (size_t)W + (2 * W + 2) + (W + 1) + (2 * W + 2);
+template <int WIN>
+__host__ __device__ constexpr size_t powSmemWords(int W) {
+    return (size_t)(1 << WIN) * rowStride<WIN>(W) + (size_t)W + (2 * W + 2) + (W + 1) +
+           (2 * W + 2);
 }
 
 // Table rows T[v * S + kPadLo + d] = word d of v * B, d <= lb (B: lb words,
@@ -52,61 +68,102 @@ __device__ void buildTable(const uint32_t *B, int lb, uint32_t *T, int S) {
 #pragma unroll
         for (int b = 0; b < WIN; b++)
             if ((v >> b) & 1) w ^= __funnelshift_l(lo, hi, b);
-        T[v * S + kPadLo + d] = w;
+        T[v * S + Comb<WIN>::kPadLo + d] = w;
     }
     __syncthreads();
 }
 
 // Out[o] ^= (A * B)[o] for o in [o_lo, o_hi); A: la words (generic
 // pointer), B: lb words through its table T.  Ends with a barrier.
+//
+// The words of A block ib (IL words) meet the output blocks (32 words) ob
+// with 0 <= 32 ob - IL ib + 31 and 32 ob - IL ib - IL + 1 <= lb: a run of
+// consecutive blocks, cut into tiles of K blocks from its first (the last
+// tile may reach past the run and reads the rows' zero padding).  The
+// tiles' A-word pairs are dealt out to the warps in equal contiguous
+// ranges, so that no warp waits for another at the closing barrier; a tile
+// split between warps adds its partial sums with the same atomics.
 template <int WIN>
 __device__ void combMul(const uint32_t *A, int la, const uint32_t *T, int S, int lb,
                         uint32_t *Out, int o_lo, int o_hi) {
-    constexpr int NB = 32 / WIN, MASK = (1 << WIN) - 1;
+    constexpr int NB = Comb<WIN>::NB, K = Comb<WIN>::K, IL = Comb<WIN>::IL, PAIRS = IL / 2;
+    constexpr int MASK = (1 << WIN) - 1, nwarps = kPowThreads / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int nwarps = kPowThreads / 32;
-    const int nib = (la + 31) >> 5;
-    const int dmax = (lb + 31) >> 5;  // ob - ib in [0, dmax]
-    const int ob1 = (o_hi - 1) >> 5;  // o_lo - 1 may carry into o_lo
-    int ob = (o_lo > 0 ? o_lo - 1 : 0) >> 5, base = 0;
-    auto ibLo = [&](int b) { return b - dmax > 0 ? b - dmax : 0; };
-    auto cnt = [&](int b) {
-        const int hi = b < nib - 1 ? b : nib - 1, lo = ibLo(b);
-        return hi >= lo ? hi - lo + 1 : 0;
+    const int nib = (la + IL - 1) / IL;
+    const int ob_lo = (o_lo > 0 ? o_lo - 1 : 0) >> 5;  // o_lo - 1 may carry into o_lo
+    const int ob_hi = (o_hi - 1) >> 5;
+    // output blocks of A block b: [first(b), last(b)]
+    auto first = [&](int b) {
+        const int f = (IL * b) >> 5;  // 32 ob + 31 >= IL b
+        return f > ob_lo ? f : ob_lo;
     };
-    for (int tt = warp;; tt += nwarps) {
-        while (ob <= ob1 && tt >= base + cnt(ob)) {
-            base += cnt(ob);
-            ob++;
+    auto last = [&](int b) {
+        const int l = (IL * b + IL - 1 + lb) >> 5;  // 32 ob <= IL b + IL - 1 + lb
+        return l < ob_hi ? l : ob_hi;
+    };
+    auto cnt = [&](int b) {
+        const int n = last(b) - first(b) + 1;
+        return n > 0 ? (n + K - 1) / K : 0;
+    };
+    int tiles = 0;
+    for (int b = 0; b < nib; b++) tiles += cnt(b);
+    const int units = tiles * PAIRS;
+    const int u1 = (int)(((long long)(warp + 1) * units) / nwarps);
+    int u = (int)(((long long)warp * units) / nwarps);
+    int ib = 0, base = 0;  // base: index of A block ib's first tile
+    while (u < u1) {
+        const int t = u / PAIRS, p0 = u - t * PAIRS;
+        const int p1 = p0 + (u1 - u) < PAIRS ? p0 + (u1 - u) : PAIRS;
+        u += p1 - p0;
+        while (t >= base + cnt(ib)) {
+            base += cnt(ib);
+            ib++;
         }
-        if (ob > ob1) break;
-        const int ib = ibLo(ob) + (tt - base);
-        const int o = (ob << 5) + lane, ia = (ib << 5) + lane;
-        const uint32_t areg = ia < la ? A[ia] : 0u;
-        uint32_t acc[NB];
+        const int ob = first(ib) + K * (t - base);
+        const int o = (ob << 5) + lane, ia = IL * ib + lane;
+        const uint32_t areg = (lane < IL && ia < la) ? A[ia] : 0u;
+        uint32_t acc[K][NB];
 #pragma unroll
-        for (int w = 0; w < NB; w++) acc[w] = 0;
-        // word d = o - i of the rows, i = 32 ib + il; |d| stays in the padding
-        const uint32_t *tp = T + kPadLo + o - (ib << 5);
-#pragma unroll 2
-        for (int il = 0; il < 32; il++) {
-            const uint32_t a = __shfl_sync(0xffffffffu, areg, il);
-            if (a) {  // the same word for the whole warp
-                const uint32_t *t = tp - il;
+        for (int k = 0; k < K; k++)
 #pragma unroll
-                for (int w = 0; w < NB; w++) acc[w] ^= t[(int)((a >> (WIN * w)) & MASK) * S];
+            for (int w = 0; w < NB; w++) acc[k][w] = 0;
+        // word d = o + 32 k - i of the rows, i = IL ib + il:
+        // -31 <= d <= lb + 32 K + IL - 2 over a visited tile
+        const uint32_t *tp = T + Comb<WIN>::kPadLo + o - IL * ib;
+#pragma unroll 1
+        for (int il = 2 * p0; il < 2 * p1; il += 2) {
+            const uint32_t a0 = __shfl_sync(0xffffffffu, areg, il);
+            const uint32_t a1 = __shfl_sync(0xffffffffu, areg, il + 1);
+            if (a0 | a1) {  // the same words for the whole warp
+#pragma unroll
+                for (int w = 0; w < NB; w++) {
+                    const uint32_t *q0 = tp - il + (int)((a0 >> (WIN * w)) & MASK) * S;
+                    const uint32_t *q1 = tp - il - 1 + (int)((a1 >> (WIN * w)) & MASK) * S;
+#pragma unroll
+                    for (int k = 0; k < K; k++) acc[k][w] ^= q0[32 * k] ^ q1[32 * k];
+                }
             }
         }
-        uint32_t lo = acc[0], hi = 0;
+        // window shifts; bits crossing into the next word move one lane up
+        // (lane 31's to lane 0 of the next block, the last block's to the
+        // word after the tile)
+        uint32_t carry = 0;
 #pragma unroll
-        for (int w = 1; w < NB; w++) {
-            lo ^= acc[w] << (WIN * w);
-            hi ^= acc[w] >> (32 - WIN * w);
+        for (int k = 0; k < K; k++) {
+            uint32_t lo = acc[k][0], hi = 0;
+#pragma unroll
+            for (int w = 1; w < NB; w++) {
+                lo ^= acc[k][w] << (WIN * w);
+                hi ^= acc[k][w] >> (32 - WIN * w);
+            }
+            const uint32_t up = __shfl_sync(0xffffffffu, hi, (lane + 31) & 31);
+            lo ^= lane ? up : carry;
+            carry = up;  // lane 0: lane 31's bits, for the next block
+            const int ok = o + 32 * k;
+            if (ok >= o_lo && ok < o_hi) atomicXor(&Out[ok], lo);
         }
-        const uint32_t carry = __shfl_up_sync(0xffffffffu, hi, 1);
-        if (lane) lo ^= carry;
-        if (o >= o_lo && o < o_hi) atomicXor(&Out[o], lo);
-        if (lane == 31 && o + 1 >= o_lo && o + 1 < o_hi) atomicXor(&Out[o + 1], hi);
+        const int oe = o - lane + 32 * K;
+        if (lane == 0 && oe >= o_lo && oe < o_hi) atomicXor(&Out[oe], carry);
     }
     __syncthreads();
 }
@@ -143,7 +200,7 @@ template <int WIN>
 __global__ void __launch_bounds__(kPowThreads, 1)
 k_powops(const PowOp *__restrict__ ops, const uint32_t *__restrict__ scratch, int W) {
     extern __shared__ __align__(16) uint32_t sm[];
-    const int S = rowStride(W);
+    const int S = rowStride<WIN>(W);
     uint32_t *T = sm, *R = T + (size_t)(1 << WIN) * S, *P = R + W, *Q = P + 2 * W + 2,
              *U = Q + W + 1;
     const PowOp &op = ops[blockIdx.x];
@@ -168,7 +225,7 @@ int g_pow_window = 0;  // 0: 4 bits where the table fits, else 2
 
 }  // namespace
 
-bool powOpsFits(int W) { return W > 0 && powSmemWords(2, W) * 4 <= kPowSmemMax; }
+bool powOpsFits(int W) { return W > 0 && powSmemWords<2>(W) * 4 <= kPowSmemMax; }
 
 void setPowWindow(int bits) { g_pow_window = bits; }
 
@@ -176,8 +233,8 @@ cudaError_t launchPowOps(const PowOp *ops, int n, const uint32_t *scratch, int W
                          cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     if (!powOpsFits(W)) return cudaErrorInvalidValue;
-    const bool wide = g_pow_window != 2 && powSmemWords(4, W) * 4 <= kPowSmemMax;
-    const size_t smem = 4 * powSmemWords(wide ? 4 : 2, W);
+    const bool wide = g_pow_window != 2 && powSmemWords<4>(W) * 4 <= kPowSmemMax;
+    const size_t smem = 4 * (wide ? powSmemWords<4>(W) : powSmemWords<2>(W));
     auto kern = wide ? k_powops<4> : k_powops<2>;
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024)
