@@ -304,6 +304,71 @@ def run_serving(args, s, local):
     return out, check
 
 
+POLY_WORKLOAD = ("jump polynomials X^e mod chi of mtgp32_params_fast_11213[0] on the GPU, "
+                 "e uniform in [2^56, 2^63)")
+
+
+def run_polys(args, s):
+    """Jump-polynomial section: X^e mod chi for arbitrary 64-bit exponents
+    computed on the GPU (byte-window tables, then products).  Latency of one
+    exponent through the public call (host exponent in, device polynomial
+    out) and throughput of args.poly_n exponents per call."""
+    import torch
+    from mtgp_gb300.api import Pool
+    from mtgp_gb300.params import load_table
+    p = load_table("mtgp32_fast_11213")[0]
+    pool = Pool.create([p], [SEED], [0])
+    t0 = time.perf_counter()
+    pool.jump_polys(0, [12345], stream=s)  # tables: characteristic polynomial, X^(k 2^(8m))
+    s.synchronize()
+    table_ms = (time.perf_counter() - t0) * 1e3
+    rng = np.random.default_rng(13)
+    lat = []
+    for _ in range(3 + args.poly_reps):
+        e = int(rng.integers(1 << 56, 1 << 63))
+        t0 = time.perf_counter()
+        pool.jump_polys(0, [e], stream=s)
+        s.synchronize()
+        lat.append(time.perf_counter() - t0)
+    lat = np.array(lat[3:])
+    st = rng.integers(1 << 56, 1 << 63, args.poly_n, dtype=np.int64)
+    pool.jump_polys(0, st, stream=s)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.synchronize()
+    t0 = time.perf_counter()
+    ev0.record(s)
+    for _ in range(args.poly_reps):
+        pool.jump_polys(0, st, stream=s)
+    ev1.record(s)
+    s.synchronize()
+    wall = (time.perf_counter() - t0) / args.poly_reps
+    dev_ms = ev0.elapsed_time(ev1) / args.poly_reps
+    return {"workload": POLY_WORKLOAD, "table_setup_ms": round(table_ms, 2),
+            "one_exponent_ms": {"p50": round(1e3 * float(np.percentile(lat, 50)), 3),
+                                "p99": round(1e3 * float(np.percentile(lat, 99)), 3),
+                                "calls": int(lat.size)},
+            "batch": {"exponents": int(args.poly_n), "ms": round(wall * 1e3, 3),
+                      "device_ms": round(dev_ms, 3),
+                      "per_s": round(args.poly_n / wall, 1)}}
+
+
+def poly_cpu_baseline(orc, seconds):
+    """The oracle's bit-serial PowerXMod (one core) on the same exponents'
+    distribution: polynomials per second over a bounded sample."""
+    from mtgp_gb300.params import load_table
+    p = load_table("mtgp32_fast_11213")[0]
+    seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
+    d, chi = orc.minpoly((seq & 1).astype(np.uint8))
+    rng = np.random.default_rng(13)
+    n, t0 = 0, time.perf_counter()
+    while n < 2 or (time.perf_counter() - t0 < seconds and n < 64):
+        orc.powxmod(int(rng.integers(1 << 56, 1 << 63)), chi, d)
+        n += 1
+    dt = time.perf_counter() - t0
+    return {"value": round(n / dt, 2), "unit": "polynomials/s", "cores": 1, "kind": "port",
+            "sample": "%d exponents, bit-serial PowerXMod" % n}
+
+
 def serve_check(orc, chk):
     """Every response of the check trace against the oracle: each stream
     replayed in submission order from the windows the pools started from
@@ -346,7 +411,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--substreams", type=int, default=N_SUB,
                     help="substreams of the batched workload (profiling runs use fewer)")
-    ap.add_argument("--only", default="all", choices=["all", "batched", "bank", "serve"],
+    ap.add_argument("--only", default="all",
+                    choices=["all", "batched", "bank", "serve", "polys"],
                     help="profiling runs: time only one path, no e2e / plain / CPU legs")
     ap.add_argument("--serve-seconds", type=float, default=3.0,
                     help="length of each Poisson trace of the serving section")
@@ -356,6 +422,9 @@ def main():
     ap.add_argument("--uniform", type=int, default=0,
                     help="profiling runs: every substream requests this many values "
                          "(steady-state throughput instead of the lognormal workload)")
+    ap.add_argument("--poly-n", type=int, default=4096,
+                    help="exponents per call of the jump-polynomial section")
+    ap.add_argument("--poly-reps", type=int, default=20)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tune", action="append", default=[],
                     help="key=value tuning knob (split_chunk, batch_grid)")
@@ -384,6 +453,11 @@ def main():
         k, v = kv.split("=")
         set_tuning(k, int(v))
     from mtgp_gb300.params import jump_table, load_table
+
+    if args.only == "polys":  # profiling run: the jump-polynomial section alone
+        if rank == 0:
+            print(json.dumps({"polys": run_polys(args, torch.cuda.Stream())}))
+        return
 
     p = load_table("mtgp32_fast_11213")[0]
     nsub = args.substreams
@@ -532,6 +606,11 @@ def main():
                   "ms": round(bb_ms, 3), "plan": bplan.describe(),
                   "setup_s": round(setup_s, 2)}
 
+    # --- jump polynomials for arbitrary offsets, on the GPU ---
+    polys = None
+    if rank == 0 and args.only == "all":
+        polys = run_polys(args, s)
+
     # --- serving: continuous batching over resident streams ---
     serve, serve_chk = None, None
     if rank == 0 and not args.no_serve and args.only in ("all", "serve"):
@@ -566,6 +645,8 @@ def main():
                "gpu_first_step_bit_exact": ok}
         if serve_chk is not None:
             serve["check"] = serve_check(orc, serve_chk)
+        if polys is not None:
+            polys["cpu_baseline"] = poly_cpu_baseline(orc, min(args.cpu_seconds, 5.0))
 
     if rank == 0:
         line = {
@@ -590,6 +671,7 @@ def main():
                      "autotune_ms": round(plan_ms, 1),
                      "autotune": [l for l in tune_report.strip().splitlines()]},
             "serve": serve,
+            "jump_polys": polys,
             "e2e": {"value": round(e2e, 3), "unit": "GB/s", "h2d_bytes_per_step": 32 * nsub,
                     "d2h_bytes_per_step": total_bytes},
             "roofline": roofline,

@@ -300,10 +300,14 @@ int mtgp32_gpu_pool_replan(mtgp32_gpu_pool_t *p, const mtgp_work_item_t *items,
 int mtgp32_gpu_pool_jump_array(mtgp32_gpu_pool_t *p, int s,
                                const uint32_t *poly, int nwords, void *stream);
 /* X^steps[j] mod chi of parameter set `param_set`, for j < n, computed on the
- * GPU (one CTA each, many at once) in the uint32-array form of
- * jump_array: mexp/32 + 1 words each at dev_out + j * (mexp/32 + 1).
- * steps is host memory.  Replaces NTL's PowerXMod (mtgp-calc-jump.hpp:135-162)
- * for many exponents; batched work items with uncached long skips use it. */
+ * GPU in the uint32-array form of jump_array: mexp/32 + 1 words each at
+ * dev_out + j * (mexp/32 + 1).  steps is host memory.  Products of at most
+ * eight byte-window table polynomials (the table is made on the GPU at the
+ * first call for the parameter set, synchronously); a few exponents spread
+ * over many CTAs, many run one per CTA.  Replaces NTL's PowerXMod
+ * (mtgp-calc-jump.hpp:135-162); batched work items with uncached long skips
+ * use the same products.  MTGP_ERR_UNSUPPORTED if the polynomials are too
+ * long for the product kernel's shared memory. */
 int mtgp32_gpu_pool_jump_polys(mtgp32_gpu_pool_t *p, int param_set,
                                const uint64_t *steps, int n, uint32_t *dev_out,
                                void *stream);

@@ -598,11 +598,15 @@ struct Pool {
     }
 
     // CTAs of the product kernel that run at once (one per SM).
-    int powWidth() const {
-        int dev = 0, sms = 152;
-        if (cudaGetDevice(&dev) == cudaSuccess)
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        return sms;
+    int pow_width = 0;
+    int powWidth() {
+        if (!pow_width) {
+            int dev = 0, sms = 152;
+            if (cudaGetDevice(&dev) == cudaSuccess)
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            pow_width = sms > 0 ? sms : 152;
+        }
+        return pow_width;
     }
 
     // Public form: host exponents, device output (mtgp*_gpu_pool_jump_polys).
@@ -946,7 +950,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         job_steps[q] = gjobs[q].steps;
     }
     PowSchedule &sch = P.pow_scratch;
-    powSchedule(job_steps.data(), (int)job_steps.size(), P.powWidth(), sch);
+    powSchedule(job_steps.data(), (int)job_steps.size(), job_steps.empty() ? 1 : P.powWidth(),
+                sch);
     for (BatchTask &t : tasks) {
         if (t.j0 >= kGpuSlot) t.j0 = remap[(size_t)(t.j0 - kGpuSlot)];
         if (t.j1 >= kGpuSlot) t.j1 = remap[(size_t)(t.j1 - kGpuSlot)];
