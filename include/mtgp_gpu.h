@@ -268,6 +268,20 @@ int mtgp32_gpu_pool_create(mtgp32_gpu_pool_t **out,
                            const mtgp32_params_fast_t *params, int nparams,
                            const int *param_idx, const uint32_t *seeds,
                            int count);
+/* Pools seeded by key schedules, on the device (one thread per stream):
+ * stream i = mtgp32_init_by_array(params[pidx[i]], keys + key_offsets[i],
+ * key_offsets[i+1] - key_offsets[i]) (mtgp32-fast.c:151-235), or
+ * mtgp32_init_by_str(params[pidx[i]], strs[i]) (mtgp32-fast.c:250-334, the
+ * bytes read as signed char).  key_offsets has count + 1 entries. */
+int mtgp32_gpu_pool_create_by_array(mtgp32_gpu_pool_t **out,
+                                    const mtgp32_params_fast_t *params,
+                                    int nparams, const int *param_idx,
+                                    const uint32_t *keys,
+                                    const uint64_t *key_offsets, int count);
+int mtgp32_gpu_pool_create_by_str(mtgp32_gpu_pool_t **out,
+                                  const mtgp32_params_fast_t *params,
+                                  int nparams, const int *param_idx,
+                                  const char *const *strs, int count);
 /* Substream pool: stream j = (para, seed) jumped ahead by j * step, where
  * jump_table row k (nwords words each) is X^(4^k * step) mod chi, the layout
  * of the reference's jump tables (cuda-sample/mtgp32-jump-table.h:6-13).
@@ -322,6 +336,15 @@ int mtgp64_gpu_pool_create(mtgp64_gpu_pool_t **out,
                            const mtgp64_params_fast_t *params, int nparams,
                            const int *param_idx, const uint64_t *seeds,
                            int count);
+int mtgp64_gpu_pool_create_by_array(mtgp64_gpu_pool_t **out,
+                                    const mtgp64_params_fast_t *params,
+                                    int nparams, const int *param_idx,
+                                    const uint64_t *keys,
+                                    const uint64_t *key_offsets, int count);
+int mtgp64_gpu_pool_create_by_str(mtgp64_gpu_pool_t **out,
+                                  const mtgp64_params_fast_t *params,
+                                  int nparams, const int *param_idx,
+                                  const char *const *strs, int count);
 int mtgp64_gpu_pool_create_substreams(mtgp64_gpu_pool_t **out,
                                       const mtgp64_params_fast_t *para,
                                       uint64_t seed, int count,

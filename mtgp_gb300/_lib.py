@@ -82,6 +82,8 @@ for B, P, W in ((32, P32, c_u32), (64, P64, c_u64)):
         pre + "set_window_host": (c_int, [vp, vp, c_int]),
         pre + "pool_create": (c_int, [pp, P, c_int, vp, vp, c_int]),
         pre + "pool_create_substreams": (c_int, [pp, P, W, c_int, vp, c_int, c_int, vp]),
+        pre + "pool_create_by_array": (c_int, [pp, P, c_int, vp, vp, vp, c_int]),
+        pre + "pool_create_by_str": (c_int, [pp, P, c_int, vp, vp, c_int]),
         pre + "pool_free": (None, [vp]),
         pre + "pool_size": (c_int, [vp]),
         pre + "pool_fill": (c_int, [vp, c_int, vp, c_size_t, vp]),

@@ -234,6 +234,42 @@ class Pool:
         return cls(bits, h, params_list[0].mexp)
 
     @classmethod
+    def create_by_array(cls, params_list, keys, param_idx=None):
+        """Stream i = init_by_array(params_list[param_idx[i]], keys[i]),
+        seeded on the device."""
+        bits = 32 if isinstance(params_list[0], MTGP32Params) else 64
+        P = MTGP32Params if bits == 32 else MTGP64Params
+        arr = (P * len(params_list))(*params_list)
+        dt = np.uint32 if bits == 32 else np.uint64
+        off = np.zeros(len(keys) + 1, dtype=np.uint64)
+        off[1:] = np.cumsum([len(k) for k in keys])
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(k, dtype=dt) for k in keys])
+                                    if int(off[-1]) else np.zeros(1, dt))
+        pidx = None if param_idx is None else np.ascontiguousarray(param_idx, dtype=np.int32)
+        h = ctypes.c_void_p()
+        check(getattr(lib(), "mtgp%d_gpu_pool_create_by_array" % bits)(
+            ctypes.byref(h), arr, len(params_list),
+            None if pidx is None else pidx.ctypes.data_as(ctypes.c_void_p),
+            flat.ctypes.data_as(ctypes.c_void_p), off.ctypes.data_as(ctypes.c_void_p), len(keys)))
+        return cls(bits, h, params_list[0].mexp)
+
+    @classmethod
+    def create_by_str(cls, params_list, strings, param_idx=None):
+        """Stream i = init_by_str(params_list[param_idx[i]], strings[i]) (bytes),
+        seeded on the device."""
+        bits = 32 if isinstance(params_list[0], MTGP32Params) else 64
+        P = MTGP32Params if bits == 32 else MTGP64Params
+        arr = (P * len(params_list))(*params_list)
+        strs = (ctypes.c_char_p * len(strings))(*[bytes(x) for x in strings])
+        pidx = None if param_idx is None else np.ascontiguousarray(param_idx, dtype=np.int32)
+        h = ctypes.c_void_p()
+        check(getattr(lib(), "mtgp%d_gpu_pool_create_by_str" % bits)(
+            ctypes.byref(h), arr, len(params_list),
+            None if pidx is None else pidx.ctypes.data_as(ctypes.c_void_p),
+            ctypes.cast(strs, ctypes.c_void_p), len(strings)))
+        return cls(bits, h, params_list[0].mexp)
+
+    @classmethod
     def substreams(cls, params, seed, count, table, stream=None):
         bits = 32 if isinstance(params, MTGP32Params) else 64
         t = np.ascontiguousarray(table, dtype=np.uint32)

@@ -99,61 +99,6 @@ struct Tuning {
 Tuning g_tune;
 
 // ------------------------------------------------------------------------
-// Seeding (host).  Same integer arithmetic as the reference.
-// ------------------------------------------------------------------------
-
-// Key-schedule seeding shared by init_by_array and init_by_str
-// (mtgp32-fast.c:151-235 / 250-334, mtgp64-fast.c:156-239 / 255-339).
-// `keyAt(j)` returns key word j as the reference adds it: array words
-// directly, string bytes as signed char (the reference's behaviour on
-// x86-64), so results do not depend on the host's char signedness.
-template <typename W, class Key>
-void keyed(W *a, int size, W hidden, int len, Key keyAt, W mul1, W mul2, int shr) {
-    const int lag = size >= 623 ? 11 : size >= 68 ? 7 : size >= 39 ? 5 : 3;
-    const int mid = (size - lag) / 2;
-    W b = (sizeof(W) == 8) ? (hidden >> 32) : hidden;
-    b += b >> 16;
-    b += b >> 8;
-    std::fill(a, a + size, (W)((b & 0xffu) * (W)0x0101010101010101ULL));
-    a[0] = hidden;
-    auto f1 = [&](W x) { return (W)((x ^ (x >> shr)) * mul1); };
-    auto f2 = [&](W x) { return (W)((x ^ (x >> shr)) * mul2); };
-    int total = (len + 1 > size) ? len + 1 : size;
-    W r = f1(a[0] ^ a[mid] ^ a[size - 1]);
-    a[mid] += r;
-    r += (W)len;
-    a[(mid + lag) % size] += r;
-    a[0] = r;
-    total--;
-    int i = 1, j = 0;
-    for (; j < total && j < len; j++) {
-        W t = f1(a[i] ^ a[(i + mid) % size] ^ a[(i + size - 1) % size]);
-        a[(i + mid) % size] += t;
-        t += keyAt(j, i);
-        a[(i + mid + lag) % size] += t;
-        a[i] = t;
-        i = (i + 1) % size;
-    }
-    for (; j < total; j++) {
-        W t = f1(a[i] ^ a[(i + mid) % size] ^ a[(i + size - 1) % size]);
-        a[(i + mid) % size] += t;
-        t += (W)i;
-        a[(i + mid + lag) % size] += t;
-        a[i] = t;
-        i = (i + 1) % size;
-    }
-    for (j = 0; j < size; j++) {
-        W t = f2(a[i] + a[(i + mid) % size] + a[(i + size - 1) % size]);
-        a[(i + mid) % size] ^= t;
-        t -= (W)i;
-        a[(i + mid + lag) % size] ^= t;
-        a[i] = t;
-        i = (i + 1) % size;
-    }
-    if (a[size - 1] == 0) a[size - 1] = (W)0x4d544750u;
-}
-
-// ------------------------------------------------------------------------
 // Traits of the two word sizes.
 // ------------------------------------------------------------------------
 struct T32 {
@@ -182,15 +127,13 @@ struct T32 {
                             int stride) {
         return launchSeed32(p, pi, seeds, st, n, size, stride, nullptr);
     }
-    static void byArray(const HP &p, const W *key, int len, W *a) {
-        keyed<W>(a, p.mexp / 32 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
-                 [&](int j, int i) { return (W)(key[j] + (W)i); }, 1664525u, 1566083941u, 27);
+    static cudaError_t keyed(const DP *p, const int *pi, const W *keys, const uint64_t *koff,
+                             W *st, int n, int size, int stride) {
+        return launchKeyed32(p, pi, keys, koff, st, n, size, stride, nullptr);
     }
-    static void byStr(const HP &p, const char *s, int len, W *a) {
-        keyed<W>(a, p.mexp / 32 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
-                 [&](int j, int i) { return (W)((int)(signed char)s[j] + i); }, 1664525u,
-                 1566083941u, 27);
-    }
+    // a string byte as the reference adds it to the state: a signed char
+    // (its behaviour on x86-64), whatever the host's char signedness
+    static W strKey(char c) { return (W)(int)(signed char)c; }
 };
 
 struct T64 {
@@ -217,16 +160,11 @@ struct T64 {
                             int stride) {
         return launchSeed64(p, pi, seeds, st, n, size, stride, nullptr);
     }
-    static void byArray(const HP &p, const W *key, int len, W *a) {
-        keyed<W>(a, p.mexp / 64 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
-                 [&](int j, int i) { return (W)(key[j] + (W)i); }, 2173292883993ULL,
-                 58885565329898161ULL, 59);
+    static cudaError_t keyed(const DP *p, const int *pi, const W *keys, const uint64_t *koff,
+                             W *st, int n, int size, int stride) {
+        return launchKeyed64(p, pi, keys, koff, st, n, size, stride, nullptr);
     }
-    static void byStr(const HP &p, const char *s, int len, W *a) {
-        keyed<W>(a, p.mexp / 64 + 1, (W)(p.tbl[4] ^ (p.tbl[8] << 16)), len,
-                 [&](int j, int i) { return (W)(int64_t)((int)(signed char)s[j] + i); },
-                 2173292883993ULL, 58885565329898161ULL, 59);
-    }
+    static W strKey(char c) { return (W)(int64_t)(int)(signed char)c; }
 };
 
 template <class T>
@@ -349,6 +287,30 @@ struct Pool {
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
         cudaFree(d_seeds);
         if (e != cudaSuccess) return cudaErr(e, "device seeding");
+        return MTGP_OK;
+    }
+
+    // Key-schedule seeding of every stream on the device: stream i from the
+    // key words keys[koff[i] .. koff[i+1]) (host arrays, koff: count + 1).
+    int seedKeys(const W *keys, const uint64_t *koff) {
+        const uint64_t nk = koff[count];
+        for (int i = 0; i < count; i++)
+            if (koff[i + 1] < koff[i] || koff[i + 1] - koff[i] > (uint64_t)INT32_MAX - 2)
+                return setErr(MTGP_ERR_INVALID, "bad key offsets at stream %d", i);
+        W *d_keys = nullptr;
+        uint64_t *d_off = nullptr;
+        cudaError_t e = cudaMalloc(&d_keys, sizeof(W) * (nk ? nk : 1));
+        if (e == cudaSuccess) e = cudaMalloc(&d_off, sizeof(uint64_t) * (count + 1));
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e == cudaSuccess && nk)
+            e = cudaMemcpy(d_keys, keys, sizeof(W) * nk, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(d_off, koff, sizeof(uint64_t) * (count + 1), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = T::keyed(d_params, d_pidx, d_keys, d_off, d_states, count, size, stride);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        cudaFree(d_keys);
+        cudaFree(d_off);
+        if (e != cudaSuccess) return cudaErr(e, "device key schedule");
         return MTGP_OK;
     }
 
@@ -1330,24 +1292,6 @@ int newObj(Obj **out) {
     return MTGP_OK;
 }
 
-template <class T, class Obj>
-int initSingle(Obj **out, const typename T::HP *para, const typename T::W *win) {
-    int rc = newObj(out);
-    if (rc) return rc;
-    if (!para) {
-        delete *out;
-        *out = nullptr;
-        return setErr(MTGP_ERR_INVALID, "null parameter set");
-    }
-    rc = (*out)->pool.init(para, 1, nullptr, 1);
-    if (!rc) rc = (*out)->pool.setWindows(win, (*out)->pool.size);
-    if (rc) {
-        delete *out;
-        *out = nullptr;
-    }
-    return rc;
-}
-
 // A single generator from an integer seed, seeded on the device.
 template <class T, class Obj>
 int initSeeded(Obj **out, const typename T::HP *para, typename T::W seed) {
@@ -1360,6 +1304,29 @@ int initSeeded(Obj **out, const typename T::HP *para, typename T::W seed) {
         *out = nullptr;
     }
     return rc;
+}
+
+// A single generator from a key schedule (init_by_array / init_by_str),
+// seeded on the device.
+template <class T, class Obj>
+int initKeyed(Obj **out, const typename T::HP *para, const typename T::W *keys, int len) {
+    int rc = newObj(out);
+    if (rc) return rc;
+    const uint64_t koff[2] = {0, (uint64_t)len};
+    rc = (*out)->pool.init(para, 1, nullptr, 1);
+    if (!rc) rc = (*out)->pool.seedKeys(keys, koff);
+    if (rc) {
+        delete *out;
+        *out = nullptr;
+    }
+    return rc;
+}
+
+template <class T>
+std::vector<typename T::W> strKeys(const char *str) {
+    std::vector<typename T::W> k(std::strlen(str));
+    for (size_t j = 0; j < k.size(); j++) k[j] = T::strKey(str[j]);
+    return k;
 }
 
 template <class T, class Obj>
@@ -1413,18 +1380,15 @@ int mtgp32_gpu_init_by_array(mtgp32_gpu_t **out, const mtgp32_params_fast_t *par
     Shape sh;
     int rc = checkParams<T32>(*para, &sh);
     if (rc) return rc;
-    std::vector<uint32_t> w(sh.n);
-    T32::byArray(*para, array, length, w.data());
-    return initSingle<T32>(out, para, w.data());
+    return initKeyed<T32>(out, para, array, length);
 }
 int mtgp32_gpu_init_by_str(mtgp32_gpu_t **out, const mtgp32_params_fast_t *para, const char *str) {
     if (!para || !str) return setErr(MTGP_ERR_INVALID, "bad seed string");
     Shape sh;
     int rc = checkParams<T32>(*para, &sh);
     if (rc) return rc;
-    std::vector<uint32_t> w(sh.n);
-    T32::byStr(*para, str, (int)std::strlen(str), w.data());
-    return initSingle<T32>(out, para, w.data());
+    const std::vector<uint32_t> k = strKeys<T32>(str);
+    return initKeyed<T32>(out, para, k.data(), (int)k.size());
 }
 void mtgp32_gpu_free(mtgp32_gpu_t *h) {
     if (!h) return;
@@ -1484,18 +1448,15 @@ int mtgp64_gpu_init_by_array(mtgp64_gpu_t **out, const mtgp64_params_fast_t *par
     Shape sh;
     int rc = checkParams<T64>(*para, &sh);
     if (rc) return rc;
-    std::vector<uint64_t> w(sh.n);
-    T64::byArray(*para, array, length, w.data());
-    return initSingle<T64>(out, para, w.data());
+    return initKeyed<T64>(out, para, array, length);
 }
 int mtgp64_gpu_init_by_str(mtgp64_gpu_t **out, const mtgp64_params_fast_t *para, const char *str) {
     if (!para || !str) return setErr(MTGP_ERR_INVALID, "bad seed string");
     Shape sh;
     int rc = checkParams<T64>(*para, &sh);
     if (rc) return rc;
-    std::vector<uint64_t> w(sh.n);
-    T64::byStr(*para, str, (int)std::strlen(str), w.data());
-    return initSingle<T64>(out, para, w.data());
+    const std::vector<uint64_t> k = strKeys<T64>(str);
+    return initKeyed<T64>(out, para, k.data(), (int)k.size());
 }
 void mtgp64_gpu_free(mtgp64_gpu_t *h) {
     if (!h) return;
@@ -1553,6 +1514,35 @@ int mtgp64_gpu_set_window_host(mtgp64_gpu_t *h, const uint64_t *w, int size) {
             *out = nullptr;                                                                      \
         }                                                                                        \
         return rc;                                                                               \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_create_by_array(mtgp##B##_gpu_pool_t **out,                           \
+                                           const mtgp##B##_params_fast_t *p, int np,             \
+                                           const int *pidx, const W *keys,                       \
+                                           const uint64_t *key_offsets, int count) {             \
+        if (count <= 0 || !key_offsets || (key_offsets[count] > 0 && !keys))                    \
+            return setErr(MTGP_ERR_INVALID, "bad key arrays");                                  \
+        int rc = newObj(out);                                                                    \
+        if (!rc) rc = (*out)->pool.init(p, np, pidx, count);                                     \
+        if (!rc) rc = (*out)->pool.seedKeys(keys, key_offsets);                                  \
+        if (rc && out && *out) {                                                                 \
+            delete *out;                                                                         \
+            *out = nullptr;                                                                      \
+        }                                                                                        \
+        return rc;                                                                               \
+    }                                                                                            \
+    int mtgp##B##_gpu_pool_create_by_str(mtgp##B##_gpu_pool_t **out,                             \
+                                         const mtgp##B##_params_fast_t *p, int np,               \
+                                         const int *pidx, const char *const *strs, int count) {  \
+        if (count <= 0 || !strs) return setErr(MTGP_ERR_INVALID, "bad key strings");           \
+        std::vector<W> keys;                                                                     \
+        std::vector<uint64_t> off((size_t)count + 1, 0);                                         \
+        for (int i = 0; i < count; i++) {                                                        \
+            if (!strs[i]) return setErr(MTGP_ERR_INVALID, "null key string %d", i);            \
+            for (const char *c = strs[i]; *c; c++) keys.push_back(T##B::strKey(*c));             \
+            off[(size_t)i + 1] = keys.size();                                                    \
+        }                                                                                        \
+        return mtgp##B##_gpu_pool_create_by_array(out, p, np, pidx, keys.data(), off.data(),    \
+                                                  count);                                        \
     }                                                                                            \
     int mtgp##B##_gpu_pool_create_substreams(mtgp##B##_gpu_pool_t **out,                         \
                                              const mtgp##B##_params_fast_t *p, W seed,           \

@@ -76,6 +76,14 @@ cudaError_t launchSeed32(const DevParams32 *params, const int *pidx, const uint3
                          uint32_t *states, int count, int size, int stride, cudaStream_t s);
 cudaError_t launchSeed64(const DevParams64 *params, const int *pidx, const uint64_t *seeds,
                          uint64_t *states, int count, int size, int stride, cudaStream_t s);
+// Key-schedule seeding (init_by_array / init_by_str) on the device: stream
+// i from the key words keys[koff[i] .. koff[i+1]).
+cudaError_t launchKeyed32(const DevParams32 *params, const int *pidx, const uint32_t *keys,
+                          const uint64_t *koff, uint32_t *states, int count, int size, int stride,
+                          cudaStream_t s);
+cudaError_t launchKeyed64(const DevParams64 *params, const int *pidx, const uint64_t *keys,
+                          const uint64_t *koff, uint64_t *states, int count, int size, int stride,
+                          cudaStream_t s);
 
 // One product of a jump-polynomial schedule (pow_sched.h): dst = product
 // of the nsrc sources mod chi (nsrc = 0: the polynomial 1).  tab points at
