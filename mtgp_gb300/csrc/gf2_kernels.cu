@@ -220,6 +220,26 @@ k_powops(const PowOp *__restrict__ ops, const uint32_t *__restrict__ scratch, in
     for (int w = threadIdx.x; w < W; w += kPowThreads) op.dst[w] = R[w];
 }
 
+// Table slot of X^(2^i): 256 m + 2^b for i = 8 m + b (pow_sched.h).
+__device__ __forceinline__ int pow2Slot(int i) { return (i >> 3) * 256 + (1 << (i & 7)); }
+
+// X^(2^i) for i < i0 (monomials, 2^i < D) into the zeroed tables of n sets.
+__global__ void k_monomials(uint32_t *blk, size_t tw, int W, int n, int i0) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * i0) return;
+    const int j = t / i0, i = t - j * i0;
+    const uint64_t deg = uint64_t(1) << i;
+    blk[(size_t)j * tw + (size_t)(2 + pow2Slot(i)) * W + (deg >> 5)] = 1u << (deg & 31);
+}
+
+// out[(j * 64 + i) * W ..] = the table slot X^(2^i) of set j.
+__global__ void k_gather_pow2(const uint32_t *blk, size_t tw, int W, uint32_t *out) {
+    const int j = blockIdx.x / 64, i = blockIdx.x % 64;
+    const uint32_t *src = blk + (size_t)j * tw + (size_t)(2 + pow2Slot(i)) * W;
+    uint32_t *dst = out + (size_t)blockIdx.x * W;
+    for (int w = threadIdx.x; w < W; w += blockDim.x) dst[w] = src[w];
+}
+
 constexpr size_t kPowSmemMax = 200 * 1024;
 int g_pow_window = 0;  // 0: 4 bits where the table fits, else 2
 
@@ -228,6 +248,19 @@ int g_pow_window = 0;  // 0: 4 bits where the table fits, else 2
 bool powOpsFits(int W) { return W > 0 && powSmemWords<2>(W) * 4 <= kPowSmemMax; }
 
 void setPowWindow(int bits) { g_pow_window = bits; }
+
+cudaError_t launchMonomials(uint32_t *blk, size_t tw, int W, int n, int i0, cudaStream_t s) {
+    if (n <= 0 || i0 <= 0) return cudaSuccess;
+    k_monomials<<<(n * i0 + 127) / 128, 128, 0, s>>>(blk, tw, W, n, i0);
+    return cudaGetLastError();
+}
+
+cudaError_t launchGatherPow2(const uint32_t *blk, size_t tw, int W, int n, uint32_t *out,
+                             cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_gather_pow2<<<n * 64, 128, 0, s>>>(blk, tw, W, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launchPowOps(const PowOp *ops, int n, const uint32_t *scratch, int W,
                          cudaStream_t s) {

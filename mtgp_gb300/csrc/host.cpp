@@ -127,6 +127,9 @@ struct T32 {
                             int stride) {
         return launchSeed32(p, pi, seeds, st, n, size, stride, nullptr);
     }
+    static cudaError_t bm(const W *seqs, int n2, int n, int nw, uint32_t *C, int *L) {
+        return launchBM32(seqs, n2, n, nw, C, L, nullptr);
+    }
     static cudaError_t keyed(const DP *p, const int *pi, const W *keys, const uint64_t *koff,
                              W *st, int n, int size, int stride) {
         return launchKeyed32(p, pi, keys, koff, st, n, size, stride, nullptr);
@@ -159,6 +162,9 @@ struct T64 {
     static cudaError_t seed(const DP *p, const int *pi, const W *seeds, W *st, int n, int size,
                             int stride) {
         return launchSeed64(p, pi, seeds, st, n, size, stride, nullptr);
+    }
+    static cudaError_t bm(const W *seqs, int n2, int n, int nw, uint32_t *C, int *L) {
+        return launchBM64(seqs, n2, n, nw, C, L, nullptr);
     }
     static cudaError_t keyed(const DP *p, const int *pi, const W *keys, const uint64_t *koff,
                              W *st, int n, int size, int stride) {
@@ -211,7 +217,7 @@ struct Pool {
     std::vector<PowOp> powop_scratch;
 
     ~Pool() {
-        for (auto &kv : gpow) cudaFree(kv.second);
+        for (uint32_t *b : gpow_blocks) cudaFree(b);
         cudaFree(d_params);
         cudaFree(d_pidx);
         cudaFree(d_states);
@@ -399,37 +405,65 @@ struct Pool {
         return jumpArray(i, w.data(), nw, s);
     }
 
-    // Characteristic polynomial of parameter set k: Berlekamp-Massey over
-    // the LSBs of 2*mexp outputs (mtgp32-calc-poly.cpp:36-45), which are
-    // generated on the GPU from a throw-away stream.
-    int characteristic(int k) {
-        if (chideg[k] >= 0) return MTGP_OK;
+    // Characteristic polynomials of the parameter sets `ks` not yet known, all
+    // at once: the LSBs of 2 * mexp outputs of each set from seed 1 (the kind
+    // of sequence mtgp32-calc-poly.cpp:36-45 feeds NTL's MinPolySeq),
+    // generated on the GPU by a throw-away pool, then Berlekamp-Massey on the
+    // GPU, one warp per set (bm_kernels.cu).  chi is the reciprocal of the
+    // connection polynomial.
+    int characteristics(const std::vector<int> &ks) {
+        std::vector<int> miss;
+        for (int k : ks)
+            if (chideg[k] < 0 && std::find(miss.begin(), miss.end(), k) == miss.end())
+                miss.push_back(k);
+        if (miss.empty()) return MTGP_OK;
+        const int n = (int)miss.size();
+        std::vector<typename T::HP> hp;
+        for (int k : miss) hp.push_back(hparams[k]);
         Pool<T> tmp;
-        int rc = tmp.init(&hparams[k], 1, nullptr, 1);
+        int rc = tmp.init(hp.data(), n, nullptr, n);
         if (rc) return rc;
-        W one = 1;
-        rc = tmp.seedAll(&one);
+        std::vector<W> ones((size_t)n, (W)1);
+        rc = tmp.seedAll(ones.data());
         if (rc) return rc;
-        const size_t n = 2 * (size_t)sh.mexp;
+        const size_t n2 = 2 * (size_t)sh.mexp;
+        const int nw = sh.mexp / 32 + 2;
         W *d_out = nullptr;
-        CK(cudaMalloc(&d_out, sizeof(W) * n), "cudaMalloc(bm)");
-        rc = tmp.fillAll(0, d_out, n, nullptr);
-        std::vector<W> h(n);
-        cudaError_t e = cudaMemcpy(h.data(), d_out, sizeof(W) * n, cudaMemcpyDeviceToHost);
+        uint32_t *d_C = nullptr;
+        int *d_L = nullptr;
+        cudaError_t e = cudaMalloc(&d_out, sizeof(W) * n2 * n);
+        if (e == cudaSuccess) e = cudaMalloc(&d_C, sizeof(uint32_t) * (size_t)nw * n);
+        if (e == cudaSuccess) e = cudaMalloc(&d_L, sizeof(int) * n);
+        if (e == cudaSuccess) rc = tmp.fillAll(0, d_out, n2, nullptr);
+        if (e == cudaSuccess && !rc) e = T::bm(d_out, (int)n2, n, nw, d_C, d_L);
+        std::vector<uint32_t> C((size_t)nw * n);
+        std::vector<int> L((size_t)n);
+        if (e == cudaSuccess && !rc)
+            e = cudaMemcpy(C.data(), d_C, sizeof(uint32_t) * C.size(), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && !rc)
+            e = cudaMemcpy(L.data(), d_L, sizeof(int) * n, cudaMemcpyDeviceToHost);
         cudaFree(d_out);
+        cudaFree(d_C);
+        cudaFree(d_L);
         if (rc) return rc;
-        if (e != cudaSuccess) return cudaErr(e, "download bm sequence");
-        std::vector<uint8_t> bits(n);
-        for (size_t j = 0; j < n; j++) bits[j] = (uint8_t)(h[j] & 1u);
-        gf2::Poly c;
-        int d = gf2::minpoly(bits, &c);
-        if (d != sh.mexp)
-            return setErr(MTGP_ERR_UNSUPPORTED, "characteristic polynomial has degree %d, not %d", d,
-                          sh.mexp);
-        chi[k] = c;
-        chideg[k] = d;
+        if (e != cudaSuccess) return cudaErr(e, "characteristic polynomials on the GPU");
+        for (int j = 0; j < n; j++) {
+            const int d = L[(size_t)j];
+            if (d != sh.mexp)
+                return setErr(MTGP_ERR_UNSUPPORTED,
+                              "characteristic polynomial has degree %d, not %d", d, sh.mexp);
+            const uint32_t *c = C.data() + (size_t)j * nw;
+            gf2::Poly out((size_t)d / 64 + 1, 0);
+            for (int i = 0; i <= d; i++) {  // chi_i = C_{d-i}
+                const int q = d - i;
+                if ((c[q >> 5] >> (q & 31)) & 1u) out[(size_t)i >> 6] |= 1ULL << (i & 63);
+            }
+            chi[miss[(size_t)j]] = out;
+            chideg[miss[(size_t)j]] = d;
+        }
         return MTGP_OK;
     }
+    int characteristic(int k) { return characteristics({k}); }
 
     int polyWords() const { return sh.mexp / 32 + 1; }
 
@@ -464,79 +498,152 @@ struct Pool {
         return MTGP_OK;
     }
 
-    // X^(2^i) mod chi_k for i < 64, by squaring (once per parameter set).
+    // X^(2^i) mod chi_k for i < 64 (host copies of the device table's slots).
     int ensurePow2(int k) {
         if (pow2.size() < hparams.size()) pow2.resize(hparams.size());
-        std::vector<gf2::Poly> &P2 = pow2[k];
-        if (!P2.empty()) return MTGP_OK;
-        const gf2::Modulus *M = nullptr;
-        int rc = modulus(k, &M);
-        if (rc) return rc;
-        gf2::Poly x((size_t)M->words(), 0);
-        x[0] = 2;  // X (the degree is far above 1)
-        P2.push_back(x);
-        for (int i = 1; i < 64; i++) P2.push_back(M->sqrmod(P2.back()));
-        return MTGP_OK;
+        if (!pow2[k].empty()) return MTGP_OK;
+        return prepare({k});
     }
 
     // Device tables for computing X^e mod chi_k on the GPU (pow_sched.h):
-    // chi | mu = floor(X^(2D) / chi) | slot 256 m + k = X^(k 2^(8m)) mod chi,
-    // polyWords() words each (5.8 MB for MEXP 11213), made on first use:
-    // the slots X^(2^i) come from the host's squarings, the others from
-    // 1,976 products on the GPU (seven launches, about a millisecond).
+    // chi | mu = floor(X^(2D) / chi) | slot 256m + k = X^(k 2^(8m)) mod chi,
+    // polyWords() words each (2.9 MB for MEXP 11213).  prepare() makes them
+    // for many parameter sets at once, all on the GPU:
+    //   - chi by Berlekamp-Massey (characteristics), mu by the power-series
+    //     inverse of chi's reciprocal (bm_kernels.cu), one warp per set;
+    //   - X^(2^i): monomials while 2^i < D, then one squaring per level
+    //     (products of k_powops, every set in the same launch);
+    //   - the other slots by tableSchedule (seven launches for all sets).
+    // The host keeps chi and copies of X^(2^i) (pow2) for its own paths.
     std::map<int, uint32_t *> gpow;
-    int gpuPowTables(int k, const uint32_t **out) {
-        auto hit = gpow.find(k);
-        if (hit != gpow.end()) {
-            *out = hit->second;
-            return MTGP_OK;
-        }
+    std::vector<uint32_t *> gpow_blocks;  // allocations holding the tables
+    int prepare(const std::vector<int> &ks) {
+        std::vector<int> miss;
+        for (int k : ks)
+            if (!gpow.count(k) && std::find(miss.begin(), miss.end(), k) == miss.end())
+                miss.push_back(k);
+        if (miss.empty()) return MTGP_OK;
         const int W = polyWords();
         if (!powOpsFits(W)) return setErr(MTGP_ERR_UNSUPPORTED, "polynomials too long for the GPU");
-        int rc = ensurePow2(k);
+        int rc = characteristics(miss);
         if (rc) return rc;
-        const int D = chideg[k];
-        const size_t words = (size_t)(2 + kPowSlots) * W;
-        std::vector<uint32_t> h(words, 0u);
-        auto put = [&](const gf2::Poly &p, size_t slot) {
-            const std::vector<uint32_t> w = gf2::toWords32(p, W);
-            std::copy(w.begin(), w.end(), h.begin() + (std::ptrdiff_t)(slot * W));
-        };
-        put(chi[k], 0);
-        put(gf2::divXpow(2 * D, chi[k], D), 1);
-        for (int i = 0; i < 64; i++) put(pow2[k][i], 2 + (size_t)powSlot(i / 8, 1 << (i % 8)));
-        PowSchedule sch;
-        tableSchedule(sch);
-        std::vector<PowOp> ops;
-        uint32_t *d = nullptr;
+        const int n = (int)miss.size(), D = sh.mexp;
+        const size_t TW = (size_t)(2 + kPowSlots) * W;  // words of one set's table
+        std::vector<uint32_t> h_chi((size_t)n * W);
+        for (int j = 0; j < n; j++) {
+            const std::vector<uint32_t> w = gf2::toWords32(chi[miss[(size_t)j]], W);
+            std::copy(w.begin(), w.end(), h_chi.begin() + (std::ptrdiff_t)((size_t)j * W));
+        }
+        // products: squarings X^(2^i) = (X^(2^(i-1)))^2 from the first 2^i >= D,
+        // one level each, then the byte-window table levels
+        int i0 = 0;
+        while (i0 < 64 && (uint64_t(1) << i0) < (uint64_t)D) i0++;
+        PowSchedule sq;
+        for (int i = i0 > 0 ? i0 : 1; i < 64; i++) {
+            std::vector<PowStep> lev;
+            for (int j = 0; j < n; j++) {
+                PowStep st{};
+                st.job = j;
+                st.nsrc = 2;
+                st.src[0] = st.src[1] = powSlot((i - 1) / 8, 1 << ((i - 1) % 8));
+                st.dst = powSlot(i / 8, 1 << (i % 8));
+                lev.push_back(st);
+            }
+            sq.levels.push_back(std::move(lev));
+        }
+        PowSchedule one, tabs;
+        tableSchedule(one);
+        tabs.levels.resize(one.levels.size());
+        for (size_t l = 0; l < one.levels.size(); l++)
+            for (int j = 0; j < n; j++)
+                for (PowStep st : one.levels[l]) {
+                    st.job = j;
+                    tabs.levels[l].push_back(st);
+                }
+        // host <-> device copies are plain 1D copies of contiguous staging
+        // (chi in, X^(2^i) out); the scatter and gather run on the device
+        uint32_t *blk = nullptr, *stage = nullptr;
         PowOp *d_ops = nullptr;
         cudaStream_t st = nullptr;
-        cudaError_t e = cudaMalloc(&d, sizeof(uint32_t) * words);
-        if (e == cudaSuccess) e = cudaMalloc(&d_ops, sizeof(PowOp) * (size_t)sch.steps());
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        const size_t nstage = (size_t)n * 64 * W;  // >= n * W (chi)
+        cudaError_t e = cudaMalloc(&blk, sizeof(uint32_t) * TW * n);
+        if (e == cudaSuccess) e = cudaMalloc(&stage, sizeof(uint32_t) * nstage);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d, h.data(), sizeof(uint32_t) * words, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) {
-            powOps(sch, [&](int) { return d; }, d + 2 * W, nullptr, D, ops);
+            e = cudaMalloc(&d_ops, sizeof(PowOp) * (size_t)(sq.steps() + tabs.steps()));
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMemsetAsync(blk, 0, sizeof(uint32_t) * TW * n, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(stage, h_chi.data(), sizeof(uint32_t) * h_chi.size(),
+                                cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)  // chi into word 0 of each table
+            e = cudaMemcpy2DAsync(blk, sizeof(uint32_t) * TW, stage, sizeof(uint32_t) * W,
+                                  sizeof(uint32_t) * W, n, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = launchBarrett(blk, D, n, W, TW, blk + W, st);
+        if (e == cudaSuccess) e = launchMonomials(blk, TW, W, n, i0, st);  // X^(2^i), 2^i < D
+        std::vector<PowOp> ops, more;
+        auto tab = [&](int j) { return (const uint32_t *)(blk + (size_t)j * TW); };
+        powOpsTo(sq, tab, blk + 2 * (size_t)W, TW, D, ops);
+        powOpsTo(tabs, tab, blk + 2 * (size_t)W, TW, D, more);
+        ops.insert(ops.end(), more.begin(), more.end());
+        if (e == cudaSuccess && !ops.empty())
             e = cudaMemcpyAsync(d_ops, ops.data(), sizeof(PowOp) * ops.size(),
                                 cudaMemcpyHostToDevice, st);
-        }
         size_t first = 0;
-        for (size_t l = 0; e == cudaSuccess && l < sch.levels.size(); l++) {
-            const int n = (int)sch.levels[l].size();
-            e = launchPowOps(d_ops + first, n, nullptr, W, st);
-            first += (size_t)n;
-        }
+        for (const PowSchedule *sc : {&sq, &tabs})
+            for (size_t l = 0; e == cudaSuccess && l < sc->levels.size(); l++) {
+                const int m = (int)sc->levels[l].size();
+                e = launchPowOps(d_ops + first, m, nullptr, W, st);
+                first += (size_t)m;
+            }
+        // host copies of X^(2^i)
+        std::vector<uint32_t> h_p2(nstage);
+        if (e == cudaSuccess) e = launchGatherPow2(blk, TW, W, n, stage, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h_p2.data(), stage, sizeof(uint32_t) * nstage, cudaMemcpyDeviceToHost);
         if (st) cudaStreamDestroy(st);
         cudaFree(d_ops);
+        cudaFree(stage);
         if (e != cudaSuccess) {
-            cudaFree(d);
+            cudaFree(blk);
             return cudaErr(e, "jump tables on the GPU");
         }
-        gpow[k] = d;
-        *out = d;
+        gpow_blocks.push_back(blk);
+        if (pow2.size() < hparams.size()) pow2.resize(hparams.size());
+        for (int j = 0; j < n; j++) {
+            const int k = miss[(size_t)j];
+            gpow[k] = blk + (size_t)j * TW;
+            std::vector<gf2::Poly> &P2 = pow2[k];
+            P2.assign(64, gf2::Poly());
+            for (int i = 0; i < 64; i++)
+                P2[(size_t)i] = gf2::fromWords32(h_p2.data() + ((size_t)j * 64 + i) * W, W);
+        }
         return MTGP_OK;
+    }
+    int gpuPowTables(int k, const uint32_t **out) {
+        int rc = prepare({k});
+        if (rc) return rc;
+        *out = gpow.at(k);
+        return MTGP_OK;
+    }
+
+    // Device form of a schedule whose output codes are table slots of each
+    // job's table (dst = dst_base + job * job_stride + slot * W).
+    template <class Tab>
+    void powOpsTo(const PowSchedule &sch, Tab tab, uint32_t *dst_base, size_t job_stride, int D,
+                  std::vector<PowOp> &ops) const {
+        const size_t W = (size_t)polyWords();
+        ops.clear();
+        for (const auto &lev : sch.levels)
+            for (const PowStep &st : lev) {
+                PowOp o{};
+                o.tab = tab(st.job);
+                o.dst = dst_base + (size_t)st.job * job_stride + (size_t)st.dst * W;
+                o.D = D;
+                o.nsrc = st.nsrc;
+                for (int q = 0; q < kPowMaxSrc; q++) o.src[q] = st.src[q];
+                ops.push_back(o);
+            }
     }
 
     // Device form of a schedule, level by level: table slots of tab(job),
@@ -569,6 +676,63 @@ struct Pool {
             pow_width = sms > 0 ? sms : 152;
         }
         return pow_width;
+    }
+
+    // X^steps mod chi for (parameter set, steps) pairs not yet in the host
+    // cache, computed on the GPU together (the tables of all their sets made
+    // first, in one prepare) and kept in the cache.
+    int fillCache(const std::vector<std::pair<int, uint64_t>> &want) {
+        std::vector<std::pair<int, uint64_t>> need;
+        for (const auto &q : want)
+            if (!jcache.count(q) && std::find(need.begin(), need.end(), q) == need.end())
+                need.push_back(q);
+        if (need.empty()) return MTGP_OK;
+        std::vector<int> sets;
+        for (const auto &q : need) sets.push_back(q.first);
+        int rc = prepare(sets);
+        if (rc) return rc;
+        const int W = polyWords(), n = (int)need.size();
+        std::vector<uint64_t> steps((size_t)n);
+        std::vector<const uint32_t *> tabs((size_t)n);
+        for (int j = 0; j < n; j++) {
+            steps[(size_t)j] = need[(size_t)j].second;
+            tabs[(size_t)j] = gpow.at(need[(size_t)j].first);
+        }
+        PowSchedule sch;
+        powSchedule(steps.data(), n, powWidth(), sch);
+        uint32_t *d_out = nullptr, *d_scratch = nullptr;
+        PowOp *d_ops = nullptr;
+        cudaStream_t st = nullptr;
+        cudaError_t e = cudaMalloc(&d_out, sizeof(uint32_t) * (size_t)n * W);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&d_scratch, sizeof(uint32_t) * (size_t)(sch.nscratch + 1) * W);
+        if (e == cudaSuccess) e = cudaMalloc(&d_ops, sizeof(PowOp) * (size_t)sch.steps());
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        std::vector<PowOp> ops;
+        powOps(sch, [&tabs](int j) { return tabs[(size_t)j]; }, d_out, d_scratch, sh.mexp, ops);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_ops, ops.data(), sizeof(PowOp) * ops.size(),
+                                cudaMemcpyHostToDevice, st);
+        size_t first = 0;
+        for (size_t l = 0; e == cudaSuccess && l < sch.levels.size(); l++) {
+            const int m = (int)sch.levels[l].size();
+            e = launchPowOps(d_ops + first, m, d_scratch, W, st);
+            first += (size_t)m;
+        }
+        std::vector<uint32_t> h((size_t)n * W);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(h.data(), d_out, sizeof(uint32_t) * h.size(),
+                                cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (st) cudaStreamDestroy(st);
+        cudaFree(d_out);
+        cudaFree(d_scratch);
+        cudaFree(d_ops);
+        if (e != cudaSuccess) return cudaErr(e, "jump polynomials on the GPU");
+        if (jcache.size() + need.size() > 16384) jcache.clear();
+        for (int j = 0; j < n; j++)
+            jcache[need[(size_t)j]] = gf2::fromWords32(h.data() + (size_t)j * W, W);
+        return MTGP_OK;
     }
 
     // Public form: host exponents, device output (mtgp*_gpu_pool_jump_polys).
@@ -612,14 +776,12 @@ struct Pool {
             *out = &hit->second;
             return MTGP_OK;
         }
-        const gf2::Modulus *M = nullptr;
-        int rc = modulus(k, &M);
-        if (!rc) rc = ensurePow2(k);
+        int rc = ensurePow2(k);
         if (rc) return rc;
         const std::vector<gf2::Poly> &P2 = pow2[k];
         gf2::Poly r;
         if (steps == 0) {
-            r.assign((size_t)M->words(), 0);
+            r.assign(P2[0].size(), 0);
             r[0] = 1;
         } else {
             const uint64_t low = steps & (~steps + 1);
@@ -627,11 +789,15 @@ struct Pool {
             while ((uint64_t(1) << b) != low) b++;
             if (steps == low) {
                 r = P2[b];
-            } else {
+            } else {  // a product on the host (the planner fills the cache on the GPU)
                 const gf2::Poly *rest = nullptr;
                 rc = jumpPoly(k, steps - low, &rest);
                 if (rc) return rc;
-                r = M->mulmod(*rest, P2[b]);
+                const gf2::Poly rest_copy = *rest;  // the cache may be cleared below
+                const gf2::Modulus *M = nullptr;
+                rc = modulus(k, &M);
+                if (rc) return rc;
+                r = M->mulmod(rest_copy, pow2[k][b]);
             }
         }
         if (jcache.size() >= 16384) jcache.clear();
@@ -871,6 +1037,21 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         *idx = hit->second;
         return MTGP_OK;
     };
+    // every parameter set that jumps gets its tables in one batch, and the
+    // chunk offsets not yet cached are computed together on the GPU
+    {
+        std::vector<int> sets;
+        std::vector<std::pair<int, uint64_t>> offs;
+        for (const PlanTask &pt : R.tasks) {
+            if (!pt.run && !pt.off) continue;
+            const int k = P.hpidx[pt.stream];
+            if (std::find(sets.begin(), sets.end(), k) == sets.end()) sets.push_back(k);
+            if (pt.off && __builtin_popcountll(pt.off) >= 2) offs.emplace_back(k, pt.off);
+        }
+        rc = P.prepare(sets);
+        if (!rc) rc = P.fillCache(offs);
+        if (rc) return rc;
+    }
     std::vector<BatchTask> tasks(R.tasks.size());
     for (size_t q = 0; q < R.tasks.size(); q++) {
         const PlanTask &pt = R.tasks[q];

@@ -100,7 +100,24 @@ struct PowOp {
 
 // The n independent products ops[0..n), one CTA each (W words per
 // polynomial); smem limits: powOpsFits(W).
+// Berlekamp-Massey over the LSBs of nseq sequences of n2 words (one warp
+// each): connection polynomial j (bit i = C_i) at C + j * nw, length L[j].
+cudaError_t launchBM32(const uint32_t *seqs, int n2, int nseq, int nw, uint32_t *C, int *L,
+                       cudaStream_t s);
+cudaError_t launchBM64(const uint64_t *seqs, int n2, int nseq, int nw, uint32_t *C, int *L,
+                       cudaStream_t s);
+// Barrett constants mu = floor(X^(2D) / chi) of n polynomials of degree D:
+// chi j at chi + j * stride, mu j written at mu + j * stride (nw words).
+cudaError_t launchBarrett(const uint32_t *chi, int D, int n, int nw, size_t stride, uint32_t *mu,
+                          cudaStream_t s);
+
 bool powOpsFits(int W);
+// Jump tables of n sets, tw words apart: the monomial slots X^(2^i), i <
+// i0; and a copy of the 64 slots X^(2^i) of each set into out (64 W words
+// per set).
+cudaError_t launchMonomials(uint32_t *blk, size_t tw, int W, int n, int i0, cudaStream_t s);
+cudaError_t launchGatherPow2(const uint32_t *blk, size_t tw, int W, int n, uint32_t *out,
+                             cudaStream_t s);
 void setPowWindow(int bits);  // comb window: 0 automatic, 2 or 4 bits
 cudaError_t launchPowOps(const PowOp *ops, int n, const uint32_t *scratch, int W,
                          cudaStream_t s);
