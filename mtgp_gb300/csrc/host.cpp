@@ -740,6 +740,12 @@ struct Pool {
         if (k < 0 || k >= nparams) return setErr(MTGP_ERR_INVALID, "parameter set %d out of range", k);
         if (n < 0 || (n > 0 && (!steps || !out))) return setErr(MTGP_ERR_INVALID, "bad arguments");
         if (n == 0) return MTGP_OK;
+        return gpuPolys(k, steps, n, out, s);
+    }
+
+    // X^steps[j] mod chi_k for j < n into out + j * polyWords() (device),
+    // ordered on stream s; the tables are made first if needed.
+    int gpuPolys(int k, const uint64_t *steps, int n, uint32_t *out, void *s) {
         const uint32_t *t = nullptr;
         int rc = gpuPowTables(k, &t);  // before any stream work
         if (rc) return rc;
@@ -764,6 +770,27 @@ struct Pool {
         cudaError_t f = cudaFreeAsync(d, S(s));
         if (e != cudaSuccess) return cudaErr(e, "jump polynomials");
         if (f != cudaSuccess) return cudaErr(f, "cudaFreeAsync");
+        return MTGP_OK;
+    }
+
+    // Jump stream i ahead by `steps` values: X^steps mod chi made on the GPU
+    // (a fraction of a millisecond for any 64-bit distance), then applied.
+    int jumpGpu(int i, uint64_t steps, void *s) {
+        if (i < 0 || i >= count) return setErr(MTGP_ERR_INVALID, "stream %d out of range", i);
+        const int W = polyWords();
+        int rc = ensureScratch((size_t)W, 1);
+        if (rc) return rc;
+        // The scratch buffers are reused: order this call after earlier ones.
+        CK(cudaStreamSynchronize(S(s)), "synchronize");
+        rc = gpuPolys(hpidx[i], &steps, 1, d_poly, s);
+        if (rc) return rc;
+        JumpDesc d{};
+        d.poly[0] = d_poly;
+        d.nchain = 1;
+        d.pidx = hpidx[i];
+        d.src = d.dst = (uint64_t)i * stride;
+        CK(cudaMemcpy(d_desc, &d, sizeof d, cudaMemcpyHostToDevice), "upload descriptor");
+        CK(T::jump(sh.mexp, d_params, d_states, d_desc, 1, W, S(s)), "jump");
         return MTGP_OK;
     }
 
@@ -808,6 +835,7 @@ struct Pool {
     int jumpSteps(int i, uint64_t lo, uint64_t hi, void *s) {
         if (i < 0 || i >= count) return setErr(MTGP_ERR_INVALID, "stream %d out of range", i);
         if (lo == 0 && hi == 0) return MTGP_OK;
+        if (hi == 0 && powOpsFits(polyWords())) return jumpGpu(i, lo, s);
         int k = hpidx[i];
         int rc = characteristic(k);
         if (rc) return rc;
@@ -1302,18 +1330,14 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
 }
 
 // Advance one generator by n steps: generated (and discarded) below
-// kSkipJumpMin steps, a GF(2) jump by X^n mod chi above (the polynomial from
-// the pool's cache; one jump kernel instead of n steps).
+// kSkipJumpMin steps, a GF(2) jump by X^n mod chi above (the polynomial made
+// on the GPU; a few launches instead of n steps).
 constexpr uint64_t kSkipJumpMin = uint64_t(1) << 22;
 
 template <class T>
 int skipSingle(Pool<T> &P, uint64_t n, void *s) {
     if (n < kSkipJumpMin) return P.fillOne(0, -1, nullptr, n, s);
-    const gf2::Poly *p = nullptr;
-    int rc = P.jumpPoly(P.hpidx[0], n, &p);
-    if (rc) return rc;
-    const std::vector<uint32_t> w = gf2::toWords32(*p, P.polyWords());
-    return P.jumpArray(0, w.data(), (int)w.size(), s);
+    return P.jumpGpu(0, n, s);
 }
 
 template <class Obj>

@@ -86,12 +86,14 @@ def test_jump_small_polys(gpu, orc):
             assert np.array_equal(g.window(), o.window()), (bits, k)
 
 
-@pytest.mark.parametrize("bits,table", CASES)
+@pytest.mark.parametrize("bits,table", CASES + [(32, "mtgp32_fast_44497"),
+                                                (64, "mtgp64_fast_110503")])
 def test_jump_steps_equals_skip(gpu, orc, bits, table):
-    """jump_steps builds X^s mod chi on the host (chi by Berlekamp-Massey over
-    GPU output) and jumps on the GPU."""
+    """jump_steps makes X^s mod chi on the GPU (chi by Berlekamp-Massey over
+    GPU output, then products from the byte-window tables; the 2-bit-window
+    product kernel for the longest exponent) and jumps on the GPU."""
     p = load_table(table)[0]
-    for steps in (1, 1000, 123457):
+    for steps in (1, 1000, 123457, (1 << 22) + 3):
         g = _gen(bits, p, seed=8)
         o = orc.gen(p, seed=8)
         g.jump_steps(steps)
@@ -100,8 +102,9 @@ def test_jump_steps_equals_skip(gpu, orc, bits, table):
 
 
 def test_jump_steps_large_exponent(gpu, orc):
-    """A 127-bit step count: the GPU path's X^s mod chi (host GF(2) code)
-    equals the oracle's bit-serial PowerXMod, so the windows agree exactly."""
+    """A 127-bit step count: X^s mod chi from the host GF(2) code (the
+    GPU schedules take 64-bit distances) equals the oracle's bit-serial
+    PowerXMod, so the windows agree exactly."""
     p = load_table("mtgp32_fast_11213")[0]
     steps = 3 ** 80
     assert steps < 2 ** 128
