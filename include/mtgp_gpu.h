@@ -401,7 +401,7 @@ uint64_t mtgp_gpu_plan_output_bytes(const mtgp_gpu_plan_t *plan);
 int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *plan, int64_t *tasks,
                        int64_t *chunk);
 /* The plan's configuration, the first n of: [0] tasks, [1] split chunk
- * length (0 = none), [2] generation core (1 or 4), [3] grid (0 = all
+ * length (0 = none), [2] generation core (1, 2 or 4), [3] grid (0 = all
  * resident CTAs), [4] kernels one launch runs, [5] 1 if tasks start with
  * in-kernel jumps.  Passing these to mtgp_gpu_set_tuning ("core",
  * "split_chunk" (-1 for 0), "batch_grid") makes plans of the same kind. */
@@ -412,8 +412,8 @@ int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
  *   "split_chunk"  0 = automatic, < 0 = never split, > 0 = chunk length
  *   "batch_grid"   0 = one CTA per resident slot, > 0 = that many CTAs
  *   "core"         32-bit generation core: 4 = four adjacent words per
- *                  thread (default), 1 = one word per thread; plans whose
- *                  items mix output kinds use the one-word core
+ *                  thread (default), 2 = two, 1 = one word per thread; plans
+ *                  whose items mix output kinds use the one-word core
  *   "poly_window"  bits per table window of the GPU's polynomial products
  *                  (jump polynomials): 0 = automatic (4 where the table
  *                  fits in shared memory, else 2), 2 or 4 */

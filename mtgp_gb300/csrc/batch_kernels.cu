@@ -46,10 +46,12 @@ template <> struct SplitGeo64<363> { using G = JGeo<363, 13, 256, 256, 2048>; };
 // depend on another (y of word i is word i - N + pos, and pos <= N - TN).
 template <int N, int TN> constexpr int kW4 = TN;
 
-// The same for the four-words-per-thread kernel (NT = W/4 threads).
-template <int N> struct SplitGeo32x4 { using G = void; };
-template <> struct SplitGeo32x4<351> { using G = JGeo<351, 11, 64, 64, 1024>; };
-template <> struct SplitGeo32x4<726> { using G = JGeo<726, 23, 128, 128, 2048>; };
+// The same for the K-words-per-thread kernels (NT = W/K threads).
+template <int N, int K> struct SplitGeo32xK { using G = void; };
+template <> struct SplitGeo32xK<351, 4> { using G = JGeo<351, 11, 64, 64, 1024>; };
+template <> struct SplitGeo32xK<726, 4> { using G = JGeo<726, 23, 128, 128, 2048>; };
+template <> struct SplitGeo32xK<351, 2> { using G = JGeo<351, 11, 128, 128, 1024>; };
+template <> struct SplitGeo32xK<726, 2> { using G = JGeo<726, 23, 256, 256, 4096>; };
 
 template <int N> constexpr bool kSplit32 = (N == 351 || N == 726);
 template <int N> constexpr bool kSplit64 = (N == 176 || N == 363);
@@ -157,19 +159,19 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
     }
 }
 
-// Four-words-per-thread core (W/4 threads per CTA).  SPLIT: tasks may start
-// with a jump; the jump works on the window laid out linearly, which is then
-// moved into the four planes of the generation buffer.
-template <int N, int W, int B, int MODE, bool SPLIT>
-__global__ void __launch_bounds__(W / 4, MODE == -2 ? 1 : 1280 / W * 4)
-k_batch32x4(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
+// K-words-per-thread core (W/K threads per CTA, K = 4 or 2).  SPLIT: tasks
+// may start with a jump; the jump works on the window laid out linearly,
+// which is then moved into the K planes of the generation buffer.
+template <int N, int W, int B, int MODE, bool SPLIT, int K>
+__global__ void __launch_bounds__(W / K, MODE == -2 ? 1 : 1280 * K / W)
+k_batch32xk(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
             const BatchTask *__restrict__ tasks, int ntasks,
             const BatchItem *__restrict__ items, char *__restrict__ out,
             unsigned *__restrict__ counter, uint32_t *__restrict__ stage,
             const uint32_t *__restrict__ polys, int nwords) {
-    constexpr int T = W / 4;
-    constexpr int PW = Geo4<N, W, B>::PW;
-    __shared__ __align__(16) uint32_t buf[Geo4<N, W, B>::BUF];
+    constexpr int T = W / K;
+    constexpr int PW = GeoK<N, W, B, K>::PW;
+    __shared__ __align__(16) uint32_t buf[GeoK<N, W, B, K>::BUF];
     __shared__ int s_task;
     (void)polys;
     (void)nwords;
@@ -185,7 +187,7 @@ k_batch32x4(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
         const uint32_t *src = states + (size_t)TK.stream * stateStride(N);
         bool planar = true;
         if constexpr (SPLIT && kSplit32<N>) {
-            using G = typename SplitGeo32x4<N>::G;
+            using G = typename SplitGeo32xK<N, K>::G;
             static_assert(G::NT == T, "jump geometry must use the kernel's threads");
             static_assert(G::template bytes<uint32_t>(N / 32 + 1) <= sizeof(buf),
                           "jump buffers must fit the generation buffer");
@@ -203,34 +205,34 @@ k_batch32x4(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
 #pragma unroll
                 for (int i = 0; i < PER; i++) {
                     const int k = threadIdx.x + i * T;
-                    if (k < N) buf[plane_at<PW>(k)] = v[i];
+                    if (k < N) buf[plane_at<PW, K>(k)] = v[i];
                 }
                 planar = false;
             }
         }
         if (planar)
-            for (int k = threadIdx.x; k < N; k += T) buf[plane_at<PW>(k)] = src[k];
+            for (int k = threadIdx.x; k < N; k += T) buf[plane_at<PW, K>(k)] = src[k];
         __syncthreads();
         for (int i = 0; i < TK.nitems; i++) {
             const BatchItem I = items[TK.first + i];
             char *o = out + I.out_off;
             if constexpr (MODE >= -1) {
-                using C = Core4<N, W, B, MODE>;
+                using C = CoreK<N, W, B, MODE, K>;
                 C::run(buf, L, L.otab(MODE < 0 ? 0 : MODE), I.count, (typename C::OT *)o);
             } else {
                 switch (I.kind) {
-                case 0: Core4<N, W, B, 0>::run(buf, L, L.tmp, I.count, (uint32_t *)o); break;
-                case 1: Core4<N, W, B, 1>::run(buf, L, L.flt, I.count, (float *)o); break;
-                case 2: Core4<N, W, B, 2>::run(buf, L, L.flt, I.count, (float *)o); break;
-                case 3: Core4<N, W, B, 3>::run(buf, L, L.flt, I.count, (float *)o); break;
-                case 4: Core4<N, W, B, 4>::run(buf, L, L.flt, I.count, (float *)o); break;
-                default: Core4<N, W, B, -1>::run(buf, L, L.tmp, I.count, nullptr); break;
+                case 0: CoreK<N, W, B, 0, K>::run(buf, L, L.tmp, I.count, (uint32_t *)o); break;
+                case 1: CoreK<N, W, B, 1, K>::run(buf, L, L.flt, I.count, (float *)o); break;
+                case 2: CoreK<N, W, B, 2, K>::run(buf, L, L.flt, I.count, (float *)o); break;
+                case 3: CoreK<N, W, B, 3, K>::run(buf, L, L.flt, I.count, (float *)o); break;
+                case 4: CoreK<N, W, B, 4, K>::run(buf, L, L.flt, I.count, (float *)o); break;
+                default: CoreK<N, W, B, -1, K>::run(buf, L, L.tmp, I.count, nullptr); break;
                 }
             }
         }
         uint32_t *dst = endWindow(TK, states, stage, stateStride(N));
         if (dst)
-            for (int k = threadIdx.x; k < N; k += T) dst[k] = buf[plane_at<PW>(k)];
+            for (int k = threadIdx.x; k < N; k += T) dst[k] = buf[plane_at<PW, K>(k)];
         __syncthreads();
     }
 }
@@ -365,18 +367,18 @@ static cudaError_t mode32(const BatchLaunch &b, const DevParams32 *p, uint32_t *
     }
 }
 
-template <int N, int W, int B, bool SPLIT>
-static cudaError_t mode32x4(const BatchLaunch &b, const DevParams32 *p, uint32_t *st,
+template <int N, int W, int B, bool SPLIT, int K>
+static cudaError_t mode32xk(const BatchLaunch &b, const DevParams32 *p, uint32_t *st,
                             cudaStream_t s) {
-    constexpr int T = W / 4;
+    constexpr int T = W / K;
     switch (b.mode) {
-    case -1: return go<uint32_t>(k_batch32x4<N, W, B, -1, SPLIT>, T, b, p, st, s);
-    case 0: return go<uint32_t>(k_batch32x4<N, W, B, 0, SPLIT>, T, b, p, st, s);
-    case 1: return go<uint32_t>(k_batch32x4<N, W, B, 1, SPLIT>, T, b, p, st, s);
-    case 2: return go<uint32_t>(k_batch32x4<N, W, B, 2, SPLIT>, T, b, p, st, s);
-    case 3: return go<uint32_t>(k_batch32x4<N, W, B, 3, SPLIT>, T, b, p, st, s);
-    case 4: return go<uint32_t>(k_batch32x4<N, W, B, 4, SPLIT>, T, b, p, st, s);
-    default: return go<uint32_t>(k_batch32x4<N, W, B, -2, SPLIT>, T, b, p, st, s);
+    case -1: return go<uint32_t>(k_batch32xk<N, W, B, -1, SPLIT, K>, T, b, p, st, s);
+    case 0: return go<uint32_t>(k_batch32xk<N, W, B, 0, SPLIT, K>, T, b, p, st, s);
+    case 1: return go<uint32_t>(k_batch32xk<N, W, B, 1, SPLIT, K>, T, b, p, st, s);
+    case 2: return go<uint32_t>(k_batch32xk<N, W, B, 2, SPLIT, K>, T, b, p, st, s);
+    case 3: return go<uint32_t>(k_batch32xk<N, W, B, 3, SPLIT, K>, T, b, p, st, s);
+    case 4: return go<uint32_t>(k_batch32xk<N, W, B, 4, SPLIT, K>, T, b, p, st, s);
+    default: return go<uint32_t>(k_batch32xk<N, W, B, -2, SPLIT, K>, T, b, p, st, s);
     }
 }
 
@@ -400,14 +402,18 @@ template <int N, int TN, int B>
 static cudaError_t run32x(const BatchLaunch &b, const DevParams32 *p, uint32_t *st,
                           cudaStream_t s) {
     cudaError_t e;
+    constexpr int W = kW4<N, TN>;
     if (b.split) {
         if constexpr (kSplit32<N>)
-            e = b.core == 4 ? mode32x4<N, kW4<N, TN>, B, true>(b, p, st, s)
-                            : mode32<N, TN, B, true>(b, p, st, s);
+            e = b.core == 4   ? mode32xk<N, W, B, true, 4>(b, p, st, s)
+                : b.core == 2 ? mode32xk<N, W, B, true, 2>(b, p, st, s)
+                              : mode32<N, TN, B, true>(b, p, st, s);
         else
             return cudaErrorInvalidValue;
     } else if (b.core == 4) {
-        e = mode32x4<N, kW4<N, TN>, B, false>(b, p, st, s);
+        e = mode32xk<N, W, B, false, 4>(b, p, st, s);
+    } else if (b.core == 2) {
+        e = mode32xk<N, W, B, false, 2>(b, p, st, s);
     } else {
         e = mode32<N, TN, B, false>(b, p, st, s);
     }
@@ -464,10 +470,13 @@ template <int N, int T, int B>
 static int resident32(bool split, int core) {
     int g = 0;
     const bool jumps = split && kSplit32<N>;
+    constexpr int W = kW4<N, T>;
     if (core == 4) {
-        constexpr int W = kW4<N, T>;
-        if (jumps) resident(k_batch32x4<N, W, B, 0, kSplit32<N>>, W / 4, &g);
-        else resident(k_batch32x4<N, W, B, 0, false>, W / 4, &g);
+        if (jumps) resident(k_batch32xk<N, W, B, 0, kSplit32<N>, 4>, W / 4, &g);
+        else resident(k_batch32xk<N, W, B, 0, false, 4>, W / 4, &g);
+    } else if (core == 2) {
+        if (jumps) resident(k_batch32xk<N, W, B, 0, kSplit32<N>, 2>, W / 2, &g);
+        else resident(k_batch32xk<N, W, B, 0, false, 2>, W / 2, &g);
     } else {
         if (jumps) resident(k_batch32<N, T, B, 0, kSplit32<N>>, T, &g);
         else resident(k_batch32<N, T, B, 0, false>, T, &g);

@@ -12,7 +12,7 @@ namespace mtgp {
 
 static int g_core32 = 4;
 int genCore32() { return g_core32; }
-void setGenCore32(int c) { g_core32 = (c == 1) ? 1 : 4; }
+void setGenCore32(int c) { g_core32 = (c == 1 || c == 2) ? c : 4; }
 
 bool shape32(int mexp, Shape *s) {
 #define X(M, N, T, B) \

@@ -1372,10 +1372,11 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
         int64_t chunk, grid;
     };
     std::vector<Cand> cands;
-    const int cores[2] = {4, 1};
-    for (int c = 0; c < (T::kBits == 32 ? 2 : 1); c++) cands.push_back({cores[c], -1, 0});
+    const int cores[3] = {4, 2, 1};
+    const int ncores = T::kBits == 32 ? 3 : 1;
+    for (int c = 0; c < ncores; c++) cands.push_back({cores[c], -1, 0});
     if (T::splits(P.sh.mexp))
-        for (int c = 0; c < (T::kBits == 32 ? 2 : 1); c++)
+        for (int c = 0; c < ncores; c++)
             for (int64_t ch = 1 << 17; ch <= (1 << 20); ch += 1 << 17)
                 cands.push_back({cores[c], ch, 0});
     const size_t sbytes = sizeof(W) * (size_t)P.stride * P.count;
@@ -1472,8 +1473,10 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
         const char *kern =
             T::kBits == 64 ? (b->split ? "k_batch64 (one word per thread, in-CTA jumps)"
                                        : "k_batch64 (one word per thread)")
-            : b->core == 4 ? (b->split ? "k_batch32x4 (four words per thread, in-CTA jumps)"
-                                       : "k_batch32x4 (four words per thread)")
+            : b->core == 4 ? (b->split ? "k_batch32xk<4> (four words per thread, in-CTA jumps)"
+                                       : "k_batch32xk<4> (four words per thread)")
+            : b->core == 2 ? (b->split ? "k_batch32xk<2> (two words per thread, in-CTA jumps)"
+                                       : "k_batch32xk<2> (two words per thread)")
                            : (b->split ? "k_batch32 (one word per thread, in-CTA jumps)"
                                        : "k_batch32 (one word per thread)");
         char grid[32], line[200];
@@ -1902,7 +1905,8 @@ int mtgp_gpu_set_tuning(const char *key, int64_t value) {
     if (!std::strcmp(key, "split_chunk")) {
         g_tune.split_chunk = value;
     } else if (!std::strcmp(key, "core")) {
-        if (value != 1 && value != 4) return setErr(MTGP_ERR_INVALID, "core must be 1 or 4");
+        if (value != 1 && value != 2 && value != 4)
+            return setErr(MTGP_ERR_INVALID, "core must be 1, 2 or 4");
         setGenCore32((int)value);
     } else if (!std::strcmp(key, "poly_window")) {
         if (value != 0 && value != 2 && value != 4)

@@ -130,13 +130,13 @@ def test_batch_rejects_bad_items(gpu):
 @pytest.mark.parametrize("bits,table", [(32, "mtgp32_fast_11213"), (64, "mtgp64dc_fast_11213"),
                                         (32, "mtgp32_fast_23209"), (64, "mtgp64_fast_23209")])
 @pytest.mark.parametrize("mixed", [False, True])
-@pytest.mark.parametrize("core", [4, 1])
+@pytest.mark.parametrize("core", [4, 2, 1])
 def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core):
     """Long requests split into chunks whose start states are GF(2) jumps
-    done inside the batched kernel (either 32-bit generation core): bit-exact
+    done inside the batched kernel (each 32-bit generation core): bit-exact
     outputs and final states, across two launches of the same plan."""
     from mtgp_gb300.api import Pool, set_tuning, work_items
-    if bits == 64 and core == 1:
+    if bits == 64 and core != 4:
         pytest.skip("one 64-bit core")
     tbl = load_table(table)
     rng = np.random.default_rng(bits + mixed + tbl[0].mexp)
@@ -233,3 +233,48 @@ def test_autotune_leaves_pool_and_picks_exact_plan(gpu, orc):
         o.set_window(before[j])
         a = int(offs[j]) // 4
         assert np.array_equal(got[a:a + int(counts[j])], o.fill(0, int(counts[j]))), j
+
+
+@pytest.mark.parametrize("core", [4, 2])
+@pytest.mark.parametrize("kind", [0, 1, 2, 3, 4, -1])
+def test_batch_vector_cores_one_kind(gpu, orc, core, kind):
+    """The two- and four-word cores on plans of one output kind (no split):
+    uneven counts, outputs at every 4-byte alignment (the cores' alignment
+    pre-step), a skip item, against the oracle."""
+    from mtgp_gb300.api import Pool, set_tuning, work_items
+    tbl = load_table("mtgp32_fast_11213")
+    nstreams = 20
+    plist = [tbl[i] for i in range(4)]
+    pidx = np.arange(nstreams) % 4
+    seeds = np.arange(nstreams) + 31
+    pool = Pool.create(plist, seeds, pidx)
+    rng = np.random.default_rng(core * 10 + kind)
+    counts = rng.integers(1, 9000, nstreams)
+    counts[:5] = [1, 2, 3, 255, 4097]
+    # consecutive outputs; each item starts 0..3 words after the previous one
+    gaps = rng.integers(0, 4, nstreams)
+    offs = np.zeros(nstreams, np.int64)
+    pos = 0
+    for k in range(nstreams):
+        pos += int(gaps[k])
+        offs[k] = pos * 4
+        if kind >= 0:
+            pos += int(counts[k])
+    set_tuning("core", core)
+    set_tuning("split_chunk", -1)
+    try:
+        plan = pool.plan(work_items(np.arange(nstreams), np.full(nstreams, kind), counts, offs))
+    finally:
+        set_tuning("core", 4)
+        set_tuning("split_chunk", 0)
+    assert plan.describe()["core"] == core
+    out = torch.zeros(pos + 8, dtype=torch.int32, device="cuda")
+    plan.launch(out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(np.uint8)
+    for k in range(nstreams):
+        o = orc.gen(plist[pidx[k]], seed=int(seeds[k]))
+        ref = np_bits(o.fill(max(kind, 0), int(counts[k])), 32).view(np.uint8)
+        if kind >= 0:
+            assert np.array_equal(got[offs[k]:offs[k] + ref.size], ref), k
+        assert np.array_equal(pool.windows()[k], o.window()), k
