@@ -664,16 +664,18 @@ def main():
                 "ms_per_step": round(plain_ms, 2), "launches_per_step": nsub},
             "batched_over_plain": None if plain_ms is None else round(plain_ms / ms, 2),
             "bank_batched": bank_b,
-            "bank": {"value": round(bank_gbs, 2), "unit": "GB/s", "ms": round(bank_ms, 3),
-                     "workload": "128 sets x 2^21 uint32, seeds 1234+i, one CTA per set"},
+            "bank": None if not bank_reps else {
+                "value": round(bank_gbs, 2), "unit": "GB/s", "ms": round(bank_ms, 3),
+                "workload": "128 sets x 2^21 uint32, seeds 1234+i, one CTA per set"},
             "jump_setup": {"ms": round(jump_ms, 2), "us_per_substream": round(1e3 * jump_ms / nsub, 2)},
             "plan": {"tasks": plan_tasks, "split_chunk": plan_chunk, "config": plan_cfg,
                      "autotune_ms": round(plan_ms, 1),
                      "autotune": [l for l in tune_report.strip().splitlines()]},
             "serve": serve,
             "jump_polys": polys,
-            "e2e": {"value": round(e2e, 3), "unit": "GB/s", "h2d_bytes_per_step": 32 * nsub,
-                    "d2h_bytes_per_step": total_bytes},
+            "e2e": None if not e2e_steps else {
+                "value": round(e2e, 3), "unit": "GB/s", "h2d_bytes_per_step": 32 * nsub,
+                "d2h_bytes_per_step": total_bytes},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),

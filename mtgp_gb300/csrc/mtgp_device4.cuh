@@ -31,10 +31,11 @@ template <int N, int W, int B, int K = 4>
 struct GeoK {
     static_assert(K == 2 || K == 4, "two or four words per thread");
     static constexpr int T = W / K;             // threads per generator
-    // Words per plane.  The +8 staggers the planes across shared-memory
-    // banks: copies that touch the planes at the same offset (window load,
-    // store and compaction) are then conflict-free.
-    static constexpr int PW = B / K + 8;
+    // Words per plane.  The +32/K staggers the planes across shared-memory
+    // banks: a warp's 32 consecutive window positions (window load, store
+    // and compaction) fall 32/K to a plane, so the planes' bank ranges then
+    // tile the 32 banks without overlap.
+    static constexpr int PW = B / K + 32 / K;
     static constexpr int BUF = K * PW;          // words of the shared buffer
     static constexpr int STEP = W / K;          // plane offset advance per sub-step
     static constexpr int S = (B - N - (K - 1)) / W;  // sub-steps per segment
