@@ -15,8 +15,9 @@
 //   - each chunk's taps are split over the warps; lane l of a warp owns R
 //     consecutive outputs and slides an R-word register window along seq,
 //     so a tap costs one shared load and, when its coefficient is set, R
-//     XORs (the coefficient is the same for a whole warp, so a zero tap is a
-//     uniform branch past them);
+//     XORs; taps go in pairs (tapsR): the coefficients are the same for a
+//     whole warp, so a pair is one uniform branch, a zero pair skips its
+//     XORs and a pair of ones costs R three-input XORs;
 //   - the warps' partial sums are combined with shared-memory atomicXor.
 // A chain of polynomials is applied in order.
 #pragma once
@@ -70,6 +71,50 @@ struct JGeo {
         return sizeof(W) * (size_t)(2 * NJ + RING) + sizeof(uint32_t) * (size_t)(nwords + PAD);
     }
 };
+
+// R taps p .. p+R-1 against the lane's R outputs: win holds seq[p + l0 ..
+// + R) on entry (l0 folded into base = p + l0) and the next R words on exit.
+// Taps go in pairs: the pair's coefficients are the same for the whole
+// warp, so each pair takes one uniform branch, and a pair with both
+// coefficients set costs R three-input XORs instead of 2R (on random
+// polynomials 0.75 R operations per pair on average instead of R).
+template <class Tr, class Geo>
+__device__ __forceinline__ void tapsR(typename Tr::W (&acc)[Geo::R], typename Tr::W (&win)[Geo::R],
+                                      const typename Tr::W *ring, uint32_t bits_lo,
+                                      uint32_t bits_hi, int base) {
+    constexpr int R = Geo::R;
+    constexpr uint32_t M = Geo::RING - 1;
+#pragma unroll
+    for (int j = 0; j < R; j += 2) {  // j even: a pair never straddles bit 31
+        const uint32_t bj = j < 32 ? bits_lo : bits_hi;
+        if (j + 1 < R) {
+            // tap j reads seq[base + j .. + R) = win[(j + r) % R]; tap j + 1
+            // reads seq[base + j + 1 .. + R), whose last word is the one that
+            // replaces win[j]
+            const typename Tr::W next = ring[(uint32_t)(base + R + j) & M];
+            auto w1 = [&](int r) { return r < R - 1 ? win[(j + 1 + r) % R] : next; };
+            const uint32_t b2 = (bj >> (j & 31)) & 3u;
+            if (b2 == 3u) {
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] ^= win[(j + r) % R] ^ w1(r);
+            } else if (b2 == 1u) {
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] ^= win[(j + r) % R];
+            } else if (b2 == 2u) {
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] ^= w1(r);
+            }
+            win[j] = next;
+            win[j + 1] = ring[(uint32_t)(base + R + j + 1) & M];
+        } else {  // the last tap of an odd R, on its own
+            if ((bj >> (j & 31)) & 1u) {
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] ^= win[(j + r) % R];
+            }
+            win[j] = ring[(uint32_t)(base + R + j) & M];
+        }
+    }
+}
 
 // Jump the window jin[0..N) in place by chain[0], chain[1], ... (uint32-array
 // polynomials of nwords words).  smem must hold Geo::bytes<W>(nwords) bytes
@@ -128,17 +173,7 @@ __device__ __forceinline__ void jump_chain_impl(typename Tr::W *smem, const type
                     const uint32_t bits_hi =
                         R > 32 ? __funnelshift_r(poly[(p >> 5) + 1], poly[(p >> 5) + 2], p & 31)
                                : 0u;
-#pragma unroll
-                    for (int j = 0; j < R; j++) {
-                        const uint32_t bj = j < 32 ? bits_lo : bits_hi;
-                        // the tap's coefficient is the same for the whole warp:
-                        // a zero skips the R XORs instead of masking them
-                        if ((bj >> (j & 31)) & 1u) {
-#pragma unroll
-                            for (int r = 0; r < R; r++) acc[r] ^= win[(j + r) % R];
-                        }
-                        win[j] = ring[(uint32_t)(p + l0 + R + j) & M];
-                    }
+                    tapsR<Tr, Geo>(acc, win, ring, bits_lo, bits_hi, p + l0);
                 }
                 __syncthreads();
             }
@@ -215,17 +250,7 @@ __device__ void jump_part(typename Tr::W *smem, const typename Tr::Lane &L, cons
                     const uint32_t bits_hi =
                         R > 32 ? __funnelshift_r(poly[(p >> 5) + 1], poly[(p >> 5) + 2], p & 31)
                                : 0u;
-#pragma unroll
-                    for (int j = 0; j < R; j++) {
-                        const uint32_t bj = j < 32 ? bits_lo : bits_hi;
-                        // the tap's coefficient is the same for the whole warp:
-                        // a zero skips the R XORs instead of masking them
-                        if ((bj >> (j & 31)) & 1u) {
-#pragma unroll
-                            for (int r = 0; r < R; r++) acc[r] ^= win[(j + r) % R];
-                        }
-                        win[j] = ring[(uint32_t)(p + l0 + R + j) & M];
-                    }
+                    tapsR<Tr, Geo>(acc, win, ring, bits_lo, bits_hi, p + l0);
                 }
             }
             __syncthreads();
