@@ -48,9 +48,12 @@ int planCore(const mtgp_work_item_t *items, int nitems, const PlanOptions &o, Pl
     r->mode = -1;
     if (nitems < 0 || (nitems > 0 && !items))
         return fail(err, MTGP_ERR_INVALID, "bad item list (%d items)", nitems);
-    // stable counting sort of the items by stream
-    std::vector<int> order;
-    std::vector<int32_t> head((size_t)o.nstreams + 1, 0);
+    // the items with work, grouped by stream in item order: keys (stream <<
+    // 32 | item) sorted, so the cost follows the items, not the streams
+    // (buffers are reused across calls of a thread: a server plans every
+    // batch)
+    thread_local std::vector<uint64_t> keys;
+    keys.clear();
     for (int k = 0; k < nitems; k++) {
         const mtgp_work_item_t &it = items[k];
         if (it.stream >= (uint32_t)o.nstreams)
@@ -66,29 +69,35 @@ int planCore(const mtgp_work_item_t *items, int nitems, const PlanOptions &o, Pl
                 return fail(err, MTGP_ERR_INVALID, "item %d: output range overflows", k);
         }
         if (it.count == 0 && it.skip == 0) continue;
-        head[it.stream + 1]++;
+        keys.push_back((uint64_t)it.stream << 32 | (uint32_t)k);
     }
-    for (int s = 0; s < o.nstreams; s++) head[s + 1] += head[s];
-    order.resize((size_t)head[o.nstreams]);
-    {
-        std::vector<int32_t> fill(head.begin(), head.end() - 1);
-        for (int k = 0; k < nitems; k++) {
-            const mtgp_work_item_t &it = items[k];
-            if (it.count == 0 && it.skip == 0) continue;
-            order[(size_t)fill[it.stream]++] = k;
-        }
+    if (keys.size() * 8 < (size_t)o.nstreams) {
+        std::sort(keys.begin(), keys.end());
+    } else {  // many items: a counting sort by stream (stable)
+        thread_local std::vector<int32_t> head;
+        thread_local std::vector<uint64_t> by;
+        head.assign((size_t)o.nstreams + 1, 0);
+        for (uint64_t key : keys) head[(key >> 32) + 1]++;
+        for (int st = 0; st < o.nstreams; st++) head[st + 1] += head[st];
+        by.resize(keys.size());
+        for (uint64_t key : keys) by[(size_t)head[key >> 32]++] = key;
+        keys.swap(by);
     }
     // runs, and the generated segments of each run
-    std::vector<Run> runs;
-    std::vector<PlanSeg> rseg;
-    rseg.reserve(order.size() + 8);
+    thread_local std::vector<Run> runs;
+    thread_local std::vector<PlanSeg> rseg;
+    runs.clear();
+    rseg.clear();
+    rseg.reserve(keys.size() + 8);
     uint64_t grand = 0;
-    for (int s = 0; s < o.nstreams; s++) {
-        if (head[s] == head[s + 1]) continue;
+    for (size_t q0 = 0, q1; q0 < keys.size(); q0 = q1) {
+        const int s = (int)(keys[q0] >> 32);
+        for (q1 = q0; q1 < keys.size() && (int)(keys[q1] >> 32) == s; q1++) {
+        }
         Run cur{s, 0, 0, (uint32_t)rseg.size(), 0};
         uint64_t pos = 0;
-        for (int32_t q = head[s]; q < head[s + 1]; q++) {
-            const int k = order[(size_t)q];
+        for (size_t q = q0; q < q1; q++) {
+            const int k = (int)(uint32_t)keys[q];
             const mtgp_work_item_t &it = items[k];
             uint64_t skip = it.skip, count = it.count;
             if (it.kind < 0) {  // advance only: all of it is a skip
@@ -209,8 +218,16 @@ int planCore(const mtgp_work_item_t *items, int nitems, const PlanOptions &o, Pl
     auto cost = [jw](const PlanTask &t) {
         return t.total + jw * ((t.run ? 1u : 0u) + (t.off ? 1u : 0u));
     };
-    std::stable_sort(r->tasks.begin(), r->tasks.end(),
-                     [&cost](const PlanTask &a, const PlanTask &b) { return cost(a) > cost(b); });
+    // by (cost descending, position): a stable order, sorted as plain pairs
+    thread_local std::vector<std::pair<uint64_t, uint32_t>> ord;
+    thread_local std::vector<PlanTask> sorted;
+    ord.resize(r->tasks.size());
+    for (size_t q = 0; q < r->tasks.size(); q++)
+        ord[q] = {~cost(r->tasks[q]), (uint32_t)q};
+    std::sort(ord.begin(), ord.end());
+    sorted.resize(r->tasks.size());
+    for (size_t q = 0; q < ord.size(); q++) sorted[q] = r->tasks[ord[q].second];
+    r->tasks.swap(sorted);
     int mode = -3;
     for (const PlanSeg &g : r->segs)
         if (g.count) mode = (mode == -3 || mode == g.kind) ? g.kind : -2;
