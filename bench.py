@@ -247,7 +247,7 @@ def run_serving(args, s, local):
     b = Pool.substreams(p64, SEED, 256, jump_table(64), stream=s)
     s.synchronize()
     win_a, win_b = a.windows(), b.windows()
-    srv = Server(a, b, budget_bytes=8 << 30, slots=4, max_batch=8192)
+    srv = Server(a, b, budget_bytes=8 << 30, slots=args.serve_slots, max_batch=8192)
     # check trace: every response kept for the bit-exact check on the CPU
     rng = np.random.default_rng(7)
     pool, stream, kind, count, skip = serve_trace(rng, 256)
@@ -277,7 +277,7 @@ def run_serving(args, s, local):
     for n in (2000, args.serve_burst):
         run(serve_trace(rng, n), np.zeros(n))
     run(serve_trace(rng, 20000), np.cumsum(rng.exponential(1e-6, 20000)))
-    out = {"workload": SERVE_WORKLOAD, "slots": 4, "max_batch": 8192,
+    out = {"workload": SERVE_WORKLOAD, "slots": args.serve_slots, "max_batch": 8192,
            "latency": "submission to the result resident in device memory"}
     with Clocks(local) as clk:
         n = args.serve_burst
@@ -419,6 +419,8 @@ def main():
     ap.add_argument("--serve-burst", type=int, default=100000,
                     help="requests of the burst that finds the saturation rate")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-slots", type=int, default=8,
+                    help="batches the server keeps in flight (CUDA streams)")
     ap.add_argument("--uniform", type=int, default=0,
                     help="profiling runs: every substream requests this many values "
                          "(steady-state throughput instead of the lognormal workload)")
