@@ -218,6 +218,7 @@ struct Pool {
 
     ~Pool() {
         for (uint32_t *b : gpow_blocks) cudaFree(b);
+        if (cache_stream) cudaStreamDestroy(cache_stream);
         cudaFree(d_params);
         cudaFree(d_pidx);
         cudaFree(d_states);
@@ -517,6 +518,7 @@ struct Pool {
     // The host keeps chi and copies of X^(2^i) (pow2) for its own paths.
     std::map<int, uint32_t *> gpow;
     std::vector<uint32_t *> gpow_blocks;  // allocations holding the tables
+    cudaStream_t cache_stream = nullptr;   // fillCache's products
     int prepare(const std::vector<int> &ks) {
         std::vector<int> miss;
         for (int k : ks)
@@ -700,34 +702,38 @@ struct Pool {
         }
         PowSchedule sch;
         powSchedule(steps.data(), n, powWidth(), sch);
-        uint32_t *d_out = nullptr, *d_scratch = nullptr;
-        PowOp *d_ops = nullptr;
-        cudaStream_t st = nullptr;
-        cudaError_t e = cudaMalloc(&d_out, sizeof(uint32_t) * (size_t)n * W);
-        if (e == cudaSuccess)
-            e = cudaMalloc(&d_scratch, sizeof(uint32_t) * (size_t)(sch.nscratch + 1) * W);
-        if (e == cudaSuccess) e = cudaMalloc(&d_ops, sizeof(PowOp) * (size_t)sch.steps());
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        // the pool's own stream and stream-ordered allocations: no
+        // device-wide synchronization (a cudaFree would wait for every batch
+        // in flight), the host waits only for these products
+        if (!cache_stream) CK(cudaStreamCreateWithFlags(&cache_stream, cudaStreamNonBlocking),
+                              "cudaStreamCreate(cache)");
+        const size_t out_bytes = sizeof(uint32_t) * (size_t)n * W;
+        const size_t ops_bytes = (sizeof(PowOp) * (size_t)sch.steps() + 255) & ~size_t(255);
+        const size_t bytes = ((out_bytes + 255) & ~size_t(255)) + ops_bytes +
+                             sizeof(uint32_t) * (size_t)sch.nscratch * W;
+        unsigned char *d = nullptr;
+        CK(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, cache_stream),
+           "cudaMallocAsync(cache products)");
+        uint32_t *d_out = reinterpret_cast<uint32_t *>(d);
+        PowOp *d_ops = reinterpret_cast<PowOp *>(d + ((out_bytes + 255) & ~size_t(255)));
+        uint32_t *d_scratch = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(d_ops) +
+                                                           ops_bytes);
         std::vector<PowOp> ops;
         powOps(sch, [&tabs](int j) { return tabs[(size_t)j]; }, d_out, d_scratch, sh.mexp, ops);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_ops, ops.data(), sizeof(PowOp) * ops.size(),
-                                cudaMemcpyHostToDevice, st);
+        cudaError_t e = cudaMemcpyAsync(d_ops, ops.data(), sizeof(PowOp) * ops.size(),
+                                        cudaMemcpyHostToDevice, cache_stream);
         size_t first = 0;
         for (size_t l = 0; e == cudaSuccess && l < sch.levels.size(); l++) {
             const int m = (int)sch.levels[l].size();
-            e = launchPowOps(d_ops + first, m, d_scratch, W, st);
+            e = launchPowOps(d_ops + first, m, d_scratch, W, cache_stream);
             first += (size_t)m;
         }
         std::vector<uint32_t> h((size_t)n * W);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(h.data(), d_out, sizeof(uint32_t) * h.size(),
-                                cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (st) cudaStreamDestroy(st);
-        cudaFree(d_out);
-        cudaFree(d_scratch);
-        cudaFree(d_ops);
+            e = cudaMemcpyAsync(h.data(), d_out, out_bytes, cudaMemcpyDeviceToHost, cache_stream);
+        cudaError_t f = cudaFreeAsync(d, cache_stream);
+        if (e == cudaSuccess) e = f;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(cache_stream);
         if (e != cudaSuccess) return cudaErr(e, "jump polynomials on the GPU");
         if (jcache.size() + need.size() > 16384) jcache.clear();
         for (int j = 0; j < n; j++)
@@ -1245,11 +1251,16 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     Pool<T> &P = *static_cast<Pool<T> *>(pl->pool);
     if (pl->ntasks == 0) return MTGP_OK;
     if (pl->out_bytes && !out) return setErr(MTGP_ERR_INVALID, "null output pointer");
+    // the GPU-made jump polynomials live in the blob after the host-made
+    // ones: they are computed on the launch that uploads the blob (which
+    // overwrites them) and stay valid for the plan's later launches
+    const bool fresh = pl->dirty;
     int rc = uploadPlan(pl, s);
     if (rc) return rc;
     const size_t pw = (size_t)P.polyWords();
     size_t first = 0;
     for (int n : pl->pow_levels) {
+        if (!fresh) break;
         CK(launchPowOps(pl->d_powops + first, n, pl->d_pscratch, (int)pw, S(s)),
            "jump polynomials");
         first += (size_t)n;

@@ -71,8 +71,11 @@ struct mtgp_server {
     std::thread th;
     std::atomic<bool> stop{false};
     uint64_t submitted = 0, completed = 0, bytes_done = 0, batches = 0;
-    std::vector<double> latency;  // seconds, by ticket - 1; -1 = not done
-    std::vector<int> status;      // MTGP_* by ticket - 1
+    // seconds and MTGP_* status by ticket - 1 (latency -1 = not done); deques,
+    // so that millions of tickets never make a submit (under the lock the
+    // scheduler needs) copy the whole history to grow
+    std::deque<double> latency;
+    std::deque<int> status;
     std::map<uint64_t, std::pair<uint64_t, uint64_t>> kept;  // ticket -> (offset, bytes)
     // scheduler time (s): admission, planning + launch, retiring, idle waits
     double prof[4] = {0, 0, 0, 0};
