@@ -968,6 +968,7 @@ struct mtgp_gpu_plan {
     // host-computed ones: the product levels of pow_sched.h (steps per
     // level, one launch each), their scratch polynomials kept and grown
     std::vector<int> pow_levels;
+    bool pow_ready = true;  // false from an upload until the products have run
     const PowOp *d_powops = nullptr;
     uint32_t *d_pscratch = nullptr;
     size_t cap_pscratch = 0;
@@ -1243,6 +1244,21 @@ int uploadPlan(mtgp_gpu_plan *pl, void *s) {
     CK(cudaMemcpyAsync(pl->d_blob, pl->h_blob, pl->blob_bytes, cudaMemcpyHostToDevice, S(s)),
        "upload plan");
     pl->dirty = false;
+    pl->pow_ready = pl->pow_levels.empty();  // the upload overwrote the GPU-made polynomials
+    return MTGP_OK;
+}
+
+// The plan's GPU-made jump polynomials (after the host-made ones in the
+// blob), on s after the upload; they stay valid for later launches until
+// the plan is refilled.
+int powJobs(mtgp_gpu_plan *pl, int pw, void *s) {
+    if (pl->pow_ready) return MTGP_OK;
+    size_t first = 0;
+    for (int n : pl->pow_levels) {
+        CK(launchPowOps(pl->d_powops + first, n, pl->d_pscratch, pw, S(s)), "jump polynomials");
+        first += (size_t)n;
+    }
+    pl->pow_ready = true;
     return MTGP_OK;
 }
 
@@ -1251,20 +1267,9 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     Pool<T> &P = *static_cast<Pool<T> *>(pl->pool);
     if (pl->ntasks == 0) return MTGP_OK;
     if (pl->out_bytes && !out) return setErr(MTGP_ERR_INVALID, "null output pointer");
-    // the GPU-made jump polynomials live in the blob after the host-made
-    // ones: they are computed on the launch that uploads the blob (which
-    // overwrites them) and stay valid for the plan's later launches
-    const bool fresh = pl->dirty;
     int rc = uploadPlan(pl, s);
+    if (!rc) rc = powJobs(pl, P.polyWords(), s);
     if (rc) return rc;
-    const size_t pw = (size_t)P.polyWords();
-    size_t first = 0;
-    for (int n : pl->pow_levels) {
-        if (!fresh) break;
-        CK(launchPowOps(pl->d_powops + first, n, pl->d_pscratch, (int)pw, S(s)),
-           "jump polynomials");
-        first += (size_t)n;
-    }
     BatchLaunch b{};
     b.mexp = P.sh.mexp;
     b.mode = pl->mode;
@@ -1875,7 +1880,14 @@ int mtgp_gpu_plan_graph_launch(mtgp_gpu_plan_t *pl, void *out, void *s) {
             pl->exec = nullptr;
         }
         cudaGraph_t g = nullptr;
-        int up = uploadPlan(pl, s);  // before the capture: replays reuse the descriptors
+        // before the capture: replays reuse the descriptors and the GPU-made
+        // jump polynomials
+        int up = uploadPlan(pl, s);
+        if (!up) {
+            const int pw = pl->bits == 32 ? static_cast<Pool<T32> *>(pl->pool)->polyWords()
+                                          : static_cast<Pool<T64> *>(pl->pool)->polyWords();
+            up = powJobs(pl, pw, s);
+        }
         if (up) return up;
         CK(cudaStreamBeginCapture(S(s), cudaStreamCaptureModeThreadLocal), "begin capture");
         int rc = planLaunch(pl, out, s);

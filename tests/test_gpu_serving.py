@@ -342,3 +342,46 @@ def test_arbitrary_skips_use_gpu_polynomials(gpu, orc, bits, table):
             gens[s].jump_words(orc.powxmod(skips[s], chi, d).view(np.uint32)[:nw])
             ref = np_bits(gens[s].fill(0, counts[s]), bits).view(np.uint8)
             assert np.array_equal(got[offs[s]:offs[s] + ref.size], ref), (rep, s)
+
+
+def test_gpu_polynomials_with_graph_and_refill(gpu, orc):
+    """A plan whose run starts are made on the GPU, launched first through a
+    CUDA graph (the products run before the capture, the replays reuse
+    them), then refilled with other skips and launched plainly: every
+    output matches the oracle."""
+    from mtgp_gb300.api import work_items
+    bits, table = 32, "mtgp32_fast_11213"
+    pool, plist, pidx, seeds = _pool(bits, table, 6, seed0=300)
+    gens = [orc.gen(plist[pidx[s]], seed=int(seeds[s])) for s in range(6)]
+    chis = {}
+    nw = plist[0].mexp // 32 + 1
+
+    def check(skips, counts, out):
+        offs = list(np.concatenate([[0], np.cumsum(counts)[:-1]]) * 4)
+        got = out.cpu().numpy().view(np.uint8)
+        for s in range(6):
+            p = plist[pidx[s]]
+            if s % 3 not in chis:
+                seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
+                chis[s % 3] = orc.minpoly((seq & 1).astype(np.uint8))
+            d, chi = chis[s % 3]
+            gens[s].jump_words(orc.powxmod(skips[s], chi, d).view(np.uint32)[:nw])
+            ref = gens[s].fill(0, counts[s]).view(np.uint8)
+            assert np.array_equal(got[offs[s]:offs[s] + ref.size], ref), (skips[s], s)
+
+    rng = np.random.default_rng(12)
+    skips = [int(x) for x in rng.integers(1 << 17, 1 << 45, 6, dtype=np.int64)]
+    counts = [777 + 100 * k for k in range(6)]
+    offs = list(np.concatenate([[0], np.cumsum(counts)[:-1]]) * 4)
+    plan = pool.plan(work_items(list(range(6)), [0] * 6, counts, offs, skips))
+    out = torch.zeros(sum(counts) + 8, dtype=torch.int32, device="cuda")
+    s = torch.cuda.Stream()
+    for rep in range(2):
+        plan.graph_launch(out, s)
+        s.synchronize()
+        check(skips, counts, out)
+    skips2 = [int(x) for x in rng.integers(1 << 17, 1 << 45, 6, dtype=np.int64)]
+    pool.replan(work_items(list(range(6)), [0] * 6, counts, offs, skips2), plan)
+    plan.launch(out, s)
+    s.synchronize()
+    check(skips2, counts, out)
