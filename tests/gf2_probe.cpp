@@ -112,3 +112,83 @@ extern "C" int probe_pow_schedule(const uint64_t *m, int dm, const uint64_t *e, 
     shape[2] = s.nscratch;
     return 0;
 }
+
+// The GPU kernels' formulations (bm_kernels.cu), restated serially with the
+// same 32-bit word layout:
+//   probe_bm_reversed: Berlekamp-Massey where the discrepancy at step N is
+//     the parity of C AND (R >> (n2 - 1 - N)), R the bit-reversed sequence;
+//     out = chi (the reciprocal of C) in 64-bit words, returns L;
+//   probe_barrett_series: mu = floor(X^(2D) / chi) as the power series
+//     1 / C(x) to D + 1 terms stored reversed.
+namespace {
+uint32_t wordAt(const std::vector<uint32_t> &v, long w) {
+    return (w >= 0 && w < (long)v.size()) ? v[(size_t)w] : 0u;
+}
+uint32_t shr32(const std::vector<uint32_t> &v, long w, long sh) {
+    const long q = w + (sh >> 5);
+    const int b = (int)(sh & 31);
+    const uint64_t lo = wordAt(v, q), hi = wordAt(v, q + 1);
+    return (uint32_t)(((hi << 32) | lo) >> b);
+}
+uint32_t shl32(const std::vector<uint32_t> &v, long w, long sh) {
+    const long q = w - (sh >> 5);
+    const int b = (int)(sh & 31);
+    const uint64_t lo = wordAt(v, q - 1), hi = wordAt(v, q);
+    return (uint32_t)((((hi << 32) | lo) << b) >> 32);
+}
+}  // namespace
+
+extern "C" int probe_bm_reversed(const uint8_t *s, int n2, uint64_t *chi_out) {
+    const int nr = (n2 + 31) / 32 + 2, nw = n2 / 64 + 2;
+    std::vector<uint32_t> R((size_t)nr, 0), C((size_t)nw, 0), B((size_t)nw, 0), T((size_t)nw, 0);
+    for (int k = 0; k < n2; k++)
+        if (s[n2 - 1 - k] & 1) R[(size_t)k >> 5] |= 1u << (k & 31);
+    C[0] = B[0] = 1;
+    int L = 0, m = -1;
+    for (int N = 0; N < n2; N++) {
+        const int base = n2 - 1 - N, lw = L / 32 + 1;
+        uint32_t acc = 0;
+        for (int w = 0; w < lw; w++) acc ^= C[(size_t)w] & shr32(R, w, base);
+        if (!(__builtin_popcount(acc) & 1)) continue;
+        const int sh = N - m;
+        const bool grow = 2 * L <= N;
+        const int nl = grow ? N + 1 - L : L, top = (nl > L ? nl : L) / 32 + 1;
+        if (grow) {
+            for (int w = 0; w < nw; w++)
+                T[(size_t)w] = w < top ? C[(size_t)w] ^ shl32(B, w, sh) : 0u;
+            std::swap(B, C);   // B = old C
+            std::swap(C, T);   // C = new
+            L = nl;
+            m = N;
+        } else {
+            std::vector<uint32_t> add((size_t)top);
+            for (int w = 0; w < top && w < nw; w++) add[(size_t)w] = shl32(B, w, sh);
+            for (int w = 0; w < top && w < nw; w++) C[(size_t)w] ^= add[(size_t)w];
+        }
+    }
+    for (int i = 0; i <= L; i++) {
+        const int q = L - i;
+        if ((C[(size_t)q >> 5] >> (q & 31)) & 1u) chi_out[i >> 6] |= 1ULL << (i & 63);
+    }
+    return L;
+}
+
+extern "C" int probe_barrett_series(const uint64_t *m, int D, uint64_t *mu_out) {
+    const int nw = D / 32 + 1;
+    std::vector<uint32_t> chi((size_t)nw, 0), Cp((size_t)nw, 0), Z((size_t)nw + 2, 0);
+    for (int i = 0; i <= D; i++)
+        if ((m[i >> 6] >> (i & 63)) & 1u) chi[(size_t)i >> 5] |= 1u << (i & 31);
+    for (int i = 0; i < D; i++)  // C' bit i = C_{i+1} = chi_{D-1-i}
+        if ((chi[(size_t)(D - 1 - i) >> 5] >> ((D - 1 - i) & 31)) & 1u)
+            Cp[(size_t)i >> 5] |= 1u << (i & 31);
+    Z[(size_t)D >> 5] |= 1u << (D & 31);
+    for (int k = 1; k <= D; k++) {
+        const int base = D - k + 1, lw = (k - 1) / 32 + 1;
+        uint32_t acc = 0;
+        for (int w = 0; w < lw; w++) acc ^= Cp[(size_t)w] & shr32(Z, w, base);
+        if (__builtin_popcount(acc) & 1) Z[(size_t)(D - k) >> 5] |= 1u << ((D - k) & 31);
+    }
+    for (int i = 0; i <= D; i++)
+        if ((Z[(size_t)i >> 5] >> (i & 31)) & 1u) mu_out[i >> 6] |= 1ULL << (i & 63);
+    return 0;
+}

@@ -129,3 +129,27 @@ def test_pow_schedules_match_oracle(orc, probe):
             assert levels == 3 and nscratch > 0
         else:
             assert levels == 1 and steps == len(exps) and nscratch == 0
+
+
+@pytest.mark.parametrize("table", ["mtgp32_fast_11213", "mtgp64dc_fast_11213"])
+def test_gpu_formulations_of_bm_and_barrett(orc, probe, table):
+    """The formulations of the GPU's Berlekamp-Massey (bit-reversed sequence,
+    discrepancy as the parity of a shifted window) and Barrett constant
+    (power-series inverse of chi's reciprocal), restated serially: the
+    oracle's characteristic polynomial, and the host's floor(X^(2d)/chi)."""
+    vp = ctypes.c_void_p
+    probe.probe_bm_reversed.argtypes = [vp, ctypes.c_int, vp]
+    probe.probe_barrett_series.argtypes = [vp, ctypes.c_int, vp]
+    probe.probe_divxpow.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp]
+    p = load_table(table)[2]
+    seq = (orc.gen(p, seed=1).fill(0, 2 * p.mexp) & 1).astype(np.uint8)
+    d, chi = orc.minpoly(seq)
+    out = np.zeros(len(chi) + 2, dtype=np.uint64)
+    assert probe.probe_bm_reversed(_p(seq), len(seq), _p(out)) == d
+    assert np.array_equal(out[:d // 64 + 1], chi[:d // 64 + 1])
+    m = np.ascontiguousarray(chi[:d // 64 + 1])
+    mu = np.zeros(d // 64 + 2, dtype=np.uint64)
+    probe.probe_barrett_series(_p(m), d, _p(mu))
+    ref = np.zeros(d // 64 + 2, dtype=np.uint64)
+    nq = probe.probe_divxpow(_p(m), d, 2 * d, _p(ref))
+    assert np.array_equal(mu[:nq], ref[:nq]) and not mu[nq:].any()
