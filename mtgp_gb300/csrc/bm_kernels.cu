@@ -10,7 +10,8 @@
 // 2n - 1 - N upwards: the discrepancy is the parity of C AND (R >> (2n - 1 -
 // N)), each lane taking every 32nd word, reduced across the warp with one
 // redux.  The 2n steps are a dependent chain, so a warp (no block barrier)
-// does one sequence; many sequences run at once.
+// does one sequence; many sequences run at once (with fewer sequences than
+// SMs, a CTA per sequence shares each step's words among its threads).
 //
 // Barrett's constant mu = floor(X^(2D) / chi): with C(x) = x^D chi(1/x) (the
 // connection polynomial, C_0 = 1), reversing X^(2D) = q chi + r gives
@@ -132,6 +133,125 @@ __global__ void k_barrett(const uint32_t *__restrict__ chi, int D, int n, int nw
     for (int w = lane; w < nw; w += 32) mu[(size_t)j * stride + w] = Z[w];
 }
 
+// The same two chains with one CTA (NT threads) per sequence, for when there
+// are fewer sequences than SMs: each thread takes every NT-th word, warps
+// reduce with redux and the CTA with one barrier per step over
+// double-buffered warp partials (a step's partials are written while
+// slower threads may still read the previous step's).
+constexpr int kChainThreads = 256;
+
+__device__ __forceinline__ unsigned ctaParity(unsigned p, unsigned *red, int step) {
+    constexpr int NWARP = kChainThreads / 32;
+    const unsigned wp = __reduce_xor_sync(0xffffffffu, p);
+    unsigned *buf = red + (step & 1) * NWARP;
+    if ((threadIdx.x & 31) == 0) buf[threadIdx.x >> 5] = wp;
+    __syncthreads();
+    unsigned d = 0;
+#pragma unroll
+    for (int k = 0; k < NWARP; k++) d ^= buf[k];
+    return d;
+}
+
+template <typename W>
+__global__ void __launch_bounds__(kChainThreads)
+k_bm_cta(const W *__restrict__ seqs, int n2, int nw, int nr, uint32_t *__restrict__ Cout,
+         int *__restrict__ Lout) {
+    extern __shared__ __align__(16) uint32_t sm[];
+    __shared__ unsigned red[2 * (kChainThreads / 32)];
+    const int tid = threadIdx.x, j = blockIdx.x;
+    uint32_t *R = sm, *C = R + nr, *B = C + nw, *T = B + nw;
+    const W *s = seqs + (size_t)j * n2;
+    for (int r = tid >> 5; r < nr; r += kChainThreads / 32) {  // one warp per word of R
+        const int k = 32 * r + (tid & 31);
+        const uint32_t word = __ballot_sync(0xffffffffu, k < n2 && (s[n2 - 1 - k] & 1u));
+        if ((tid & 31) == 0) R[r] = word;
+    }
+    for (int w = tid; w < nw; w += kChainThreads) C[w] = B[w] = (w == 0 ? 1u : 0u);
+    __syncthreads();
+    int L = 0, m = -1;
+    for (int N = 0; N < n2; N++) {
+        const int base = n2 - 1 - N;
+        const int lw = L / 32 + 1;
+        uint32_t acc = 0;
+        for (int w = tid; w < lw; w += kChainThreads) acc ^= C[w] & shr(R, nr, w, base);
+        const unsigned d = ctaParity(__popc(acc) & 1u, red, N);
+        if (d) {  // the same for the whole CTA
+            const int sh = N - m;
+            const bool grow = 2 * L <= N;
+            const int nl = grow ? N + 1 - L : L;
+            const int top = (nl > L ? nl : L) / 32 + 1;
+            if (grow) {
+                for (int w = tid; w < nw; w += kChainThreads)
+                    T[w] = w < top ? C[w] ^ shl(B, nw, w, sh) : 0u;
+                uint32_t *old = B;
+                B = C;
+                C = T;
+                T = old;
+                L = nl;
+                m = N;
+            } else {
+                for (int w = tid; w < top && w < nw; w += kChainThreads) C[w] ^= shl(B, nw, w, sh);
+            }
+        }
+        // the next step's barrier (in ctaParity) orders these writes before
+        // any thread reads another's words
+    }
+    __syncthreads();
+    for (int w = tid; w < nw; w += kChainThreads) Cout[(size_t)j * nw + w] = C[w];
+    if (tid == 0) Lout[j] = L;
+}
+
+__global__ void __launch_bounds__(kChainThreads)
+k_barrett_cta(const uint32_t *__restrict__ chi, int D, int nw, size_t stride,
+              uint32_t *__restrict__ mu) {
+    extern __shared__ __align__(16) uint32_t sm[];
+    __shared__ unsigned red[2 * (kChainThreads / 32)];
+    const int tid = threadIdx.x, j = blockIdx.x;
+    uint32_t *Cp = sm, *Z = Cp + nw;
+    const uint32_t *ch = chi + (size_t)j * stride;
+    for (int w = tid; w < nw; w += kChainThreads) {
+        const int lo = D - 32 - 32 * w;
+        uint32_t g;
+        if (lo >= 0) {
+            g = __funnelshift_r(ch[lo >> 5], (lo >> 5) + 1 < nw ? ch[(lo >> 5) + 1] : 0u, lo & 31);
+        } else if (lo > -32) {
+            g = ch[0] << (-lo);
+        } else {
+            g = 0;
+        }
+        Cp[w] = __brev(g);
+    }
+    for (int w = tid; w < nw + 2; w += kChainThreads)
+        Z[w] = (w == (D >> 5)) ? 1u << (D & 31) : 0u;
+    __syncthreads();
+    for (int k = 1; k <= D; k++) {
+        const int base = D - k + 1;
+        const int lw = (k - 1) / 32 + 1;
+        uint32_t acc = 0;
+        for (int w = tid; w < lw; w += kChainThreads) acc ^= Cp[w] & shr(Z, nw + 2, w, base);
+        const unsigned d = ctaParity(__popc(acc) & 1u, red, k);
+        if (d && tid == 0) Z[(D - k) >> 5] |= 1u << ((D - k) & 31);
+        // the new bit sits in the next window's lowest word, which another
+        // thread reads when the window crosses a word boundary
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int w = tid; w < nw; w += kChainThreads) mu[(size_t)j * stride + w] = Z[w];
+}
+
+int smCount() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && v > 0)
+            sms = v;
+        else
+            return 152;
+    }
+    return sms;
+}
+
 int warpsPerBlock(size_t per_warp_bytes) {
     int w = (int)((200 * 1024) / (per_warp_bytes ? per_warp_bytes : 1));
     return w < 1 ? 1 : w > 4 ? 4 : w;
@@ -144,6 +264,15 @@ cudaError_t bmLaunch(const W *seqs, int n2, int nseq, int nw, uint32_t *C, int *
     const int nr = (n2 + 31) / 32 + 2;
     const size_t per = sizeof(uint32_t) * ((size_t)nr + 3 * (size_t)nw);
     if (per > 200 * 1024) return cudaErrorInvalidValue;
+    if (nseq < smCount()) {  // few sequences: a CTA each
+        cudaError_t e = cudaSuccess;
+        if (per > 48 * 1024)
+            e = cudaFuncSetAttribute(k_bm_cta<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)per);
+        if (e != cudaSuccess) return e;
+        k_bm_cta<W><<<nseq, kChainThreads, per, s>>>(seqs, n2, nw, nr, C, L);
+        return cudaGetLastError();
+    }
     const int wpb = warpsPerBlock(per);
     const size_t smem = per * wpb;
     cudaError_t e = cudaSuccess;
@@ -171,6 +300,15 @@ cudaError_t launchBarrett(const uint32_t *chi, int D, int n, int nw, size_t stri
     if (n <= 0) return cudaSuccess;
     const size_t per = sizeof(uint32_t) * (2 * (size_t)nw + 2);
     if (per > 200 * 1024) return cudaErrorInvalidValue;
+    if (n < smCount()) {  // few sets: a CTA each
+        cudaError_t e = cudaSuccess;
+        if (per > 48 * 1024)
+            e = cudaFuncSetAttribute(k_barrett_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)per);
+        if (e != cudaSuccess) return e;
+        k_barrett_cta<<<n, kChainThreads, per, s>>>(chi, D, nw, stride, mu);
+        return cudaGetLastError();
+    }
     const int wpb = warpsPerBlock(per);
     const size_t smem = per * wpb;
     cudaError_t e = cudaSuccess;

@@ -385,3 +385,36 @@ def test_gpu_polynomials_with_graph_and_refill(gpu, orc):
     plan.launch(out, s)
     s.synchronize()
     check(skips2, counts, out)
+
+
+def test_huge_arbitrary_skips(gpu, orc):
+    """Skips near 2^63 with every byte set (eight table factors, the full
+    product tree) in a batched plan and on a single generator, against the
+    oracle jumped by the same distances."""
+    from mtgp_gb300.api import MTGP32, work_items
+    p = load_table("mtgp32_fast_11213")[0]
+    seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
+    d, chi = orc.minpoly((seq & 1).astype(np.uint8))
+    nw = p.mexp // 32 + 1
+    skips = [0x7edcba9876543211, (1 << 63) + 0x0101010101010101]
+    # batched: two streams of one pool
+    pool, plist, pidx, seeds = _pool(32, "mtgp32_fast_11213", 2, seed0=900)
+    counts, offs = [3000, 2000], [0, 3000 * 4]
+    plan = pool.plan(work_items([0, 1], [0, 0], counts, offs, skips))
+    out = torch.zeros(5000 + 8, dtype=torch.int32, device="cuda")
+    plan.launch(out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(np.uint32)
+    for s in range(2):
+        q = plist[pidx[s]]
+        sq = orc.gen(q, seed=1).fill(0, 2 * q.mexp)
+        dq, cq = orc.minpoly((sq & 1).astype(np.uint8))
+        o = orc.gen(q, seed=int(seeds[s]))
+        o.jump_words(orc.powxmod(skips[s], cq, dq).view(np.uint32)[:nw])
+        ref = o.fill(0, counts[s])
+        assert np.array_equal(got[offs[s] // 4:offs[s] // 4 + counts[s]], ref), s
+    # single generator: skip() by the same distance
+    g, o = MTGP32(p, seed=4321), orc.gen(p, seed=4321)
+    g.skip(skips[0])
+    o.jump_words(orc.powxmod(skips[0], chi, d).view(np.uint32)[:nw])
+    assert np.array_equal(g.fill_uint32(2000).cpu().numpy().view(np.uint32), o.fill(0, 2000))
