@@ -238,7 +238,7 @@ def run_serving(args, s, local):
     from mtgp_gb300.api import Pool, Server, requests, set_tuning
     from mtgp_gb300.params import jump_table, load_table
     # the library's default planning (the batched section's tuning is global)
-    set_tuning("core", 4)
+    set_tuning("core", 2)
     set_tuning("split_chunk", 0)
     set_tuning("batch_grid", 0)
     p32 = load_table("mtgp32_fast_11213")[0]

@@ -411,8 +411,8 @@ int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
  * counterpart; the autotuner and tests use them):
  *   "split_chunk"  0 = automatic, < 0 = never split, > 0 = chunk length
  *   "batch_grid"   0 = one CTA per resident slot, > 0 = that many CTAs
- *   "core"         32-bit generation core: 4 = four adjacent words per
- *                  thread (default), 2 = two, 1 = one word per thread; plans
+ *   "core"         32-bit generation core: 2 = two adjacent words per
+ *                  thread (default), 4 = four, 1 = one word per thread; plans
  *                  whose items mix output kinds use the one-word core
  *   "poly_window"  bits per table window of the GPU's polynomial products
  *                  (jump polynomials): 0 = automatic (4 where the table

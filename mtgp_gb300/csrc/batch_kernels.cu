@@ -18,8 +18,9 @@
 // after the launch, so no chunk can read a window that another chunk has
 // already advanced.
 //
-// Plans without split requests use the four-words-per-thread core
-// (mtgp_device4.cuh) for 32-bit streams.
+// 32-bit streams run on the one-, two- or four-words-per-thread core
+// (mtgp_device.cuh, mtgp_device4.cuh), two by default; plans whose items mix
+// output kinds use the one-word core.
 #include <mutex>
 #include <vector>
 

@@ -10,9 +10,9 @@
 
 namespace mtgp {
 
-static int g_core32 = 4;
+static int g_core32 = 2;  // the fastest per generator and in steady state
 int genCore32() { return g_core32; }
-void setGenCore32(int c) { g_core32 = (c == 1 || c == 2) ? c : 4; }
+void setGenCore32(int c) { g_core32 = (c == 1 || c == 4) ? c : 2; }
 
 bool shape32(int mexp, Shape *s) {
 #define X(M, N, T, B) \
@@ -49,26 +49,43 @@ k_gen32(const DevParams32 *__restrict__ params, const int *__restrict__ pidx,
     for (int k = threadIdx.x; k < N; k += TN) st[k] = ring[k];
 }
 
-// Same as k_gen32 with the four-words-per-thread core (W = parallel width,
-// W/4 threads per CTA).
-template <int N, int W, int B, int KIND>
-__global__ void __launch_bounds__(W / 4)
-k_gen32x4(const DevParams32 *__restrict__ params, const int *__restrict__ pidx,
+// Same as k_gen32 with the K-words-per-thread core (W = parallel width, W/K
+// threads per CTA, K = 4 or 2).
+template <int N, int W, int B, int KIND, int K>
+__global__ void __launch_bounds__(W / K)
+k_gen32xk(const DevParams32 *__restrict__ params, const int *__restrict__ pidx,
           uint32_t *__restrict__ states, void *__restrict__ out, uint64_t n,
           uint64_t out_stride) {
-    using C = Core4<N, W, B, KIND>;
-    __shared__ __align__(16) uint32_t buf[Geo4<N, W, B>::BUF];
+    using C = CoreK<N, W, B, KIND, K>;
+    __shared__ __align__(16) uint32_t buf[GeoK<N, W, B, K>::BUF];
     const int g = blockIdx.x;
     const DevParams32 &P = params[pidx ? pidx[g] : g];
     Lane32 L;
     L.load(P, threadIdx.x & 31);
     uint32_t *st = states + (size_t)g * stateStride(N);
-    for (int k = threadIdx.x; k < N; k += W / 4) buf[plane_at<C::G::PW>(k)] = st[k];
+    for (int k = threadIdx.x; k < N; k += W / K) buf[plane_at<C::G::PW, K>(k)] = st[k];
     __syncthreads();
     using T = typename C::OT;
     T *o = KIND < 0 ? nullptr : reinterpret_cast<T *>(out) + (size_t)g * out_stride;
     C::run(buf, L, L.otab(KIND < 0 ? 0 : KIND), n, o);
-    for (int k = threadIdx.x; k < N; k += W / 4) st[k] = buf[plane_at<C::G::PW>(k)];
+    for (int k = threadIdx.x; k < N; k += W / K) st[k] = buf[plane_at<C::G::PW, K>(k)];
+}
+
+template <int N, int W, int B, int K>
+static cudaError_t gen32xk(int kind, const DevParams32 *params, const int *pidx,
+                           uint32_t *states, int ngen, void *out, uint64_t n, uint64_t os,
+                           cudaStream_t s) {
+    dim3 grid(ngen), b(W / K);
+    switch (kind) {
+    case -1: k_gen32xk<N, W, B, -1, K><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 0: k_gen32xk<N, W, B, 0, K><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 1: k_gen32xk<N, W, B, 1, K><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 2: k_gen32xk<N, W, B, 2, K><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 3: k_gen32xk<N, W, B, 3, K><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 4: k_gen32xk<N, W, B, 4, K><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 template <int N, int TN, int B, int KIND>
@@ -96,19 +113,8 @@ static cudaError_t gen32_kind(int kind, const DevParams32 *params, const int *pi
                               uint32_t *states, int ngen, void *out, uint64_t n,
                               uint64_t os, cudaStream_t s) {
     dim3 grid(ngen), block(TN);
-    if (genCore32() == 4) {
-        dim3 b4(TN / 4);
-        switch (kind) {
-        case -1: k_gen32x4<N, TN, B, -1><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
-        case 0: k_gen32x4<N, TN, B, 0><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
-        case 1: k_gen32x4<N, TN, B, 1><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
-        case 2: k_gen32x4<N, TN, B, 2><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
-        case 3: k_gen32x4<N, TN, B, 3><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
-        case 4: k_gen32x4<N, TN, B, 4><<<grid, b4, 0, s>>>(params, pidx, states, out, n, os); break;
-        default: return cudaErrorInvalidValue;
-        }
-        return cudaGetLastError();
-    }
+    if (genCore32() == 4) return gen32xk<N, TN, B, 4>(kind, params, pidx, states, ngen, out, n, os, s);
+    if (genCore32() == 2) return gen32xk<N, TN, B, 2>(kind, params, pidx, states, ngen, out, n, os, s);
     switch (kind) {
     case -1: k_gen32<N, TN, B, -1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
     case 0: k_gen32<N, TN, B, 0><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;

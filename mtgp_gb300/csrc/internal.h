@@ -54,8 +54,8 @@ struct Shape {
 
 
 bool shape32(int mexp, Shape *s);
-// Which 32-bit generation core the plain and batched kernels use: 4 = four
-// adjacent words per thread (default), 1 = one word per thread.
+// Which 32-bit generation core the plain and batched kernels use: 2 = two
+// adjacent words per thread (default), 4 = four, 1 = one word per thread.
 int genCore32();
 void setGenCore32(int core);
 bool shape64(int mexp, Shape *s);

@@ -161,7 +161,7 @@ def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core):
         plan = pool.plan(work_items(streams, kinds, counts, offs))
     finally:
         set_tuning("split_chunk", 0)
-        set_tuning("core", 4)
+        set_tuning("core", 2)
     ntasks, chunk = plan.info()
     assert chunk == 1500 and ntasks > nstreams
     out = torch.zeros(int(sum(counts)) * esz // 4 + 16, dtype=torch.int32, device="cuda")
@@ -265,7 +265,7 @@ def test_batch_vector_cores_one_kind(gpu, orc, core, kind):
     try:
         plan = pool.plan(work_items(np.arange(nstreams), np.full(nstreams, kind), counts, offs))
     finally:
-        set_tuning("core", 4)
+        set_tuning("core", 2)
         set_tuning("split_chunk", 0)
     assert plan.describe()["core"] == core
     out = torch.zeros(pos + 8, dtype=torch.int32, device="cuda")
