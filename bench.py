@@ -352,6 +352,38 @@ def run_polys(args, s):
                       "per_s": round(args.poly_n / wall, 1)}}
 
 
+def run_single(s, reps=50):
+    """One generator (mtgp32_params_fast_11213[0], seed 1234): 2^20 uint32
+    then 2^20 float32 in [1,2) per step into device memory, through the
+    generator's fill calls (each fill split over many CTAs from chunk
+    windows jumped ahead on the GPU)."""
+    import torch
+    from mtgp_gb300.api import MTGP32
+    from mtgp_gb300.params import load_table
+    g = MTGP32(load_table("mtgp32_fast_11213")[0], seed=1234)
+    n = 1 << 20
+    out = torch.empty(2 * n, dtype=torch.int32, device="cuda")
+    flt = out[n:].view(torch.float32)
+
+    def step():
+        g.fill_into(0, out[:n], n, stream=s)
+        g.fill_into(1, flt, n, stream=s)
+    for _ in range(5):
+        step()
+    s.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(s)
+    for _ in range(reps):
+        step()
+    ev1.record(s)
+    s.synchronize()
+    ms = ev0.elapsed_time(ev1) / reps
+    return {"workload": "one generator, mtgp32_params_fast_11213[0] seed 1234: 2^20 uint32 "
+                        "then 2^20 float32 [1,2) per step, device output",
+            "value": round(2 * n * 4 / (ms * 1e-3) / 1e9, 2), "unit": "GB/s",
+            "ms_per_step": round(ms, 4), "steps": reps}
+
+
 def poly_cpu_baseline(orc, seconds):
     """The oracle's bit-serial PowerXMod (one core) on the same exponents'
     distribution: polynomials per second over a bounded sample."""
@@ -609,9 +641,10 @@ def main():
                   "setup_s": round(setup_s, 2)}
 
     # --- jump polynomials for arbitrary offsets, on the GPU ---
-    polys = None
+    polys, single = None, None
     if rank == 0 and args.only == "all":
         polys = run_polys(args, s)
+        single = run_single(s)
 
     # --- serving: continuous batching over resident streams ---
     serve, serve_chk = None, None
@@ -669,6 +702,7 @@ def main():
             "bank": None if not bank_reps else {
                 "value": round(bank_gbs, 2), "unit": "GB/s", "ms": round(bank_ms, 3),
                 "workload": "128 sets x 2^21 uint32, seeds 1234+i, one CTA per set"},
+            "single": single,
             "jump_setup": {"ms": round(jump_ms, 2), "us_per_substream": round(1e3 * jump_ms / nsub, 2)},
             "plan": {"tasks": plan_tasks, "split_chunk": plan_chunk, "config": plan_cfg,
                      "autotune_ms": round(plan_ms, 1),

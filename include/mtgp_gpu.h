@@ -158,10 +158,12 @@ int mtgp32_gpu_fill_open_open(mtgp32_gpu_t *h, float *dev_out, size_t n,
                               void *stream);
 /* Generic form of the five fills above; kind is an MTGP_KIND_* value.
  * Fills of 2^20 values or more (MEXP 11213 and 23209) are split into chunks
- * that start with a GF(2) jump and run on many CTAs; such a fill may first
- * wait for the split fill issued two calls earlier on the same handle, and
- * the first one of a parameter set computes its jump tables (tens of ms).
- * Fills issued during stream capture always run on one CTA. */
+ * that start from GF(2)-jumped windows (made on the GPU first) and run on
+ * many CTAs; such a fill may first wait for the split fill issued two calls
+ * earlier on the same handle, the first one of a parameter set computes its
+ * jump tables (tens of ms), and the first one with a new chunk length its
+ * chunk polynomials (a synchronisation of `stream`).  Fills issued during
+ * stream capture always run on one CTA. */
 int mtgp32_gpu_fill(mtgp32_gpu_t *h, int kind, void *dev_out, size_t n,
                     void *stream);
 /* Advance the state by n steps without writing output.  From 2^22 steps on
@@ -416,7 +418,13 @@ int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
  *                  whose items mix output kinds use the one-word core
  *   "poly_window"  bits per table window of the GPU's polynomial products
  *                  (jump polynomials): 0 = automatic (4 where the table
- *                  fits in shared memory, else 2), 2 or 4 */
+ *                  fits in shared memory, else 2), 2 or 4
+ *   "single_chunk" chunk length of a split single-generator fill (fills of
+ *                  at least 2^20 values): 0 = automatic, > 0 = that length
+ *   "single_parts" CTAs that share one chunk-start jump of such a fill:
+ *                  0 = automatic (4), > 0 = that many (at most one per tap
+ *                  chunk of the jump kernel), -1 = chunks start with a jump
+ *                  inside the batched kernel instead */
 int mtgp_gpu_set_tuning(const char *key, int64_t value);
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
 

@@ -7,6 +7,7 @@
 // generation, jump and batched kernels.  Everything that produces random
 // numbers runs on the GPU; there is no CPU generation path.
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -92,9 +93,15 @@ constexpr uint64_t kJumpMinSkip = 1 << 17;
 // jump): about ten seconds of one CTA.
 constexpr uint64_t kMaxGenSkip = uint64_t(1) << 34;
 
+// single_chunk / single_parts: chunk length of split single-generator fills
+// (0 = automatic) and CTAs per chunk-start jump (0 = four; at most one per
+// tap chunk of the jump kernel; -1 = chunks start with in-kernel jumps
+// instead).
 struct Tuning {
     int64_t split_chunk = 0;
     int64_t batch_grid = 0;
+    int64_t single_chunk = 0;
+    int64_t single_parts = 0;
 };
 Tuning g_tune;
 
@@ -118,6 +125,14 @@ struct T32 {
     }
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch32(b, p, st, s);
+    }
+    static cudaError_t parts(int mexp, const DP *p, const W *st, const JumpPart *d, int nd, int nw,
+                             cudaStream_t s) {
+        return launchJumpParts32(mexp, p, st, d, nd, nw, s);
+    }
+    static int jumpChunks(int mexp, int nw) { return jumpChunks32(mexp, nw); }
+    static cudaError_t windows(const W *gen, W *win, int n, int stride, int nwin, cudaStream_t s) {
+        return launchChunkWindows32(gen, win, n, stride, nwin, s);
     }
     static int resident(int mexp, bool split, int core) {
         return batchResident32(mexp, split, core);
@@ -156,6 +171,14 @@ struct T64 {
     }
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch64(b, p, st, s);
+    }
+    static cudaError_t parts(int mexp, const DP *p, const W *st, const JumpPart *d, int nd, int nw,
+                             cudaStream_t s) {
+        return launchJumpParts64(mexp, p, st, d, nd, nw, s);
+    }
+    static int jumpChunks(int mexp, int nw) { return jumpChunks64(mexp, nw); }
+    static cudaError_t windows(const W *gen, W *win, int n, int stride, int nwin, cudaStream_t s) {
+        return launchChunkWindows64(gen, win, n, stride, nwin, s);
     }
     static int resident(int mexp, bool split, int) { return batchResident64(mexp, split); }
     static bool splits(int mexp) { return batchSplits64(mexp); }
@@ -921,11 +944,29 @@ struct Pool {
 // ==========================================================================
 // Public structs
 // ==========================================================================
-// Large fills of a single generator run as split plans (see fillSingle);
-// two plans are used in turn, so a fill never refills a plan whose previous
-// launch the GPU may still be reading.
+// Large fills of a single generator run split over many CTAs (see
+// fillSingle).  Two slots of buffers are used in turn, so a fill never
+// rewrites buffers that the GPU may still be reading for the previous one.
 struct SingleFill {
-    mtgp_gpu_plan *plan[2] = {nullptr, nullptr};
+    // chunk-start jump polynomials X^(c * poly_chunk) mod chi, c = 1..npolys
+    // (device, polyWords words each), kept while the chunk length stays
+    uint32_t *d_polys = nullptr;
+    size_t cap_polys = 0;
+    int64_t poly_chunk = 0;
+    int npolys = 0;
+    struct Slot {
+        void *d_win = nullptr;  // chunk-start windows
+        size_t cap_win = 0;
+        unsigned char *h_desc = nullptr, *d_desc = nullptr;  // tasks | items | parts
+        size_t cap_desc = 0;
+        unsigned *d_counter = nullptr;
+        // what the uploaded descriptors describe
+        size_t n = 0;
+        int kind = -9, parts = 0;
+        int64_t chunk = 0;
+        const void *win = nullptr, *polys = nullptr;
+        mtgp_gpu_plan *plan = nullptr;  // single_parts = -1: a split plan
+    } slot[2];
     cudaEvent_t done[2] = {nullptr, nullptr};
     int next = 0;
 };
@@ -1291,14 +1332,45 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
 }
 
 // n successive values of one generator.  A fill of at least kSplitFillMin
-// values, on an exponent with the in-kernel jump, runs as a split plan: chunks
-// of the request start from the window jumped by X^(c*chunk) and run on many
-// CTAs at once (one CTA alone generates about 2.6 G values/s), on the
-// one-word core, whose CTAs run a single task fastest.  Smaller fills, and
-// fills issued while the stream is being captured, run on one CTA.  The first
-// split fill of a parameter set also computes its characteristic polynomial
-// and jump polynomials (tens of milliseconds, and a device synchronisation).
+// values, on an exponent with GF(2) jumps, is cut into chunks: chunk c starts
+// from the generator's window jumped by X^(c * chunk) mod chi.  Those windows
+// are made first, every jump's correlation split over several CTAs
+// (k_jump_part, a range of the jump kernel's tap chunks each), from
+// polynomials kept on the device for the chunk length; then one batched
+// launch runs every chunk from its window on the two-word core, with no jump
+// inside it, and the window after the last chunk becomes the generator's.
+// A 2^20-value fill takes 0.05 ms this way (0.12 ms with one in-kernel jump
+// per chunk, 0.41 ms on one CTA), 2^26 values 0.18 ms.  Smaller fills,
+// and fills issued while the stream is being captured, run on one CTA.  The
+// first split fill of a parameter set also computes its characteristic
+// polynomial and jump tables (tens of milliseconds, and a device
+// synchronisation), and a new chunk length its chunk polynomials.
 constexpr size_t kSplitFillMin = size_t(1) << 20;
+constexpr int64_t kMaxFillChunks = 4096;
+
+// Chunk length of a split fill of n values: the power of two nearest to
+// 32 sqrt(n) for MEXP 11213 (measured on GB300: 2^15 for 2^20 values, 2^18
+// for 2^26; more chunks cost more jumps, longer ones a longer run), scaled
+// by mexp / 11213 (a jump's correlation grows with mexp^2, so the best
+// length grows with mexp).  Jump parts: four per jump (each part
+// regenerates the sequence up to its taps, so one per tap chunk costs more
+// than it saves).
+constexpr int kFillParts = 4;
+
+int64_t singleChunk(size_t n, int mexp) {
+    const double t = 32.0 * (mexp / 11213.0) * std::sqrt((double)n);
+    int64_t c = 1;
+    while ((double)c * 1.4142135623730951 < t) c <<= 1;
+    return c;
+}
+
+int waitSlot(SingleFill &F, int i) {
+    if (F.done[i])
+        CK(cudaEventSynchronize(F.done[i]), "wait for an earlier fill");
+    else
+        CK(cudaEventCreateWithFlags(&F.done[i], cudaEventDisableTiming), "cudaEventCreate");
+    return MTGP_OK;
+}
 
 template <class T, class Obj>
 int fillSingle(Obj *h, int kind, void *out, size_t n, void *s);
@@ -1307,8 +1379,36 @@ int planLaunch(mtgp_gpu_plan *pl, void *out, void *s) {
     return pl->bits == 32 ? launchPlan<T32>(pl, out, s) : launchPlan<T64>(pl, out, s);
 }
 
+// The same fill as a one-item split plan whose chunks start with in-kernel
+// jumps, one CTA per jump, on the one-word core (tuning knob single_parts =
+// -1; about two chunks per SM).
+template <class T, class Obj>
+int fillSplitPlan(Obj *h, int kind, void *out, size_t n, void *s, int sms) {
+    Pool<T> &P = h->pool;
+    SingleFill &F = h->fill;
+    const int i = F.next;
+    int rc = waitSlot(F, i);
+    if (rc) return rc;
+    mtgp_work_item_t it{};
+    it.stream = 0;
+    it.kind = kind;
+    it.count = n;
+    int64_t chunk = g_tune.split_chunk;
+    if (chunk == 0) {
+        chunk = 1 << 17;
+        while ((uint64_t)chunk * 2 * (uint64_t)sms < n) chunk <<= 1;
+    }
+    rc = makePlan(P, &it, 1, &F.slot[i].plan, 1, chunk);
+    if (!rc) rc = launchPlan<T>(F.slot[i].plan, out, s);
+    if (rc) return rc;
+    CK(cudaEventRecord(F.done[i], S(s)), "record fill");
+    F.next ^= 1;
+    return MTGP_OK;
+}
+
 template <class T, class Obj>
 int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
+    using W = typename T::W;
     Pool<T> &P = h->pool;
     if (n < kSplitFillMin || !T::splits(P.sh.mexp)) return P.fillAll(kind, out, n, s);
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1317,29 +1417,135 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
     int rc = P.checkKind(kind);
     if (!rc) rc = P.checkOut(out, n);
     if (rc) return rc;
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_tune.single_parts < 0) return fillSplitPlan<T>(h, kind, out, n, s, sms);
+    int64_t chunk = g_tune.single_chunk > 0 ? g_tune.single_chunk : singleChunk(n, P.sh.mexp);
+    if ((n + chunk - 1) / chunk > (uint64_t)kMaxFillChunks)
+        chunk = (int64_t)((n + kMaxFillChunks - 1) / kMaxFillChunks);
+    const int nch = (int)((n + chunk - 1) / chunk);
+    if (nch < 2) return P.fillAll(kind, out, n, s);
     SingleFill &F = h->fill;
     const int i = F.next;
-    if (F.done[i])
-        CK(cudaEventSynchronize(F.done[i]), "wait for an earlier fill");
-    else
-        CK(cudaEventCreateWithFlags(&F.done[i], cudaEventDisableTiming), "cudaEventCreate");
-    mtgp_work_item_t it{};
-    it.stream = 0;
-    it.kind = kind;
-    it.count = n;
-    // about two chunks per SM: more chunks make the in-CTA jumps (tens of
-    // microseconds of integer work each) the larger cost
-    int64_t chunk = g_tune.split_chunk;
-    if (chunk == 0) {
-        int dev = 0, sms = 152;
-        if (cudaGetDevice(&dev) == cudaSuccess)
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        chunk = 1 << 17;
-        while ((uint64_t)chunk * 2 * (uint64_t)sms < n) chunk <<= 1;
-    }
-    rc = makePlan(P, &it, 1, &F.plan[i], 1, chunk);
-    if (!rc) rc = launchPlan<T>(F.plan[i], out, s);
+    SingleFill::Slot &L = F.slot[i];
+    rc = waitSlot(F, i);
     if (rc) return rc;
+
+    // chunk-start polynomials X^(c * chunk), c = 1 .. nch - 1
+    const int pw = P.polyWords();
+    if (F.poly_chunk != chunk || F.npolys < nch - 1) {
+        for (int q = 0; q < 2; q++)  // earlier fills may still read them
+            if (F.done[q]) CK(cudaEventSynchronize(F.done[q]), "wait for an earlier fill");
+        const size_t words = (size_t)(nch - 1) * (size_t)pw;
+        F.poly_chunk = 0;
+        F.npolys = 0;
+        if (words > F.cap_polys) {
+            cudaFree(F.d_polys);
+            F.d_polys = nullptr;
+            F.cap_polys = 0;
+            CK(cudaMalloc(&F.d_polys, sizeof(uint32_t) * words), "cudaMalloc(chunk polynomials)");
+            F.cap_polys = words;
+        }
+        std::vector<uint64_t> steps((size_t)nch - 1);
+        for (int c = 1; c < nch; c++) steps[(size_t)c - 1] = (uint64_t)c * (uint64_t)chunk;
+        rc = P.gpuPolys(P.hpidx[0], steps.data(), nch - 1, F.d_polys, s);
+        if (rc) return rc;
+        // later fills may be issued on other streams
+        CK(cudaStreamSynchronize(S(s)), "chunk polynomials");
+        F.poly_chunk = chunk;
+        F.npolys = nch - 1;
+    }
+
+    // windows, and descriptors (rebuilt only when the fill's shape changes)
+    const size_t stride = (size_t)P.stride;
+    const size_t win_bytes = sizeof(W) * stride * (size_t)nch;
+    if (win_bytes > L.cap_win) {
+        cudaFree(L.d_win);
+        L.d_win = nullptr;
+        L.cap_win = 0;
+        CK(cudaMalloc(&L.d_win, win_bytes), "cudaMalloc(chunk windows)");
+        L.cap_win = win_bytes;
+    }
+    if (!L.d_counter) CK(cudaMalloc(&L.d_counter, sizeof(unsigned)), "cudaMalloc(counter)");
+    W *win = static_cast<W *>(L.d_win);
+    const int tchunks = T::jumpChunks(P.sh.mexp, pw);
+    const int parts = (int)std::min<int64_t>(
+        g_tune.single_parts > 0 ? g_tune.single_parts : kFillParts, tchunks);
+    const int nparts = (nch - 1) * parts;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t off_items = al(sizeof(BatchTask) * (size_t)nch);
+    const size_t off_parts = off_items + al(sizeof(BatchItem) * (size_t)nch);
+    const size_t bytes = off_parts + sizeof(JumpPart) * (size_t)nparts;
+    if (L.n != n || L.kind != kind || L.chunk != chunk || L.parts != parts || L.win != L.d_win ||
+        L.polys != F.d_polys) {
+        L.n = 0;
+        if (bytes > L.cap_desc) {
+            cudaFreeHost(L.h_desc);
+            cudaFree(L.d_desc);
+            L.h_desc = L.d_desc = nullptr;
+            L.cap_desc = 0;
+            CK(cudaMallocHost(&L.h_desc, bytes), "cudaMallocHost(fill descriptors)");
+            CK(cudaMalloc(&L.d_desc, bytes), "cudaMalloc(fill descriptors)");
+            L.cap_desc = bytes;
+        }
+        BatchTask *t = reinterpret_cast<BatchTask *>(L.h_desc);
+        BatchItem *it = reinterpret_cast<BatchItem *>(L.h_desc + off_items);
+        JumpPart *jp = reinterpret_cast<JumpPart *>(L.h_desc + off_parts);
+        for (int c = 0; c < nch; c++) {
+            t[c] = BatchTask{};
+            t[c].stream = c;
+            t[c].first = c;
+            t[c].nitems = 1;
+            t[c].pidx = P.hpidx[0];
+            t[c].j0 = t[c].j1 = -1;
+            t[c].wb = c == nch - 1 ? kWbStream : kWbNone;
+            it[c] = BatchItem{};
+            it[c].out_off = (uint64_t)c * (uint64_t)chunk * sizeof(W);
+            it[c].count = c == nch - 1 ? n - (uint64_t)c * (uint64_t)chunk : (uint64_t)chunk;
+            it[c].kind = kind;
+        }
+        for (int c = 1; c < nch; c++)
+            for (int q = 0; q < parts; q++) {
+                JumpPart &d = jp[(size_t)(c - 1) * parts + q];
+                d = JumpPart{};
+                d.poly = F.d_polys + (size_t)(c - 1) * pw;
+                d.src = 0;
+                d.dst = win + (size_t)c * stride;
+                d.pidx = P.hpidx[0];
+                d.ch0 = q * tchunks / parts;
+                d.ch1 = (q + 1) * tchunks / parts;
+            }
+        CK(cudaMemcpyAsync(L.d_desc, L.h_desc, bytes, cudaMemcpyHostToDevice, S(s)),
+           "upload fill descriptors");
+        L.n = n;
+        L.kind = kind;
+        L.chunk = chunk;
+        L.parts = parts;
+        L.win = L.d_win;
+        L.polys = F.d_polys;
+    }
+
+    CK(T::windows(P.d_states, win, P.size, (int)stride, nch, S(s)), "chunk windows");
+    CK(T::parts(P.sh.mexp, P.d_params, win, reinterpret_cast<const JumpPart *>(L.d_desc + off_parts),
+                nparts, pw, S(s)),
+       "chunk-start jumps");
+    BatchLaunch b{};
+    b.mexp = P.sh.mexp;
+    b.mode = kind;
+    b.grid = std::min(nch, T::resident(P.sh.mexp, false, 2));
+    b.core = 2;
+    b.split = false;
+    b.nwords = pw;
+    b.tasks = reinterpret_cast<const BatchTask *>(L.d_desc);
+    b.ntasks = nch;
+    b.items = reinterpret_cast<const BatchItem *>(L.d_desc + off_items);
+    b.out = out;
+    b.counter = L.d_counter;
+    CK(T::batch(b, P.d_params, win, S(s)), "chunks");
+    CK(cudaMemcpyAsync(P.d_states, win + (size_t)(nch - 1) * stride, sizeof(W) * (size_t)P.size,
+                       cudaMemcpyDeviceToDevice, S(s)),
+       "window after the last chunk");
     CK(cudaEventRecord(F.done[i], S(s)), "record fill");
     F.next ^= 1;
     return MTGP_OK;
@@ -1359,10 +1565,17 @@ int skipSingle(Pool<T> &P, uint64_t n, void *s) {
 template <class Obj>
 void freeSingle(Obj *h) {
     cudaDeviceSynchronize();
+    SingleFill &F = h->fill;
     for (int i = 0; i < 2; i++) {
-        delete h->fill.plan[i];
-        if (h->fill.done[i]) cudaEventDestroy(h->fill.done[i]);
+        SingleFill::Slot &L = F.slot[i];
+        delete L.plan;
+        cudaFree(L.d_win);
+        cudaFree(L.d_desc);
+        cudaFreeHost(L.h_desc);
+        cudaFree(L.d_counter);
+        if (F.done[i]) cudaEventDestroy(F.done[i]);
     }
+    cudaFree(F.d_polys);
     delete h;
 }
 
@@ -1938,6 +2151,12 @@ int mtgp_gpu_set_tuning(const char *key, int64_t value) {
     } else if (!std::strcmp(key, "batch_grid")) {
         if (value < 0) return setErr(MTGP_ERR_INVALID, "batch_grid must be >= 0");
         g_tune.batch_grid = value;
+    } else if (!std::strcmp(key, "single_chunk")) {
+        if (value < 0) return setErr(MTGP_ERR_INVALID, "single_chunk must be >= 0");
+        g_tune.single_chunk = value;
+    } else if (!std::strcmp(key, "single_parts")) {
+        if (value < -1) return setErr(MTGP_ERR_INVALID, "single_parts must be >= -1");
+        g_tune.single_parts = value;
     } else {
         return setErr(MTGP_ERR_INVALID, "unknown tuning key '%s'", key);
     }

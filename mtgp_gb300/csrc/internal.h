@@ -160,6 +160,12 @@ cudaError_t launchJumpParts64(int mexp, const DevParams64 *params, const uint64_
                               const JumpPart *parts, int nparts, int nwords, cudaStream_t s);
 int jumpChunks32(int mexp, int nwords);
 int jumpChunks64(int mexp, int nwords);
+// nwin windows of `stride` words at win: window 0 = gen[0..n), the others
+// zero (the destinations of jump parts).
+cudaError_t launchChunkWindows32(const uint32_t *gen, uint32_t *win, int n, int stride, int nwin,
+                                 cudaStream_t s);
+cudaError_t launchChunkWindows64(const uint64_t *gen, uint64_t *win, int n, int stride, int nwin,
+                                 cudaStream_t s);
 cudaError_t launchJump32(int mexp, const DevParams32 *params, uint32_t *states,
                          const JumpDesc *descs, int ndesc, int nwords,
                          cudaStream_t s);

@@ -144,4 +144,35 @@ int jumpChunks64(int mexp, int nwords) {
     return 1;
 }
 
+namespace {
+
+// Block c: win[c] = the generator's window for c = 0, zero otherwise (the
+// jump parts XOR into windows 1..).
+template <typename W>
+__global__ void __launch_bounds__(128)
+k_chunk_windows(const W *__restrict__ gen, W *__restrict__ win, int n, int stride) {
+    const size_t c = blockIdx.x;
+    W *dst = win + c * (size_t)stride;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = c ? W(0) : gen[k];
+}
+
+template <typename W>
+cudaError_t chunkWindows(const W *gen, W *win, int n, int stride, int nwin, cudaStream_t s) {
+    if (nwin <= 0 || n <= 0 || n > stride) return cudaErrorInvalidValue;
+    k_chunk_windows<W><<<nwin, 128, 0, s>>>(gen, win, n, stride);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launchChunkWindows32(const uint32_t *gen, uint32_t *win, int n, int stride, int nwin,
+                                 cudaStream_t s) {
+    return chunkWindows(gen, win, n, stride, nwin, s);
+}
+
+cudaError_t launchChunkWindows64(const uint64_t *gen, uint64_t *win, int n, int stride, int nwin,
+                                 cudaStream_t s) {
+    return chunkWindows(gen, win, n, stride, nwin, s);
+}
+
 }  // namespace mtgp
