@@ -588,6 +588,9 @@ def main():
     s.synchronize()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / max(e2e_steps, 1), world)
     e2e = job_value(world, total_bytes, e2e_s * 1e3)
+    # the plain and bank legs run on the default generation core, not on the
+    # batched plan's
+    set_tuning("core", 2)
 
     # --- plain: one launch (one CTA) per substream ---
     plain_ms = None
