@@ -405,8 +405,10 @@ int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *plan, int64_t *tasks,
 /* The plan's configuration, the first n of: [0] tasks, [1] split chunk
  * length (0 = none), [2] generation core (1, 2 or 4), [3] grid (0 = all
  * resident CTAs), [4] kernels one launch runs, [5] 1 if tasks start with
- * in-kernel jumps.  Passing these to mtgp_gpu_set_tuning ("core",
- * "split_chunk" (-1 for 0), "batch_grid") makes plans of the same kind. */
+ * in-kernel jumps, [6] tasks that start from a window jumped ahead of the
+ * launch (by jump parts, before the persistent kernel).  Passing [1]-[3] to
+ * mtgp_gpu_set_tuning ("core", "split_chunk" (-1 for 0), "batch_grid")
+ * makes plans of the same kind. */
 int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
                            int n);
 /* Process-wide tuning knobs for plans made afterwards (no reference
@@ -421,10 +423,11 @@ int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
  *                  fits in shared memory, else 2), 2 or 4
  *   "single_chunk" chunk length of a split single-generator fill (fills of
  *                  at least 2^20 values): 0 = automatic, > 0 = that length
- *   "single_parts" CTAs that share one chunk-start jump of such a fill:
- *                  0 = automatic (4), > 0 = that many (at most one per tap
- *                  chunk of the jump kernel), -1 = chunks start with a jump
- *                  inside the batched kernel instead */
+ *   "jump_parts"   jumps made ahead of a batched launch (the chunk starts of
+ *                  such a fill, and batched tasks that start with one jump):
+ *                  CTAs per jump, 0 = automatic (4), > 0 = that many (at
+ *                  most one per tap chunk of the jump kernel); -1 = such
+ *                  jumps run inside the batched kernel instead */
 int mtgp_gpu_set_tuning(const char *key, int64_t value);
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
 

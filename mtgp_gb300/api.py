@@ -165,11 +165,13 @@ class Plan:
 
     def describe(self):
         """Configuration: tasks, split chunk, core, grid, kernels per launch,
-        jumps (see mtgp_gpu_plan_describe)."""
-        v = np.zeros(6, dtype=np.int64)
-        check(lib().mtgp_gpu_plan_describe(self.h, v.ctypes.data_as(ctypes.c_void_p), 6))
+        in-kernel jumps, tasks from windows jumped ahead of the launch (see
+        mtgp_gpu_plan_describe)."""
+        v = np.zeros(7, dtype=np.int64)
+        check(lib().mtgp_gpu_plan_describe(self.h, v.ctypes.data_as(ctypes.c_void_p), 7))
         return {"tasks": int(v[0]), "split_chunk": int(v[1]), "core": int(v[2]),
-                "grid": int(v[3]), "kernels_per_launch": int(v[4]), "jumps": bool(v[5])}
+                "grid": int(v[3]), "kernels_per_launch": int(v[4]), "jumps": bool(v[5]),
+                "prejumps": int(v[6])}
 
     def launch(self, out, stream=None):
         check(lib().mtgp_gpu_plan_launch(self.h, ctypes.c_void_p(out.data_ptr()), _stream(stream)))

@@ -28,7 +28,10 @@ struct BatchTask {
     // stream after the launch, so no task can read a window that another
     // task already advanced).
     int32_t wb;
-    int32_t pad_;
+    // k + 1: the task starts from pre-jumped window k (BatchLaunch::prewin,
+    // made before the launch by jump parts) instead of the stream's window;
+    // 0: from the stream's window
+    int32_t pre;
 };
 static_assert(sizeof(BatchTask) == 32, "BatchTask is 32 bytes");
 constexpr int32_t kWbStream = -1;
@@ -54,6 +57,7 @@ struct BatchLaunch {
     void *stage;
     const int32_t *stage_streams;
     int nstage;
+    const void *prewin;             // pre-jumped start windows (BatchTask::pre)
 };
 cudaError_t launchBatch32(const BatchLaunch &b, const DevParams32 *params, uint32_t *states,
                           cudaStream_t s);

@@ -57,6 +57,14 @@ template <> struct SplitGeo32xK<726, 2> { using G = JGeo<726, 23, 256, 256, 4096
 template <int N> constexpr bool kSplit32 = (N == 351 || N == 726);
 template <int N> constexpr bool kSplit64 = (N == 176 || N == 363);
 
+// Where a task's start window is: a pre-jumped window, or its stream's.
+template <typename W>
+__device__ __forceinline__ const W *startWindow(const BatchTask &T, const W *states,
+                                                const W *prewin, int stride) {
+    return T.pre > 0 ? prewin + (size_t)(T.pre - 1) * stride
+                     : states + (size_t)T.stream * stride;
+}
+
 template <typename W>
 __device__ __forceinline__ W *endWindow(const BatchTask &T, W *states, W *stage, int stride) {
     return T.wb == kWbStream ? states + (size_t)T.stream * stride
@@ -113,7 +121,7 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
           unsigned *__restrict__ counter, uint32_t *__restrict__ stage,
-          const uint32_t *__restrict__ polys, int nwords) {
+          const uint32_t *__restrict__ polys, int nwords, const uint32_t *__restrict__ prewin) {
     __shared__ __align__(16) uint32_t sbuf[MODE == -2 ? 4 : B];
     uint32_t *const buf = MODE == -2 ? g_mix32 : sbuf;
     __shared__ int s_task;
@@ -126,7 +134,7 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
         const BatchTask T = tasks[t];
         Lane32 L;
         L.load(params[T.pidx], threadIdx.x & 31);
-        uint32_t *st = states + (size_t)T.stream * stateStride(N);
+        const uint32_t *st = startWindow(T, states, prewin, stateStride(N));
         for (int k = threadIdx.x; k < N; k += TN) buf[k] = st[k];
         if constexpr (SPLIT && kSplit32<N>) {
             using G = typename SplitGeo32<N>::G;
@@ -169,7 +177,8 @@ k_batch32xk(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
             const BatchTask *__restrict__ tasks, int ntasks,
             const BatchItem *__restrict__ items, char *__restrict__ out,
             unsigned *__restrict__ counter, uint32_t *__restrict__ stage,
-            const uint32_t *__restrict__ polys, int nwords) {
+            const uint32_t *__restrict__ polys, int nwords,
+            const uint32_t *__restrict__ prewin) {
     constexpr int T = W / K;
     constexpr int PW = GeoK<N, W, B, K>::PW;
     __shared__ __align__(16) uint32_t buf[GeoK<N, W, B, K>::BUF];
@@ -185,7 +194,7 @@ k_batch32xk(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
         const BatchTask TK = tasks[t];
         Lane32 L;
         L.load(params[TK.pidx], threadIdx.x & 31);
-        const uint32_t *src = states + (size_t)TK.stream * stateStride(N);
+        const uint32_t *src = startWindow(TK, states, prewin, stateStride(N));
         bool planar = true;
         if constexpr (SPLIT && kSplit32<N>) {
             using G = typename SplitGeo32xK<N, K>::G;
@@ -246,7 +255,7 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
           unsigned *__restrict__ counter, uint64_t *__restrict__ stage,
-          const uint32_t *__restrict__ polys, int nwords) {
+          const uint32_t *__restrict__ polys, int nwords, const uint64_t *__restrict__ prewin) {
     __shared__ __align__(16) uint64_t sbuf[MODE == -2 ? 4 : B];
     uint64_t *const buf = MODE == -2 ? g_mix64 : sbuf;
     __shared__ int s_task;
@@ -259,7 +268,7 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
         const BatchTask T = tasks[t];
         Lane64 L;
         L.load(params[T.pidx], threadIdx.x & 31);
-        uint64_t *st = states + (size_t)T.stream * stateStride(N);
+        const uint64_t *st = startWindow(T, states, prewin, stateStride(N));
         for (int k = threadIdx.x; k < N; k += TN) buf[k] = st[k];
         if constexpr (SPLIT && kSplit64<N>) {
             using G = typename SplitGeo64<N>::G;
@@ -348,7 +357,7 @@ static cudaError_t go(K kern, int tn, const BatchLaunch &b, const P *params, W *
     if (e != cudaSuccess) return e;
     kern<<<grid, tn, smem, s>>>(params, states, b.tasks, b.ntasks, b.items,
                              static_cast<char *>(b.out), b.counter, static_cast<W *>(b.stage),
-                             b.polys, b.nwords);
+                             b.polys, b.nwords, static_cast<const W *>(b.prewin));
     return cudaGetLastError();
 }
 

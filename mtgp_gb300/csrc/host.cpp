@@ -93,17 +93,30 @@ constexpr uint64_t kJumpMinSkip = 1 << 17;
 // jump): about ten seconds of one CTA.
 constexpr uint64_t kMaxGenSkip = uint64_t(1) << 34;
 
-// single_chunk / single_parts: chunk length of split single-generator fills
-// (0 = automatic) and CTAs per chunk-start jump (0 = four; at most one per
-// tap chunk of the jump kernel; -1 = chunks start with in-kernel jumps
-// instead).
+// single_chunk: chunk length of split single-generator fills (0 =
+// automatic).  jump_parts: CTAs per jump made ahead of a batched launch
+// (split single fills, and batched tasks that start with one jump): 0 =
+// four, at most one per tap chunk of the jump kernel; -1 = such jumps run
+// inside the batched kernel instead.
 struct Tuning {
     int64_t split_chunk = 0;
     int64_t batch_grid = 0;
     int64_t single_chunk = 0;
-    int64_t single_parts = 0;
+    int64_t jump_parts = 0;
 };
 Tuning g_tune;
+
+// Jumps made ahead of a batched launch run as four CTAs each: every part
+// regenerates the sequence up to its taps, so one CTA per tap chunk (11 for
+// MEXP 11213) costs more than it saves (measured on split single fills).
+constexpr int kJumpParts = 4;
+
+// CTAs per jump made ahead of a batched launch, for a jump of tchunks tap
+// chunks (tuning knob jump_parts).
+int jumpParts(int tchunks) {
+    const int64_t p = g_tune.jump_parts > 0 ? g_tune.jump_parts : kJumpParts;
+    return (int)std::min<int64_t>(p, tchunks);
+}
 
 // ------------------------------------------------------------------------
 // Traits of the two word sizes.
@@ -126,9 +139,9 @@ struct T32 {
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch32(b, p, st, s);
     }
-    static cudaError_t parts(int mexp, const DP *p, const W *st, const JumpPart *d, int nd, int nw,
-                             cudaStream_t s) {
-        return launchJumpParts32(mexp, p, st, d, nd, nw, s);
+    static cudaError_t parts(int mexp, const DP *p, const W *st, const uint32_t *polys, int nw,
+                             W *dst, int stride, const JumpPart *d, int nd, cudaStream_t s) {
+        return launchJumpParts32(mexp, p, st, polys, nw, dst, stride, d, nd, s);
     }
     static int jumpChunks(int mexp, int nw) { return jumpChunks32(mexp, nw); }
     static cudaError_t windows(const W *gen, W *win, int n, int stride, int nwin, cudaStream_t s) {
@@ -172,9 +185,9 @@ struct T64 {
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch64(b, p, st, s);
     }
-    static cudaError_t parts(int mexp, const DP *p, const W *st, const JumpPart *d, int nd, int nw,
-                             cudaStream_t s) {
-        return launchJumpParts64(mexp, p, st, d, nd, nw, s);
+    static cudaError_t parts(int mexp, const DP *p, const W *st, const uint32_t *polys, int nw,
+                             W *dst, int stride, const JumpPart *d, int nd, cudaStream_t s) {
+        return launchJumpParts64(mexp, p, st, polys, nw, dst, stride, d, nd, s);
     }
     static int jumpChunks(int mexp, int nw) { return jumpChunks64(mexp, nw); }
     static cudaError_t windows(const W *gen, W *win, int n, int stride, int nwin, cudaStream_t s) {
@@ -238,6 +251,7 @@ struct Pool {
     PlanResult plan_scratch;  // reused by every plan of this pool
     PowSchedule pow_scratch;
     std::vector<PowOp> powop_scratch;
+    std::vector<JumpPart> part_scratch;
 
     ~Pool() {
         for (uint32_t *b : gpow_blocks) cudaFree(b);
@@ -965,7 +979,7 @@ struct SingleFill {
         int kind = -9, parts = 0;
         int64_t chunk = 0;
         const void *win = nullptr, *polys = nullptr;
-        mtgp_gpu_plan *plan = nullptr;  // single_parts = -1: a split plan
+        mtgp_gpu_plan *plan = nullptr;  // jump_parts = -1: a split plan
     } slot[2];
     cudaEvent_t done[2] = {nullptr, nullptr};
     int next = 0;
@@ -1015,12 +1029,20 @@ struct mtgp_gpu_plan {
     size_t cap_pscratch = 0;
     void *d_stage = nullptr;  // final windows of streams with several tasks
     size_t cap_stage = 0;
+    // jumps made ahead of the launch (BatchTask::pre): npre windows, each the
+    // sum of its jump's parts (nparts descriptors in the blob), cleared and
+    // made before every launch
+    int npre = 0, nparts = 0;
+    const JumpPart *d_parts = nullptr;
+    void *d_prewin = nullptr;
+    size_t cap_prewin = 0;
 
     cudaGraphExec_t exec = nullptr;
     void *graph_out = nullptr;
     ~mtgp_gpu_plan() {
         if (exec) cudaGraphExecDestroy(exec);
         cudaFree(d_stage);
+        cudaFree(d_prewin);
         cudaFree(d_pscratch);
         cudaFree(d_blob);
         cudaFreeHost(h_blob);
@@ -1068,7 +1090,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         }
     }
     const int core = force_core ? force_core : (T::kBits == 32 && kinds == -2) ? 1 : genCore32();
-    o.resident = o.can_jump ? T::resident(P.sh.mexp, true, core) : 1;
+    // with jumps made ahead of the launch, the kernel without the jump code
+    o.resident = o.can_jump ? T::resident(P.sh.mexp, g_tune.jump_parts < 0, core) : 1;
     PlanResult &R = P.plan_scratch;
     std::string msg;
     int rc = planCore(items, nitems, o, &R, &msg);
@@ -1176,7 +1199,34 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         if (t.j1 >= kGpuSlot) t.j1 = remap[(size_t)(t.j1 - kGpuSlot)];
     }
     const size_t npolys = (size_t)nhost + gjobs.size();
-    const bool split = npolys > 0;  // the kernel variant with the jump code
+    // A task that starts with one jump takes its window from a slot made
+    // ahead of the launch by jump parts (jumpParts() CTAs per jump, all
+    // SMs at once), so no jump runs inside the persistent kernel; a chain of
+    // two (a run start, then a chunk offset) still jumps inside it.
+    std::vector<JumpPart> &jparts = P.part_scratch;
+    jparts.clear();
+    int npre = 0;
+    if (g_tune.jump_parts >= 0 && npolys > 0) {
+        const int tch = T::jumpChunks(P.sh.mexp, (int)pw);
+        const int parts = jumpParts(tch);
+        for (BatchTask &t : tasks) {
+            if (t.j0 < 0 || t.j1 >= 0) continue;
+            for (int q = 0; q < parts; q++) {
+                JumpPart d{};
+                d.src = (uint64_t)t.stream * (uint64_t)P.stride;
+                d.poly = t.j0;
+                d.dst = npre;
+                d.pidx = t.pidx;
+                d.ch0 = (int16_t)(q * tch / parts);
+                d.ch1 = (int16_t)((q + 1) * tch / parts);
+                jparts.push_back(d);
+            }
+            t.pre = ++npre;
+            t.j0 = -1;
+        }
+    }
+    bool split = false;  // the kernel variant with the jump code
+    for (const BatchTask &t : tasks) split = split || t.j0 >= 0;
     // reuse the caller's plan (replan) when given: its device buffers are
     // kept and only grown, so a server can refill plans without freeing
     // device memory (cudaFree would wait for every batch in flight)
@@ -1200,11 +1250,14 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->core = pl->mode == -2 ? 1 : core;
     pl->chunk = cut ? chunk : 0;
     pl->nstage = (int)stage_streams.size();
+    pl->npre = npre;
+    pl->nparts = (int)jparts.size();
     auto align = [](size_t n) { return (n + 255) & ~size_t(255); };
     const size_t off_items = align(sizeof(BatchTask) * tasks.size());
     const size_t off_polys = off_items + align(sizeof(BatchItem) * bitems.size());
     const size_t off_ops = off_polys + align(sizeof(uint32_t) * pw * npolys);
-    const size_t off_ss = off_ops + align(sizeof(PowOp) * (size_t)sch.steps());
+    const size_t off_parts = off_ops + align(sizeof(PowOp) * (size_t)sch.steps());
+    const size_t off_ss = off_parts + align(sizeof(JumpPart) * jparts.size());
     const size_t bytes = off_ss + sizeof(int32_t) * stage_streams.size();
     cudaError_t e = cudaSuccess;
     if (!pl->d_counter) e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
@@ -1240,12 +1293,24 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (e == cudaSuccess) pl->cap_stage = need + need / 4;
         }
     }
+    if (e == cudaSuccess && pl->npre) {
+        const size_t need = sizeof(W) * (size_t)P.stride * pl->npre;
+        if (need > pl->cap_prewin) {
+            cudaFree(pl->d_prewin);
+            pl->d_prewin = nullptr;
+            pl->cap_prewin = 0;
+            e = cudaMalloc(&pl->d_prewin, need + need / 4);
+            if (e == cudaSuccess) pl->cap_prewin = need + need / 4;
+        }
+    }
     if (e != cudaSuccess) {
         if (fresh) {
             delete pl;
         } else {  // a refilled plan that could not grow launches nothing
             pl->ntasks = 0;
             pl->nstage = 0;
+            pl->npre = 0;
+            pl->nparts = 0;
             pl->out_bytes = 0;
             pl->dirty = false;
         }
@@ -1267,6 +1332,9 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         for (const auto &lev : sch.levels) pl->pow_levels.push_back((int)lev.size());
     }
     pl->d_powops = reinterpret_cast<const PowOp *>(pl->d_blob + off_ops);
+    if (!jparts.empty())
+        std::memcpy(h + off_parts, jparts.data(), sizeof(JumpPart) * jparts.size());
+    pl->d_parts = reinterpret_cast<const JumpPart *>(pl->d_blob + off_parts);
     if (!stage_streams.empty())
         std::memcpy(h + off_ss, stage_streams.data(), sizeof(int32_t) * stage_streams.size());
     pl->blob_bytes = bytes;
@@ -1311,6 +1379,15 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     int rc = uploadPlan(pl, s);
     if (!rc) rc = powJobs(pl, P.polyWords(), s);
     if (rc) return rc;
+    if (pl->nparts) {  // the start windows jumped ahead of the launch
+        using W = typename T::W;
+        W *pre = static_cast<W *>(pl->d_prewin);
+        CK(cudaMemsetAsync(pre, 0, sizeof(W) * (size_t)P.stride * pl->npre, S(s)),
+           "clear jumped windows");
+        CK(T::parts(P.sh.mexp, P.d_params, P.d_states, pl->d_polys, P.polyWords(), pre, P.stride,
+                    pl->d_parts, pl->nparts, S(s)),
+           "jumps ahead of the launch");
+    }
     BatchLaunch b{};
     b.mexp = P.sh.mexp;
     b.mode = pl->mode;
@@ -1327,6 +1404,7 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     b.stage = pl->d_stage;
     b.stage_streams = pl->d_stage_streams;
     b.nstage = pl->nstage;
+    b.prewin = pl->d_prewin;
     CK(T::batch(b, P.d_params, P.d_states, S(s)), "batched launch");
     return MTGP_OK;
 }
@@ -1352,10 +1430,7 @@ constexpr int64_t kMaxFillChunks = 4096;
 // 32 sqrt(n) for MEXP 11213 (measured on GB300: 2^15 for 2^20 values, 2^18
 // for 2^26; more chunks cost more jumps, longer ones a longer run), scaled
 // by mexp / 11213 (a jump's correlation grows with mexp^2, so the best
-// length grows with mexp).  Jump parts: four per jump (each part
-// regenerates the sequence up to its taps, so one per tap chunk costs more
-// than it saves).
-constexpr int kFillParts = 4;
+// length grows with mexp).
 
 int64_t singleChunk(size_t n, int mexp) {
     const double t = 32.0 * (mexp / 11213.0) * std::sqrt((double)n);
@@ -1380,7 +1455,7 @@ int planLaunch(mtgp_gpu_plan *pl, void *out, void *s) {
 }
 
 // The same fill as a one-item split plan whose chunks start with in-kernel
-// jumps, one CTA per jump, on the one-word core (tuning knob single_parts =
+// jumps, one CTA per jump, on the one-word core (tuning knob jump_parts =
 // -1; about two chunks per SM).
 template <class T, class Obj>
 int fillSplitPlan(Obj *h, int kind, void *out, size_t n, void *s, int sms) {
@@ -1420,7 +1495,7 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_tune.single_parts < 0) return fillSplitPlan<T>(h, kind, out, n, s, sms);
+    if (g_tune.jump_parts < 0) return fillSplitPlan<T>(h, kind, out, n, s, sms);
     int64_t chunk = g_tune.single_chunk > 0 ? g_tune.single_chunk : singleChunk(n, P.sh.mexp);
     if ((n + chunk - 1) / chunk > (uint64_t)kMaxFillChunks)
         chunk = (int64_t)((n + kMaxFillChunks - 1) / kMaxFillChunks);
@@ -1470,8 +1545,7 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
     if (!L.d_counter) CK(cudaMalloc(&L.d_counter, sizeof(unsigned)), "cudaMalloc(counter)");
     W *win = static_cast<W *>(L.d_win);
     const int tchunks = T::jumpChunks(P.sh.mexp, pw);
-    const int parts = (int)std::min<int64_t>(
-        g_tune.single_parts > 0 ? g_tune.single_parts : kFillParts, tchunks);
+    const int parts = jumpParts(tchunks);
     const int nparts = (nch - 1) * parts;
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t off_items = al(sizeof(BatchTask) * (size_t)nch);
@@ -1509,12 +1583,12 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
             for (int q = 0; q < parts; q++) {
                 JumpPart &d = jp[(size_t)(c - 1) * parts + q];
                 d = JumpPart{};
-                d.poly = F.d_polys + (size_t)(c - 1) * pw;
                 d.src = 0;
-                d.dst = win + (size_t)c * stride;
+                d.poly = c - 1;
+                d.dst = c;
                 d.pidx = P.hpidx[0];
-                d.ch0 = q * tchunks / parts;
-                d.ch1 = (q + 1) * tchunks / parts;
+                d.ch0 = (int16_t)(q * tchunks / parts);
+                d.ch1 = (int16_t)((q + 1) * tchunks / parts);
             }
         CK(cudaMemcpyAsync(L.d_desc, L.h_desc, bytes, cudaMemcpyHostToDevice, S(s)),
            "upload fill descriptors");
@@ -1527,8 +1601,8 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
     }
 
     CK(T::windows(P.d_states, win, P.size, (int)stride, nch, S(s)), "chunk windows");
-    CK(T::parts(P.sh.mexp, P.d_params, win, reinterpret_cast<const JumpPart *>(L.d_desc + off_parts),
-                nparts, pw, S(s)),
+    CK(T::parts(P.sh.mexp, P.d_params, win, F.d_polys, pw, win, (int)stride,
+                reinterpret_cast<const JumpPart *>(L.d_desc + off_parts), nparts, S(s)),
        "chunk-start jumps");
     BatchLaunch b{};
     b.mexp = P.sh.mexp;
@@ -1708,11 +1782,13 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
                                        : "k_batch32xk<2> (two words per thread)")
                            : (b->split ? "k_batch32 (one word per thread, in-CTA jumps)"
                                        : "k_batch32 (one word per thread)");
-        char grid[32], line[200];
+        char grid[32], pre[64] = "", line[256];
         if (b->grid > 0) std::snprintf(grid, sizeof grid, "%d CTAs", b->grid);
         else std::snprintf(grid, sizeof grid, "all resident");
-        std::snprintf(line, sizeof line, "chosen: %s, chunk=%lld, grid=%s, tasks=%d: %.4f ms\n",
-                      kern, (long long)b->chunk, grid, b->ntasks, best_ms);
+        if (b->npre)
+            std::snprintf(pre, sizeof pre, " after k_jump_part (%d windows jumped ahead)", b->npre);
+        std::snprintf(line, sizeof line, "chosen: %s%s, chunk=%lld, grid=%s, tasks=%d: %.4f ms\n",
+                      kern, pre, (long long)b->chunk, grid, b->ntasks, best_ms);
         rep += line;
     }
     if (report && cap > 0) {
@@ -2130,9 +2206,10 @@ int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *pl, int64_t *tasks, int64_t *chunk
 
 int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *pl, int64_t *values, int n) {
     if (!pl || (n > 0 && !values)) return setErr(MTGP_ERR_INVALID, "null plan or values");
-    const int64_t v[6] = {pl->ntasks, pl->chunk, pl->bits == 64 ? 1 : pl->core, pl->grid,
-                          pl->ntasks ? 1 + (pl->nstage > 0) : 0, pl->split ? 1 : 0};
-    for (int k = 0; k < n && k < 6; k++) values[k] = v[k];
+    const int64_t v[7] = {pl->ntasks, pl->chunk, pl->bits == 64 ? 1 : pl->core, pl->grid,
+                          pl->ntasks ? 1 + (pl->nstage > 0) + (pl->nparts > 0) : 0,
+                          pl->split ? 1 : 0, pl->npre};
+    for (int k = 0; k < n && k < 7; k++) values[k] = v[k];
     return MTGP_OK;
 }
 
@@ -2154,9 +2231,9 @@ int mtgp_gpu_set_tuning(const char *key, int64_t value) {
     } else if (!std::strcmp(key, "single_chunk")) {
         if (value < 0) return setErr(MTGP_ERR_INVALID, "single_chunk must be >= 0");
         g_tune.single_chunk = value;
-    } else if (!std::strcmp(key, "single_parts")) {
-        if (value < -1) return setErr(MTGP_ERR_INVALID, "single_parts must be >= -1");
-        g_tune.single_parts = value;
+    } else if (!std::strcmp(key, "jump_parts")) {
+        if (value < -1) return setErr(MTGP_ERR_INVALID, "jump_parts must be >= -1");
+        g_tune.jump_parts = value;
     } else {
         return setErr(MTGP_ERR_INVALID, "unknown tuning key '%s'", key);
     }

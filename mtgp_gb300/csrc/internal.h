@@ -145,19 +145,24 @@ struct JumpDesc {
     uint64_t dst;      // element offset of the destination window
 };
 // Partial jumps: CTA b correlates the tap chunks [ch0, ch1) of one jump and
-// XORs the result into dst (a zeroed window); the parts of a jump together
-// give the full jump.  jumpChunks*() = tap chunks of one jump.
+// XORs the result into its destination window (zero on entry); the parts of
+// a jump together give the full jump.  jumpChunks*() = tap chunks of one
+// jump.  Source windows are in `states`, polynomials in `polys` (nwords
+// words each), destination windows `stride` words apart from `dst`.
 struct JumpPart {
-    const uint32_t *poly;
     uint64_t src;      // element offset of the source window in states
-    void *dst;         // destination window (global), zero on entry
-    int pidx;
-    int ch0, ch1;
+    int32_t poly;      // polynomial index
+    int32_t dst;       // destination window index
+    int32_t pidx;      // parameter-set index
+    int16_t ch0, ch1;
 };
+static_assert(sizeof(JumpPart) == 24, "JumpPart is 24 bytes");
 cudaError_t launchJumpParts32(int mexp, const DevParams32 *params, const uint32_t *states,
-                              const JumpPart *parts, int nparts, int nwords, cudaStream_t s);
+                              const uint32_t *polys, int nwords, uint32_t *dst, int stride,
+                              const JumpPart *parts, int nparts, cudaStream_t s);
 cudaError_t launchJumpParts64(int mexp, const DevParams64 *params, const uint64_t *states,
-                              const JumpPart *parts, int nparts, int nwords, cudaStream_t s);
+                              const uint32_t *polys, int nwords, uint64_t *dst, int stride,
+                              const JumpPart *parts, int nparts, cudaStream_t s);
 int jumpChunks32(int mexp, int nwords);
 int jumpChunks64(int mexp, int nwords);
 // nwin windows of `stride` words at win: window 0 = gen[0..n), the others

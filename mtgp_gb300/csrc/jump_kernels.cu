@@ -28,12 +28,13 @@ k_jump(const typename Tr::P *__restrict__ params, typename Tr::W *__restrict__ s
     for (int k = threadIdx.x; k < Geo::N; k += Geo::NT) states[D.dst + k] = smem[k];
 }
 
-// One CTA per (jump, slice of tap chunks): partial correlation XOR-ed into
+// One CTA per (jump, range of tap chunks): partial correlation XOR-ed into
 // the zeroed destination window (jump_device.cuh: jump_part).
 template <class Tr, class Geo>
 __global__ void __launch_bounds__(Geo::NT)
 k_jump_part(const typename Tr::P *__restrict__ params, const typename Tr::W *__restrict__ states,
-            const JumpPart *__restrict__ parts, int nwords) {
+            const uint32_t *__restrict__ polys, int nwords, typename Tr::W *__restrict__ dst,
+            int stride, const JumpPart *__restrict__ parts) {
     using W = typename Tr::W;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     W *smem = reinterpret_cast<W *>(smem_raw);
@@ -42,12 +43,14 @@ k_jump_part(const typename Tr::P *__restrict__ params, const typename Tr::W *__r
     L.load(params[D.pidx], threadIdx.x & 31);
     for (int k = threadIdx.x; k < Geo::N; k += Geo::NT) smem[k] = states[D.src + k];
     __syncthreads();
-    jump_part<Tr, Geo>(smem, L, D.poly, nwords, D.ch0, D.ch1, static_cast<W *>(D.dst));
+    jump_part<Tr, Geo>(smem, L, polys + (size_t)D.poly * nwords, nwords, D.ch0, D.ch1,
+                       dst + (size_t)D.dst * stride);
 }
 
 template <class Tr, class Geo>
 cudaError_t launchParts(const typename Tr::P *params, const typename Tr::W *states,
-                        const JumpPart *parts, int nparts, int nwords, cudaStream_t s) {
+                        const uint32_t *polys, int nwords, typename Tr::W *dst, int stride,
+                        const JumpPart *parts, int nparts, cudaStream_t s) {
     using W = typename Tr::W;
     const size_t smem = Geo::template bytes<W>(nwords);
     auto kern = k_jump_part<Tr, Geo>;
@@ -55,7 +58,7 @@ cudaError_t launchParts(const typename Tr::P *params, const typename Tr::W *stat
                                          (int)smem);
     if (e != cudaSuccess) return e;
     if (nparts <= 0) return cudaSuccess;
-    kern<<<nparts, Geo::NT, smem, s>>>(params, states, parts, nwords);
+    kern<<<nparts, Geo::NT, smem, s>>>(params, states, polys, nwords, dst, stride, parts);
     return cudaGetLastError();
 }
 
@@ -111,18 +114,24 @@ cudaError_t launchJump64(int mexp, const DevParams64 *params, uint64_t *states,
 }
 
 cudaError_t launchJumpParts32(int mexp, const DevParams32 *params, const uint32_t *states,
-                              const JumpPart *parts, int nparts, int nwords, cudaStream_t s) {
-#define X(M, G) \
-    if (mexp == M) return launchParts<Tr32, UNWRAP(G)>(params, states, parts, nparts, nwords, s);
+                              const uint32_t *polys, int nwords, uint32_t *dst, int stride,
+                              const JumpPart *parts, int nparts, cudaStream_t s) {
+#define X(M, G)                                                                              \
+    if (mexp == M)                                                                          \
+        return launchParts<Tr32, UNWRAP(G)>(params, states, polys, nwords, dst, stride, parts, \
+                                            nparts, s);
     MTGP_JGEO32(X)
 #undef X
     return cudaErrorInvalidValue;
 }
 
 cudaError_t launchJumpParts64(int mexp, const DevParams64 *params, const uint64_t *states,
-                              const JumpPart *parts, int nparts, int nwords, cudaStream_t s) {
-#define X(M, G) \
-    if (mexp == M) return launchParts<Tr64, UNWRAP(G)>(params, states, parts, nparts, nwords, s);
+                              const uint32_t *polys, int nwords, uint64_t *dst, int stride,
+                              const JumpPart *parts, int nparts, cudaStream_t s) {
+#define X(M, G)                                                                              \
+    if (mexp == M)                                                                          \
+        return launchParts<Tr64, UNWRAP(G)>(params, states, polys, nwords, dst, stride, parts, \
+                                            nparts, s);
     MTGP_JGEO64(X)
 #undef X
     return cudaErrorInvalidValue;

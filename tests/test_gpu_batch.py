@@ -131,9 +131,11 @@ def test_batch_rejects_bad_items(gpu):
                                         (32, "mtgp32_fast_23209"), (64, "mtgp64_fast_23209")])
 @pytest.mark.parametrize("mixed", [False, True])
 @pytest.mark.parametrize("core", [4, 2, 1])
-def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core):
-    """Long requests split into chunks whose start states are GF(2) jumps
-    done inside the batched kernel (each 32-bit generation core): bit-exact
+@pytest.mark.parametrize("parts", [0, -1])
+def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core, parts):
+    """Long requests split into chunks whose start states are GF(2) jumps,
+    made ahead of the batched kernel by jump parts (parts 0: four CTAs per
+    jump) or inside it (parts -1), on each 32-bit generation core: bit-exact
     outputs and final states, across two launches of the same plan."""
     from mtgp_gb300.api import Pool, set_tuning, work_items
     if bits == 64 and core != 4:
@@ -157,13 +159,18 @@ def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core):
     offs = list(offs) + [int(sum(counts[:-1])) * esz]
     set_tuning("split_chunk", 1500)
     set_tuning("core", core)
+    set_tuning("jump_parts", parts)
     try:
         plan = pool.plan(work_items(streams, kinds, counts, offs))
     finally:
         set_tuning("split_chunk", 0)
         set_tuning("core", 2)
+        set_tuning("jump_parts", 0)
     ntasks, chunk = plan.info()
     assert chunk == 1500 and ntasks > nstreams
+    desc = plan.describe()
+    assert (desc["prejumps"] > 0 and not desc["jumps"]) if parts == 0 else \
+        (desc["jumps"] and desc["prejumps"] == 0)
     out = torch.zeros(int(sum(counts)) * esz // 4 + 16, dtype=torch.int32, device="cuda")
     gens = {s: orc.gen(plist[pidx[s]], seed=int(seeds[s])) for s in range(nstreams)}
     for rep in range(2):

@@ -16,7 +16,7 @@ CASES = [(32, "mtgp32_fast_11213", 0), (64, "mtgp64dc_fast_11213", 0),
          (32, "mtgp32_fast_23209", 1), (64, "mtgp64_fast_23209", 2)]
 
 
-# (single_parts, single_chunk): automatic; three CTAs per jump with an odd
+# (jump_parts, single_chunk): automatic; three CTAs per jump with an odd
 # chunk length; one CTA per jump; chunks that jump inside the batched kernel
 TUNINGS = [(0, 0), (3, 100003), (1, 0), (-1, 0)]
 
@@ -25,10 +25,10 @@ TUNINGS = [(0, 0), (3, 100003), (1, 0), (-1, 0)]
 def tuning(request):
     from mtgp_gb300.api import set_tuning
     parts, chunk = request.param
-    set_tuning("single_parts", parts)
+    set_tuning("jump_parts", parts)
     set_tuning("single_chunk", chunk)
     yield request.param
-    set_tuning("single_parts", 0)
+    set_tuning("jump_parts", 0)
     set_tuning("single_chunk", 0)
 
 
