@@ -77,7 +77,7 @@ template <class Tr, class G>
 __device__ __forceinline__ void jump_task(typename Tr::W *buf, const typename Tr::Lane &L,
                                           const BatchTask &T, const uint32_t *polys, int nwords) {
     const int j0 = T.j0, j1 = T.j1;
-    jump_chain_impl<Tr, G>(
+    jump_chain_impl<Tr, G, false>(
         buf, L, [=](int c) { return polys + (size_t)(c ? j1 : j0) * nwords; }, j1 >= 0 ? 2 : 1,
         nwords);
 }

@@ -52,8 +52,10 @@ struct Tr64 {
 // Geometry of one jump instance.
 //   N    live words          R    outputs per lane (odd: conflict-free loads)
 //   NT   threads of the CTA  GW   words per recursion sub-step (<= NT, <= lanes)
-//   RING shared ring length (power of two)
-// Shared layout, in words W: jin[NJ] | jout[NJ] | ring[RING] | poly (uint32).
+//   RING shared ring length (power of two), followed by MIR words that repeat
+//        ring[0 .. MIR): the 2R words a tap group reads from one base are
+//        then contiguous, whatever their ring position
+// Shared layout, in words W: jin[NJ] | jout[NJ] | ring[RING + MIR] | poly (uint32).
 template <int N_, int R_, int NT_, int GW_, int RING_>
 struct JGeo {
     static constexpr int N = N_, R = R_, NT = NT_, GW = GW_, RING = RING_;
@@ -65,25 +67,105 @@ struct JGeo {
     static constexpr int C = NWARP * TPW;                  // taps per chunk
     static constexpr int NJ = (N + 3) & ~3;
     static constexpr int PAD = C / 32 + 4;                 // zero words after the poly
+    static constexpr int MIR = (2 * R + 3) & ~3;           // mirrored ring head
     static_assert(C + N + GW <= RING, "jump ring too small");
+    static_assert(MIR <= RING, "mirror longer than the ring");
     template <typename W>
     __host__ __device__ static constexpr size_t bytes(int nwords) {
-        return sizeof(W) * (size_t)(2 * NJ + RING) + sizeof(uint32_t) * (size_t)(nwords + PAD);
+        return sizeof(W) * (size_t)(2 * NJ + RING + MIR) +
+               sizeof(uint32_t) * (size_t)(nwords + PAD);
     }
 };
 
+// Ring slot k (k < RING) written with its mirror copy.
+template <class Geo, typename W>
+__device__ __forceinline__ void ringPut(W *ring, uint32_t k, W v) {
+    ring[k] = v;
+    if (k < (uint32_t)Geo::MIR) ring[Geo::RING + k] = v;
+}
+
+// The taps of one group, J .. J+3, against the lane's R outputs: bit t of
+// D says whether tap J + t is set.  Tap J + t reads seq[base + J + t + r]
+// for output r: win[(J + t + r) % R] while t + r < R (the register window,
+// rotated), else nx[t + r - R], the words just past the window.  The terms
+// are XOR-ed in a chain that the compiler fuses into three-input XORs (two
+// terms per instruction).
+template <class Tr, int R, int J, int D>
+__device__ __forceinline__ void tapGroup(typename Tr::W (&acc)[R], const typename Tr::W (&win)[R],
+                                         const typename Tr::W (&nx)[4]) {
+    using W = typename Tr::W;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        W v = acc[r];
+#pragma unroll
+        for (int t = 0; t < 4; t++)
+            if ((D >> t) & 1) v ^= (t + r < R) ? win[(J + t + r) % R] : nx[t + r - R];
+        acc[r] = v;
+    }
+}
+
+// One uniform branch per group of NT4 <= 4 taps: the group's coefficient
+// bits are the same for the whole warp.
+template <class Tr, int R, int J, int NT4>
+__device__ __forceinline__ void tapSwitch(typename Tr::W (&acc)[R], const typename Tr::W (&win)[R],
+                                          const typename Tr::W (&nx)[4], uint32_t d) {
+#define MTGP_TAP_CASE(D) \
+    case D:              \
+        if constexpr ((D >> NT4) == 0) tapGroup<Tr, R, J, D>(acc, win, nx); \
+        break;
+    switch (d) {
+        MTGP_TAP_CASE(1) MTGP_TAP_CASE(2) MTGP_TAP_CASE(3) MTGP_TAP_CASE(4)
+        MTGP_TAP_CASE(5) MTGP_TAP_CASE(6) MTGP_TAP_CASE(7) MTGP_TAP_CASE(8)
+        MTGP_TAP_CASE(9) MTGP_TAP_CASE(10) MTGP_TAP_CASE(11) MTGP_TAP_CASE(12)
+        MTGP_TAP_CASE(13) MTGP_TAP_CASE(14) MTGP_TAP_CASE(15)
+    default: break;
+    }
+#undef MTGP_TAP_CASE
+}
+
+// Groups J, J + 4, ... of the R taps of one tapsR call; each group's words
+// replace the window words its taps no longer need.
+template <class Tr, int R, int J>
+__device__ __forceinline__ void tapGroups(typename Tr::W (&acc)[R], typename Tr::W (&win)[R],
+                                          const typename Tr::W *rp, uint32_t bits_lo,
+                                          uint32_t bits_hi) {
+    if constexpr (J < R) {
+        using W = typename Tr::W;
+        constexpr int NT4 = R - J < 4 ? R - J : 4;
+        const uint32_t bj = J < 32 ? bits_lo : bits_hi;  // J % 4 == 0: never straddles bit 31
+        const uint32_t d = (bj >> (J & 31)) & ((1u << NT4) - 1u);
+        W nx[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) nx[u] = u < NT4 ? rp[R + J + u] : W(0);
+        tapSwitch<Tr, R, J, NT4>(acc, win, nx, d);
+#pragma unroll
+        for (int u = 0; u < NT4; u++) win[J + u] = nx[u];
+        tapGroups<Tr, R, J + 4>(acc, win, rp, bits_lo, bits_hi);
+    }
+}
+
+// Largest R for which taps go in groups of four (a 16-way branch per group,
+// whose code grows with R); larger R take them in pairs.  Groups of four
+// hold a few more registers live, so the jumps inside the batched kernels
+// (whose generation core caps the registers) keep pairs.
+constexpr int kQuadTapsMaxR = 13;
+
 // R taps p .. p+R-1 against the lane's R outputs: win holds seq[p + l0 ..
 // + R) on entry (l0 folded into base = p + l0) and the next R words on exit.
-// Taps go in pairs: the pair's coefficients are the same for the whole
-// warp, so each pair takes one uniform branch, and a pair with both
-// coefficients set costs R three-input XORs instead of 2R (on random
-// polynomials 0.75 R operations per pair on average instead of R).
-template <class Tr, class Geo>
+// rp = ring + (base & (RING - 1)): the next R words are rp[R .. 2R), which
+// the mirror keeps contiguous, so every load is one base plus a constant.
+// The coefficients of a group of taps are the same for the whole warp, so
+// each group takes one uniform branch.  In groups of four, a set of m taps
+// costs ceil(m / 2) three-input XORs per output (1.25 per group on random
+// polynomials, 0.31 per tap); in pairs (larger R) 0.375 per tap.
+template <class Tr, class Geo, bool GROUPS4>
 __device__ __forceinline__ void tapsR(typename Tr::W (&acc)[Geo::R], typename Tr::W (&win)[Geo::R],
-                                      const typename Tr::W *ring, uint32_t bits_lo,
-                                      uint32_t bits_hi, int base) {
+                                      const typename Tr::W *rp, uint32_t bits_lo,
+                                      uint32_t bits_hi) {
     constexpr int R = Geo::R;
-    constexpr uint32_t M = Geo::RING - 1;
+    if constexpr (GROUPS4 && R <= kQuadTapsMaxR) {
+        tapGroups<Tr, R, 0>(acc, win, rp, bits_lo, bits_hi);
+    } else {
 #pragma unroll
     for (int j = 0; j < R; j += 2) {  // j even: a pair never straddles bit 31
         const uint32_t bj = j < 32 ? bits_lo : bits_hi;
@@ -91,7 +173,7 @@ __device__ __forceinline__ void tapsR(typename Tr::W (&acc)[Geo::R], typename Tr
             // tap j reads seq[base + j .. + R) = win[(j + r) % R]; tap j + 1
             // reads seq[base + j + 1 .. + R), whose last word is the one that
             // replaces win[j]
-            const typename Tr::W next = ring[(uint32_t)(base + R + j) & M];
+            const typename Tr::W next = rp[R + j];
             auto w1 = [&](int r) { return r < R - 1 ? win[(j + 1 + r) % R] : next; };
             const uint32_t b2 = (bj >> (j & 31)) & 3u;
             if (b2 == 3u) {
@@ -105,22 +187,23 @@ __device__ __forceinline__ void tapsR(typename Tr::W (&acc)[Geo::R], typename Tr
                 for (int r = 0; r < R; r++) acc[r] ^= w1(r);
             }
             win[j] = next;
-            win[j + 1] = ring[(uint32_t)(base + R + j + 1) & M];
+            win[j + 1] = rp[R + j + 1];
         } else {  // the last tap of an odd R, on its own
             if ((bj >> (j & 31)) & 1u) {
 #pragma unroll
                 for (int r = 0; r < R; r++) acc[r] ^= win[(j + r) % R];
             }
-            win[j] = ring[(uint32_t)(base + R + j) & M];
+            win[j] = rp[R + j];
         }
+    }
     }
 }
 
 // Jump the window jin[0..N) in place by chain[0], chain[1], ... (uint32-array
 // polynomials of nwords words).  smem must hold Geo::bytes<W>(nwords) bytes
 // laid out as described above (jin first).  All NT threads must call it; it
-// begins and ends with a barrier.
-template <class Tr, class Geo, class ChainAt>
+// begins and ends with a barrier.  GROUPS4: taps in groups of four (tapsR).
+template <class Tr, class Geo, bool GROUPS4, class ChainAt>
 __device__ __forceinline__ void jump_chain_impl(typename Tr::W *smem, const typename Tr::Lane &L,
                                                 ChainAt chain, int nchain, int nwords) {
     using W = typename Tr::W;
@@ -129,7 +212,7 @@ __device__ __forceinline__ void jump_chain_impl(typename Tr::W *smem, const type
     W *jin = smem;
     W *jout = jin + Geo::NJ;
     W *ring = jout + Geo::NJ;
-    uint32_t *poly = reinterpret_cast<uint32_t *>(ring + Geo::RING);
+    uint32_t *poly = reinterpret_cast<uint32_t *>(ring + Geo::RING + Geo::MIR);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int taps = nwords * 32;
     const int pwords = nwords + Geo::PAD;
@@ -140,7 +223,7 @@ __device__ __forceinline__ void jump_chain_impl(typename Tr::W *smem, const type
         for (int k = tid; k < pwords; k += NT) poly[k] = k < nwords ? pg[k] : 0u;
         for (int k = tid; k < N; k += NT) jout[k] = 0;
         for (int g = 0; g < Geo::G; g++) {
-            for (int k = tid; k < N; k += NT) ring[k] = jin[k];
+            for (int k = tid; k < N; k += NT) ringPut<Geo>(ring, (uint32_t)k, jin[k]);
             __syncthreads();
             int generated = N;
             const int l0 = g * 32 * R + lane * R;
@@ -155,7 +238,7 @@ __device__ __forceinline__ void jump_chain_impl(typename Tr::W *smem, const type
                         W x1 = ring[(w - N) & M];
                         W x2 = ring[(w - N + 1) & M];
                         W y = ring[(w - N + L.pos) & M];
-                        ring[w & M] = Tr::rec(x1, x2, y, L);
+                        ringPut<Geo>(ring, w & M, Tr::rec(x1, x2, y, L));
                     }
                     __syncthreads();
                     generated += Geo::GW;
@@ -173,7 +256,7 @@ __device__ __forceinline__ void jump_chain_impl(typename Tr::W *smem, const type
                     const uint32_t bits_hi =
                         R > 32 ? __funnelshift_r(poly[(p >> 5) + 1], poly[(p >> 5) + 2], p & 31)
                                : 0u;
-                    tapsR<Tr, Geo>(acc, win, ring, bits_lo, bits_hi, p + l0);
+                    tapsR<Tr, Geo, GROUPS4>(acc, win, ring + ((uint32_t)(p + l0) & M), bits_lo, bits_hi);
                 }
                 __syncthreads();
             }
@@ -190,14 +273,14 @@ __device__ __forceinline__ void jump_chain_impl(typename Tr::W *smem, const type
 template <class Tr, class Geo>
 __device__ void jump_chain(typename Tr::W *smem, const typename Tr::Lane &L,
                            const uint32_t *const *chain, int nchain, int nwords) {
-    jump_chain_impl<Tr, Geo>(smem, L, [chain](int c) { return chain[c]; }, nchain, nwords);
+    jump_chain_impl<Tr, Geo, true>(smem, L, [chain](int c) { return chain[c]; }, nchain, nwords);
 }
 
 // One polynomial.
 template <class Tr, class Geo>
 __device__ void jump_one(typename Tr::W *smem, const typename Tr::Lane &L, const uint32_t *poly,
                          int nwords) {
-    jump_chain_impl<Tr, Geo>(smem, L, [poly](int) { return poly; }, 1, nwords);
+    jump_chain_impl<Tr, Geo, true>(smem, L, [poly](int) { return poly; }, 1, nwords);
 }
 
 // Part of one jump: the correlation over the tap chunks [ch0, ch1) only
@@ -213,12 +296,12 @@ __device__ void jump_part(typename Tr::W *smem, const typename Tr::Lane &L, cons
     constexpr uint32_t M = Geo::RING - 1;
     W *jin = smem;
     W *ring = jin + 2 * Geo::NJ;
-    uint32_t *poly = reinterpret_cast<uint32_t *>(ring + Geo::RING);
+    uint32_t *poly = reinterpret_cast<uint32_t *>(ring + Geo::RING + Geo::MIR);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int pwords = nwords + Geo::PAD;
     for (int k = tid; k < pwords; k += NT) poly[k] = k < nwords ? pg[k] : 0u;
     for (int g = 0; g < Geo::G; g++) {
-        for (int k = tid; k < N; k += NT) ring[k] = jin[k];
+        for (int k = tid; k < N; k += NT) ringPut<Geo>(ring, (uint32_t)k, jin[k]);
         __syncthreads();
         int generated = N;
         const int l0 = g * 32 * R + lane * R;
@@ -233,7 +316,7 @@ __device__ void jump_part(typename Tr::W *smem, const typename Tr::Lane &L, cons
                     W x1 = ring[(w - N) & M];
                     W x2 = ring[(w - N + 1) & M];
                     W y = ring[(w - N + L.pos) & M];
-                    ring[w & M] = Tr::rec(x1, x2, y, L);
+                    ringPut<Geo>(ring, w & M, Tr::rec(x1, x2, y, L));
                 }
                 __syncthreads();
                 generated += Geo::GW;
@@ -250,7 +333,7 @@ __device__ void jump_part(typename Tr::W *smem, const typename Tr::Lane &L, cons
                     const uint32_t bits_hi =
                         R > 32 ? __funnelshift_r(poly[(p >> 5) + 1], poly[(p >> 5) + 2], p & 31)
                                : 0u;
-                    tapsR<Tr, Geo>(acc, win, ring, bits_lo, bits_hi, p + l0);
+                    tapsR<Tr, Geo, true>(acc, win, ring + ((uint32_t)(p + l0) & M), bits_lo, bits_hi);
                 }
             }
             __syncthreads();
