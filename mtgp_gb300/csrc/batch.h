@@ -57,7 +57,8 @@ struct BatchLaunch {
     void *stage;
     const int32_t *stage_streams;
     int nstage;
-    const void *prewin;             // pre-jumped start windows (BatchTask::pre)
+    void *prewin;                   // pre-jumped start windows (BatchTask::pre);
+                                    // zero on entry, zeroed again as tasks read them
 };
 cudaError_t launchBatch32(const BatchLaunch &b, const DevParams32 *params, uint32_t *states,
                           cudaStream_t s);

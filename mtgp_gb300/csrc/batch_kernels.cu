@@ -65,6 +65,14 @@ __device__ __forceinline__ const W *startWindow(const BatchTask &T, const W *sta
                      : states + (size_t)T.stream * stride;
 }
 
+// The task's pre-jumped window, which each thread zeroes word by word right
+// after reading it (so the slots are zero again for the next launch's jump
+// parts, which XOR into them), or null.
+template <typename W>
+__device__ __forceinline__ W *preSlot(const BatchTask &T, W *prewin, int stride) {
+    return T.pre > 0 ? prewin + (size_t)(T.pre - 1) * stride : nullptr;
+}
+
 template <typename W>
 __device__ __forceinline__ W *endWindow(const BatchTask &T, W *states, W *stage, int stride) {
     return T.wb == kWbStream ? states + (size_t)T.stream * stride
@@ -121,7 +129,7 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
           unsigned *__restrict__ counter, uint32_t *__restrict__ stage,
-          const uint32_t *__restrict__ polys, int nwords, const uint32_t *__restrict__ prewin) {
+          const uint32_t *__restrict__ polys, int nwords, uint32_t *__restrict__ prewin) {
     __shared__ __align__(16) uint32_t sbuf[MODE == -2 ? 4 : B];
     uint32_t *const buf = MODE == -2 ? g_mix32 : sbuf;
     __shared__ int s_task;
@@ -135,7 +143,11 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
         Lane32 L;
         L.load(params[T.pidx], threadIdx.x & 31);
         const uint32_t *st = startWindow(T, states, prewin, stateStride(N));
-        for (int k = threadIdx.x; k < N; k += TN) buf[k] = st[k];
+        uint32_t *clr = preSlot(T, prewin, stateStride(N));
+        for (int k = threadIdx.x; k < N; k += TN) {
+            buf[k] = st[k];
+            if (clr) clr[k] = 0;
+        }
         if constexpr (SPLIT && kSplit32<N>) {
             using G = typename SplitGeo32<N>::G;
             static_assert(G::NT == TN, "jump geometry must use the kernel's threads");
@@ -178,7 +190,7 @@ k_batch32xk(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
             const BatchItem *__restrict__ items, char *__restrict__ out,
             unsigned *__restrict__ counter, uint32_t *__restrict__ stage,
             const uint32_t *__restrict__ polys, int nwords,
-            const uint32_t *__restrict__ prewin) {
+            uint32_t *__restrict__ prewin) {
     constexpr int T = W / K;
     constexpr int PW = GeoK<N, W, B, K>::PW;
     __shared__ __align__(16) uint32_t buf[GeoK<N, W, B, K>::BUF];
@@ -220,8 +232,13 @@ k_batch32xk(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
                 planar = false;
             }
         }
-        if (planar)
-            for (int k = threadIdx.x; k < N; k += T) buf[plane_at<PW, K>(k)] = src[k];
+        if (planar) {
+            uint32_t *clr = preSlot(TK, prewin, stateStride(N));
+            for (int k = threadIdx.x; k < N; k += T) {
+                buf[plane_at<PW, K>(k)] = src[k];
+                if (clr) clr[k] = 0;
+            }
+        }
         __syncthreads();
         for (int i = 0; i < TK.nitems; i++) {
             const BatchItem I = items[TK.first + i];
@@ -255,7 +272,7 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
           const BatchTask *__restrict__ tasks, int ntasks,
           const BatchItem *__restrict__ items, char *__restrict__ out,
           unsigned *__restrict__ counter, uint64_t *__restrict__ stage,
-          const uint32_t *__restrict__ polys, int nwords, const uint64_t *__restrict__ prewin) {
+          const uint32_t *__restrict__ polys, int nwords, uint64_t *__restrict__ prewin) {
     __shared__ __align__(16) uint64_t sbuf[MODE == -2 ? 4 : B];
     uint64_t *const buf = MODE == -2 ? g_mix64 : sbuf;
     __shared__ int s_task;
@@ -269,7 +286,11 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
         Lane64 L;
         L.load(params[T.pidx], threadIdx.x & 31);
         const uint64_t *st = startWindow(T, states, prewin, stateStride(N));
-        for (int k = threadIdx.x; k < N; k += TN) buf[k] = st[k];
+        uint64_t *clr = preSlot(T, prewin, stateStride(N));
+        for (int k = threadIdx.x; k < N; k += TN) {
+            buf[k] = st[k];
+            if (clr) clr[k] = 0;
+        }
         if constexpr (SPLIT && kSplit64<N>) {
             using G = typename SplitGeo64<N>::G;
             static_assert(G::NT == TN, "jump geometry must use the kernel's threads");
@@ -357,7 +378,7 @@ static cudaError_t go(K kern, int tn, const BatchLaunch &b, const P *params, W *
     if (e != cudaSuccess) return e;
     kern<<<grid, tn, smem, s>>>(params, states, b.tasks, b.ntasks, b.items,
                              static_cast<char *>(b.out), b.counter, static_cast<W *>(b.stage),
-                             b.polys, b.nwords, static_cast<const W *>(b.prewin));
+                             b.polys, b.nwords, static_cast<W *>(b.prewin));
     return cudaGetLastError();
 }
 

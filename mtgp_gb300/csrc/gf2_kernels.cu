@@ -269,9 +269,9 @@ cudaError_t launchPowOps(const PowOp *ops, int n, const uint32_t *scratch, int W
     const bool wide = g_pow_window != 2 && powSmemWords<4>(W) * 4 <= kPowSmemMax;
     const size_t smem = 4 * (wide ? powSmemWords<4>(W) : powSmemWords<2>(W));
     auto kern = wide ? k_powops<4> : k_powops<2>;
+    static std::atomic<size_t> seen[2][16];
     cudaError_t e = cudaSuccess;
-    if (smem > 48 * 1024)
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 48 * 1024) e = allowSmem(kern, smem, seen[wide]);
     if (e != cudaSuccess) return e;
     kern<<<n, kPowThreads, smem, s>>>(ops, scratch, W);
     return cudaGetLastError();

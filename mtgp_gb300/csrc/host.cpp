@@ -1030,12 +1030,14 @@ struct mtgp_gpu_plan {
     void *d_stage = nullptr;  // final windows of streams with several tasks
     size_t cap_stage = 0;
     // jumps made ahead of the launch (BatchTask::pre): npre windows, each the
-    // sum of its jump's parts (nparts descriptors in the blob), cleared and
-    // made before every launch
+    // sum of its jump's parts (nparts descriptors in the blob), made before
+    // every launch into slots that are zero (zeroed at allocation, and by the
+    // batched kernel as each task reads its slot)
     int npre = 0, nparts = 0;
     const JumpPart *d_parts = nullptr;
     void *d_prewin = nullptr;
     size_t cap_prewin = 0;
+    bool prewin_fresh = false;  // allocated, not yet zeroed
 
     cudaGraphExec_t exec = nullptr;
     void *graph_out = nullptr;
@@ -1301,6 +1303,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             pl->cap_prewin = 0;
             e = cudaMalloc(&pl->d_prewin, need + need / 4);
             if (e == cudaSuccess) pl->cap_prewin = need + need / 4;
+            pl->prewin_fresh = true;
         }
     }
     if (e != cudaSuccess) {
@@ -1347,6 +1350,15 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     return MTGP_OK;
 }
 
+// Zero a newly allocated pre-jumped window buffer, ordered before the next
+// launch on s (afterwards the batched kernel zeroes each slot as it reads it).
+int clearPrewin(mtgp_gpu_plan *pl, void *s) {
+    if (!pl->prewin_fresh) return MTGP_OK;
+    CK(cudaMemsetAsync(pl->d_prewin, 0, pl->cap_prewin, S(s)), "clear jumped windows");
+    pl->prewin_fresh = false;
+    return MTGP_OK;
+}
+
 // The plan's descriptors to the device, ordered before the next launch on s.
 int uploadPlan(mtgp_gpu_plan *pl, void *s) {
     if (!pl->dirty) return MTGP_OK;
@@ -1378,12 +1390,11 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     if (pl->out_bytes && !out) return setErr(MTGP_ERR_INVALID, "null output pointer");
     int rc = uploadPlan(pl, s);
     if (!rc) rc = powJobs(pl, P.polyWords(), s);
+    if (!rc) rc = clearPrewin(pl, s);
     if (rc) return rc;
-    if (pl->nparts) {  // the start windows jumped ahead of the launch
+    if (pl->nparts) {  // the start windows jumped ahead of the launch, into zeroed slots
         using W = typename T::W;
         W *pre = static_cast<W *>(pl->d_prewin);
-        CK(cudaMemsetAsync(pre, 0, sizeof(W) * (size_t)P.stride * pl->npre, S(s)),
-           "clear jumped windows");
         CK(T::parts(P.sh.mexp, P.d_params, P.d_states, pl->d_polys, P.polyWords(), pre, P.stride,
                     pl->d_parts, pl->nparts, S(s)),
            "jumps ahead of the launch");
@@ -1405,7 +1416,11 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     b.stage_streams = pl->d_stage_streams;
     b.nstage = pl->nstage;
     b.prewin = pl->d_prewin;
-    CK(T::batch(b, P.d_params, P.d_states, S(s)), "batched launch");
+    const cudaError_t e = T::batch(b, P.d_params, P.d_states, S(s));
+    if (e != cudaSuccess) {
+        pl->prewin_fresh = pl->npre > 0;  // the slots may hold jump parts: zero them again
+        return cudaErr(e, "batched launch");
+    }
     return MTGP_OK;
 }
 
@@ -2177,6 +2192,7 @@ int mtgp_gpu_plan_graph_launch(mtgp_gpu_plan_t *pl, void *out, void *s) {
                                           : static_cast<Pool<T64> *>(pl->pool)->polyWords();
             up = powJobs(pl, pw, s);
         }
+        if (!up) up = clearPrewin(pl, s);
         if (up) return up;
         CK(cudaStreamBeginCapture(S(s), cudaStreamCaptureModeThreadLocal), "begin capture");
         int rc = planLaunch(pl, out, s);

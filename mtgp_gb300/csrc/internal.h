@@ -13,6 +13,7 @@
 //                              reference's array[(idx - size + 1 + k) &
 //                              large_mask] (mtgp32-fast.h:165-183).
 #pragma once
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 
@@ -52,6 +53,26 @@ struct Shape {
 #define MTGP_SHAPES64(X) X(11213, 176, 128, 2048) X(23209, 363, 256, 4096) X(44497, 696, 512, 4096) \
     X(110503, 1727, 512, 5760)
 
+
+// Dynamic shared memory of `kern` raised to at least `smem` bytes on the
+// current device; the attribute call is made once per kernel, device and
+// size (servers launch jump kernels for every batch).  `seen` holds, per
+// device, the largest size set so far for this kernel.
+template <class K>
+cudaError_t allowSmem(K kern, size_t smem, std::atomic<size_t> (&seen)[16]) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 16 && seen[dev].load(std::memory_order_acquire) >= smem)
+        return cudaSuccess;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && dev >= 0 && dev < 16) {
+        size_t cur = seen[dev].load(std::memory_order_relaxed);
+        while (cur < smem && !seen[dev].compare_exchange_weak(cur, smem)) {
+        }
+    }
+    return e;
+}
 
 bool shape32(int mexp, Shape *s);
 // Which 32-bit generation core the plain and batched kernels use: 2 = two

@@ -54,8 +54,8 @@ cudaError_t launchParts(const typename Tr::P *params, const typename Tr::W *stat
     using W = typename Tr::W;
     const size_t smem = Geo::template bytes<W>(nwords);
     auto kern = k_jump_part<Tr, Geo>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    static std::atomic<size_t> seen[16];
+    cudaError_t e = allowSmem(kern, smem, seen);
     if (e != cudaSuccess) return e;
     if (nparts <= 0) return cudaSuccess;
     kern<<<nparts, Geo::NT, smem, s>>>(params, states, polys, nwords, dst, stride, parts);
@@ -71,8 +71,8 @@ cudaError_t launch(const typename Tr::P *params, typename Tr::W *states,
     using W = typename Tr::W;
     const size_t smem = Geo::template bytes<W>(nwords);
     auto kern = k_jump<Tr, Geo>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    static std::atomic<size_t> seen[16];
+    cudaError_t e = allowSmem(kern, smem, seen);
     if (e != cudaSuccess) return e;
     if (ndesc <= 0) return cudaSuccess;
     kern<<<ndesc, Geo::NT, smem, s>>>(params, states, descs, nwords);
