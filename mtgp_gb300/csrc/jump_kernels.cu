@@ -31,10 +31,11 @@ k_jump(const typename Tr::P *__restrict__ params, typename Tr::W *__restrict__ s
 // One CTA per (jump, range of tap chunks): partial correlation XOR-ed into
 // the zeroed destination window (jump_device.cuh: jump_part).
 template <class Tr, class Geo>
-__global__ void __launch_bounds__(Geo::NT)
-k_jump_part(const typename Tr::P *__restrict__ params, const typename Tr::W *__restrict__ states,
-            const uint32_t *__restrict__ polys, int nwords, typename Tr::W *__restrict__ dst,
-            int stride, const JumpPart *__restrict__ parts) {
+__device__ __forceinline__ void jumpPart(const typename Tr::P *__restrict__ params,
+                                         const typename Tr::W *__restrict__ states,
+                                         const uint32_t *__restrict__ polys, int nwords,
+                                         typename Tr::W *__restrict__ dst, int stride,
+                                         const JumpPart *__restrict__ parts) {
     using W = typename Tr::W;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     W *smem = reinterpret_cast<W *>(smem_raw);
@@ -48,18 +49,49 @@ k_jump_part(const typename Tr::P *__restrict__ params, const typename Tr::W *__r
 }
 
 template <class Tr, class Geo>
-cudaError_t launchParts(const typename Tr::P *params, const typename Tr::W *states,
-                        const uint32_t *polys, int nwords, typename Tr::W *dst, int stride,
-                        const JumpPart *parts, int nparts, cudaStream_t s) {
+__global__ void __launch_bounds__(Geo::NT)
+k_jump_part(const typename Tr::P *__restrict__ params, const typename Tr::W *__restrict__ states,
+            const uint32_t *__restrict__ polys, int nwords, typename Tr::W *__restrict__ dst,
+            int stride, const JumpPart *__restrict__ parts) {
+    jumpPart<Tr, Geo>(params, states, polys, nwords, dst, stride, parts);
+}
+
+// The same with at most 48 registers, five CTAs per SM, for the 32-bit
+// geometries with groups of four taps: a bench step's 184 jumps × 4 parts
+// then run in one wave on 152 SMs (49 registers allowed four CTAs per SM,
+// 1.2 waves).
+template <class Tr, class Geo>
+__global__ void __launch_bounds__(Geo::NT, 5)
+k_jump_part5(const typename Tr::P *__restrict__ params, const typename Tr::W *__restrict__ states,
+             const uint32_t *__restrict__ polys, int nwords, typename Tr::W *__restrict__ dst,
+             int stride, const JumpPart *__restrict__ parts) {
+    jumpPart<Tr, Geo>(params, states, polys, nwords, dst, stride, parts);
+}
+
+template <class Tr, class Geo, class K>
+cudaError_t launchPartsWith(K kern, const typename Tr::P *params, const typename Tr::W *states,
+                            const uint32_t *polys, int nwords, typename Tr::W *dst, int stride,
+                            const JumpPart *parts, int nparts, cudaStream_t s) {
     using W = typename Tr::W;
     const size_t smem = Geo::template bytes<W>(nwords);
-    auto kern = k_jump_part<Tr, Geo>;
     static std::atomic<size_t> seen[16];
     cudaError_t e = allowSmem(kern, smem, seen);
     if (e != cudaSuccess) return e;
     if (nparts <= 0) return cudaSuccess;
     kern<<<nparts, Geo::NT, smem, s>>>(params, states, polys, nwords, dst, stride, parts);
     return cudaGetLastError();
+}
+
+template <class Tr, class Geo>
+cudaError_t launchParts(const typename Tr::P *params, const typename Tr::W *states,
+                        const uint32_t *polys, int nwords, typename Tr::W *dst, int stride,
+                        const JumpPart *parts, int nparts, cudaStream_t s) {
+    if constexpr (sizeof(typename Tr::W) == 4 && Geo::R <= kQuadTapsMaxR)
+        return launchPartsWith<Tr, Geo>(k_jump_part5<Tr, Geo>, params, states, polys, nwords, dst,
+                                        stride, parts, nparts, s);
+    else
+        return launchPartsWith<Tr, Geo>(k_jump_part<Tr, Geo>, params, states, polys, nwords, dst,
+                                        stride, parts, nparts, s);
 }
 
 template <class Geo>
