@@ -45,7 +45,7 @@ constexpr int32_t kWbNone = -2;
 // (stage slot k -> stream stage_streams[k]) are copied back.
 struct BatchLaunch {
     int mexp, mode, grid;
-    int core;                       // 32-bit generation core (1 or 4) when not split
+    int core;                       // 32-bit generation core: 1, 2 or 4 words per thread
     bool split;
     int nwords;                     // words of every jump polynomial
     const uint32_t *polys;          // jump polynomials, nwords words each
@@ -65,7 +65,7 @@ cudaError_t launchBatch32(const BatchLaunch &b, const DevParams32 *params, uint3
 cudaError_t launchBatch64(const BatchLaunch &b, const DevParams64 *params, uint64_t *states,
                           cudaStream_t s);
 // Number of CTAs of the batched kernel resident at once on the device
-// (32-bit: for the given generation core, 1 or 4).
+// (32-bit: for the given generation core, 1, 2 or 4).
 int batchResident32(int mexp, bool split, int core);
 int batchResident64(int mexp, bool split);
 // Whether split requests are supported for this exponent.

@@ -1801,7 +1801,10 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
         if (b->grid > 0) std::snprintf(grid, sizeof grid, "%d CTAs", b->grid);
         else std::snprintf(grid, sizeof grid, "all resident");
         if (b->npre)
-            std::snprintf(pre, sizeof pre, " after k_jump_part (%d windows jumped ahead)", b->npre);
+            // k_jump_part5 is the 48-register form for 32-bit MEXP 11213
+            std::snprintf(pre, sizeof pre, " after %s (%d windows jumped ahead)",
+                          T::kBits == 32 && P.sh.mexp == 11213 ? "k_jump_part5" : "k_jump_part",
+                          b->npre);
         std::snprintf(line, sizeof line, "chosen: %s%s, chunk=%lld, grid=%s, tasks=%d: %.4f ms\n",
                       kern, pre, (long long)b->chunk, grid, b->ntasks, best_ms);
         rep += line;
