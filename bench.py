@@ -28,6 +28,10 @@ import argparse
 import ctypes
 import json
 import os
+
+# the concurrent plain leg spreads its launches over 32 CUDA streams; give
+# each its own hardware queue (read when the CUDA context is created)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import statistics
 import subprocess
 import sys
@@ -41,6 +45,10 @@ sys.path.insert(0, ROOT)
 N_SUB = 4096
 SEED = 1234
 L2_BYTES = 129 * 2 ** 20
+# DRAM bytes per step of the batched plan's kernels, from one ncu capture
+# each (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (kernel
+# description, split chunk, grid) of the plan captured; see profiles/
+CAPTURED_TRAFFIC = {}
 METRIC = "batched MTGP32-11213 output GB/s"
 WORKLOAD = ("batched: mtgp32_params_fast_11213[0], seed 1234, 4096 substreams j*3^162 "
             "(GPU jump), lognormal lengths median 2^16 sigma 1.0 seed 42 clip [2^10,2^22], uint32")
@@ -230,17 +238,19 @@ def run_reference(args):
 
 
 def run_serving(args, s, local):
-    """Serving section: a check trace whose responses are kept for the
-    oracle, a burst that finds the saturation rate, then Poisson traces at
-    0.3 / 0.6 / 0.9 of it with p50 / p99 latency (submission to the result
-    resident in device memory)."""
+    """Serving section: a check trace, a burst that finds the saturation
+    rate, then Poisson traces at 0.3 / 0.6 / 0.9 of it with p50 / p99
+    latency (submission to the result resident in device memory).  Every
+    request submitted is recorded in order, so that the oracle can place any
+    of them in its stream; from each timed trace a sample of requests (of
+    each output type, the trace's largest, and one planted request of 2^25 +
+    12345 uint32 plus one of 2^24 + 7 uint64 after a jumped offset) gets a
+    device destination and is checked afterwards."""
     import torch
-    from mtgp_gb300.api import Pool, Server, requests, set_tuning
+    from mtgp_gb300.api import Pool, Server, requests
     from mtgp_gb300.params import jump_table, load_table
-    # the library's default planning (the batched section's tuning is global)
-    set_tuning("core", 2)
-    set_tuning("split_chunk", 0)
-    set_tuning("batch_grid", 0)
+    # the library's default planning: the pools below take the process
+    # defaults (the batched section tuned its own pool only)
     p32 = load_table("mtgp32_fast_11213")[0]
     p64 = load_table("mtgp64dc_fast_11213")[0]
     a = Pool.substreams(p32, SEED, 4096, jump_table(32), stream=s)
@@ -248,6 +258,8 @@ def run_serving(args, s, local):
     s.synchronize()
     win_a, win_b = a.windows(), b.windows()
     srv = Server(a, b, budget_bytes=8 << 30, slots=args.serve_slots, max_batch=8192)
+    history = []          # every request submitted, in submission order
+    samples = []          # (index in history, host output)
     # check trace: every response kept for the bit-exact check on the CPU
     rng = np.random.default_rng(7)
     pool, stream, kind, count, skip = serve_trace(rng, 256)
@@ -260,15 +272,37 @@ def run_serving(args, s, local):
         srv.submit(int(pool[k]), int(stream[k]), int(kind[k]), int(count[k]), dst,
                    skip=int(skip[k]))
     srv.drain()
-    check = (pool, stream, kind, count, skip, [o.cpu().numpy() for o in outs], win_a, win_b)
+    base = len(history)
+    history.extend(zip(pool, stream, kind, count, skip))
+    samples.extend((base + k, outs[k].cpu().numpy()) for k in range(256))
     del outs
 
-    def run(tr, arrivals):
+    def run(tr, arrivals, sample=0):
+        req = requests(*tr)
+        picked, bufs = [], []
+        if sample:
+            n = len(req)
+            # planted long requests: above 2^24 values, uint32 and uint64
+            req[n // 2] = (0, req[n // 2]["stream"] % 4096, 0, 0, 0, (1 << 25) + 12345, 0)
+            req[n // 3] = (1, req[n // 3]["stream"] % 256, 0, 0, 1 << 20, (1 << 24) + 7, 0)
+            picked = {n // 2, n // 3, int(np.argmax(req["count"]))}
+            for pool_, kind_ in ((0, 0), (0, 2), (1, 0)):
+                idx = np.flatnonzero((req["pool"] == pool_) & (req["kind"] == kind_))
+                picked.update(int(x) for x in rng.choice(idx, min(sample, idx.size), False))
+            picked = sorted(picked)
+            for k in picked:
+                dt = torch.int32 if req[k]["pool"] == 0 else torch.int64
+                d = torch.empty(int(req[k]["count"]), dtype=dt, device="cuda")
+                bufs.append(d)
+                req["dst"][k] = d.data_ptr()
         c0, b0, k0 = srv.stats()
-        wall = srv.replay(requests(*tr), arrivals)
+        wall = srv.replay(req, arrivals)
         c1, b1, k1 = srv.stats()
         lat, st = srv.results()
         assert (st[c0:c1] == 0).all(), "failed requests"
+        base = len(history)
+        history.extend(zip(req["pool"], req["stream"], req["kind"], req["count"], req["skip"]))
+        samples.extend((base + k, d.cpu().numpy()) for k, d in zip(picked, bufs))
         return wall, b1 - b0, k1 - k0, lat[c0:c1]
 
     rng = np.random.default_rng(11)
@@ -281,7 +315,7 @@ def run_serving(args, s, local):
            "latency": "submission to the result resident in device memory"}
     with Clocks(local) as clk:
         n = args.serve_burst
-        wall, nbytes, batches, lat = run(serve_trace(rng, n), np.zeros(n))
+        wall, nbytes, batches, lat = run(serve_trace(rng, n), np.zeros(n), args.serve_sample)
         sat = n / wall
         out["saturation"] = {"requests": n, "req_per_s": round(sat, 1),
                              "GB_per_s": round(nbytes / wall / 1e9, 2), "batches": batches}
@@ -290,7 +324,7 @@ def run_serving(args, s, local):
             rate = load * sat
             n = max(200, int(rate * args.serve_seconds))
             arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
-            wall, nbytes, batches, lat = run(serve_trace(rng, n), arrivals)
+            wall, nbytes, batches, lat = run(serve_trace(rng, n), arrivals, args.serve_sample)
             rates.append({"load": load, "offered_req_per_s": round(rate, 1), "requests": n,
                           "req_per_s": round(n / wall, 1),
                           "GB_per_s": round(nbytes / wall / 1e9, 2),
@@ -301,7 +335,7 @@ def run_serving(args, s, local):
     out["clocks"] = clk.summary()
     out["scheduler_s"] = {k: round(v, 3) for k, v in srv.profile().items()}
     srv.close()
-    return out, check
+    return out, (history, samples, win_a, win_b)
 
 
 POLY_WORKLOAD = ("jump polynomials X^e mod chi of mtgp32_params_fast_11213[0] on the GPU, "
@@ -401,35 +435,249 @@ def poly_cpu_baseline(orc, seconds):
             "sample": "%d exponents, bit-serial PowerXMod" % n}
 
 
+def full_check(orc, p, start_windows, lens, first_step, last_step, end_windows, nsteps):
+    """Every substream of the first and of the last timed step against the
+    oracle (OpenMP over substreams): the oracle replays all nsteps launches
+    from the substreams' start windows, and the outputs of launch 1 and
+    launch nsteps are compared word for word, then the windows after launch
+    nsteps (word 0 under the state mask, as the reference's own check does,
+    cuda-sample/mtgp32-sample-jump1-host.cu:100-108)."""
+    from mtgp_gb300.params import MTGP32Params, params_array
+    n = len(lens)
+    parr = params_array(MTGP32Params, [p])
+    win = np.ascontiguousarray(start_windows.copy())
+    counts = lens.astype(np.uint64)
+    offs = (np.concatenate([[0], np.cumsum(lens)[:-1]]) * 4).astype(np.uint64)
+    ref = np.empty(int(lens.sum()), dtype=np.uint32)
+    zeros = np.zeros(n, np.int32)
+    t0 = time.perf_counter()
+    res = {"substreams": n, "launches_replayed": nsteps}
+
+    def bad_streams(got):
+        return [j for j in range(n) if not np.array_equal(
+            got[offs[j] // 4:offs[j] // 4 + counts[j]], ref[offs[j] // 4:offs[j] // 4 + counts[j]])]
+
+    for k in range(1, nsteps + 1):
+        orc.multi_fill(32, parr, win, counts, zeros, offs, ref, param_idx=zeros)
+        if k == 1:
+            res["first_step_mismatched_substreams"] = len(bad_streams(first_step))
+        if k == nsteps:
+            res["last_step_mismatched_substreams"] = len(bad_streams(last_step))
+    w0 = ((end_windows[:, 0] ^ win[:, 0]) & np.uint32(p.mask)) == 0
+    res["final_windows_mismatched"] = int((~(w0 & (end_windows[:, 1:] == win[:, 1:]).all(1))).sum())
+    res["bit_exact"] = (res["first_step_mismatched_substreams"] == 0
+                        and res["last_step_mismatched_substreams"] == 0
+                        and res["final_windows_mismatched"] == 0)
+    res["oracle_s"] = round(time.perf_counter() - t0, 2)
+    return res
+
+
+def cpu_rate(orc, bits, plist, pidx, windows, counts, kinds, seconds):
+    """The oracle (OpenMP over streams) on a sample of a bank workload,
+    repeated for about `seconds`: GB/s of output."""
+    from mtgp_gb300.params import MTGP32Params, MTGP64Params, params_array
+    parr = params_array(MTGP32Params if bits == 32 else MTGP64Params, plist)
+    win = np.ascontiguousarray(windows.copy())
+    counts = np.ascontiguousarray(counts, np.uint64)
+    esz = bits // 8
+    offs = (np.concatenate([[0], np.cumsum(counts)[:-1]]) * esz).astype(np.uint64)
+    out = np.empty(int(counts.sum()) * esz, dtype=np.uint8)
+    reps, t0 = 0, time.perf_counter()
+    while reps < 2 or time.perf_counter() - t0 < seconds:
+        orc.multi_fill(bits, parr, win, counts, np.asarray(kinds, np.int32), offs, out,
+                       param_idx=np.asarray(pidx, np.int32))
+        reps += 1
+    dt = time.perf_counter() - t0
+    return round(reps * out.nbytes / dt / 1e9, 3), reps, out.nbytes
+
+
+def write_peak(reps=10):
+    """Store-only HBM bandwidth: a 4 GiB buffer written by torch's fill
+    kernel, best of `reps` (CUDA events); the roofline's copy peak counts a
+    read and a write per byte, this one writes only."""
+    import torch
+    buf = torch.empty(1 << 30, dtype=torch.int32, device="cuda")
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for r in range(reps + 2):
+        ev0.record()
+        buf.fill_(r)
+        ev1.record()
+        ev1.synchronize()
+        if r >= 2:
+            ms = ev0.elapsed_time(ev1)
+            best = ms if best is None else min(best, ms)
+    del buf
+    return round(4 * (1 << 30) / (best * 1e-3) / 1e9, 1)
+
+
+def plain_concurrent(pool, lens, offs, out, nstreams=32, steps=3):
+    """The plain one-launch-per-substream path (one CTA each, as the
+    reference's sample launches one block per generator) with the launches
+    dealt round-robin to `nstreams` CUDA streams, so that many CTAs run at
+    once, captured once into a CUDA graph (no host launch cost) and replayed:
+    ms per step."""
+    import torch
+    n = len(lens)
+    s0 = torch.cuda.Stream()
+    streams = [torch.cuda.Stream() for _ in range(nstreams)]
+
+    def issue():
+        ev = torch.cuda.Event()
+        ev.record(s0)
+        for st in streams:
+            st.wait_event(ev)
+        for j in range(n):
+            pool.fill_stream(j, 0, out, int(lens[j]), stream=streams[j % nstreams],
+                             byte_offset=int(offs[j]))
+        for st in streams:
+            e = torch.cuda.Event()
+            e.record(st)
+            s0.wait_event(e)
+
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s0):
+        issue()
+    g.replay()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(s0):
+        ev0.record(s0)
+        for _ in range(steps):
+            g.replay()
+        ev1.record(s0)
+    s0.synchronize()
+    return ev0.elapsed_time(ev1) / steps
+
+
 def serve_check(orc, chk):
-    """Every response of the check trace against the oracle: each stream
-    replayed in submission order from the windows the pools started from
-    (offsets of 2^17 or more by X^offset mod chi, as the server does)."""
+    """The sampled responses against the oracle.  A request's values start
+    at its stream's position when it is served: the sum of skip + count of
+    every earlier request on that stream, in submission order, plus its own
+    skip.  The oracle goes there from the stream's start window by X^position
+    mod chi when that is 2^17 or more (its bit-serial PowerXMod; the same
+    values as stepping), else by stepping, and fills."""
     from mtgp_gb300.params import load_table
-    pool, stream, kind, count, skip, outs, win_a, win_b = chk
+    history, samples, win_a, win_b = chk
     par = {0: load_table("mtgp32_fast_11213")[0], 1: load_table("mtgp64dc_fast_11213")[0]}
     chis = {}
     for q, p in par.items():
         seq = orc.gen(p, seed=1).fill(0, 2 * p.mexp)
         chis[q] = orc.minpoly((seq & 1).astype(np.uint8))
-    gens, bad = {}, 0
-    for k in range(len(pool)):
-        q, j = int(pool[k]), int(stream[k])
-        if (q, j) not in gens:
-            o = orc.gen(par[q], seed=1)
-            o.set_window((win_a if q == 0 else win_b)[j])
-            gens[(q, j)] = o
-        o = gens[(q, j)]
-        if int(skip[k]) >= (1 << 17):
+    want = {k: o for k, o in samples}
+    pos, where = {}, {}
+    for k, (q, j, kind, count, skip) in enumerate(history):
+        key = (int(q), int(j))
+        start = pos.get(key, 0) + int(skip)
+        pos[key] = start + int(count)
+        if k in want:
+            where[k] = (key, start, int(kind), int(count))
+    bad, big, types = 0, 0, set()
+    for k, o in want.items():
+        (q, j), start, kind, count = where[k]
+        g = orc.gen(par[q], seed=1)
+        g.set_window((win_a if q == 0 else win_b)[j])
+        if start >= (1 << 17):
             d, chi = chis[q]
-            o.jump_words(orc.powxmod(int(skip[k]), chi, d).view(np.uint32)[:351])
+            g.jump_words(orc.powxmod(start, chi, d).view(np.uint32)[:351])
         else:
-            o.skip(int(skip[k]))
-        ref = np.ascontiguousarray(o.fill(int(kind[k]), int(count[k])))
+            g.skip(start)
+        ref = np.ascontiguousarray(g.fill(kind, count))
         dt = np.uint32 if q == 0 else np.uint64
-        bad += not np.array_equal(outs[k].view(dt), ref.view(dt))
-    return {"requests": len(pool), "mismatches": int(bad), "bit_exact": bad == 0,
-            "jumped": int((skip >= (1 << 17)).sum())}
+        bad += not np.array_equal(np.ascontiguousarray(o).view(dt), ref.view(dt))
+        big += count > (1 << 24)
+        types.add((q, kind))
+    return {"requests_checked": len(want), "mismatches": int(bad), "bit_exact": bad == 0,
+            "above_2^24_values": int(big),
+            "types": sorted({(0, 0): "uint32", (0, 2): "float32 [0,1)", (1, 0): "uint64"}.get(
+                t, str(t)) for t in types),
+            "requests_in_history": len(history)}
+
+
+BANK_WORKLOADS = {
+    32: "bank: mtgp32_params_fast_11213[0..127], set i seeded 1234+i, one generator per set: "
+        "2^21 uint32, then 2^21 float32 [0,1) per set",
+    64: "bank: mtgp64dc_params_fast_11213[0..199] (the shipped 64-bit table), set i seeded "
+        "5678+i, one generator per set: 2^20 uint64, then 2^20 float64 [1,2) per set"}
+
+
+def run_bank(s, bits, table, nsets, seed0, n, kinds, hbm, reps=5):
+    """A bank of generators, one per parameter set, each producing n values
+    of each kind in turn: the plain path (pool fill, one CTA per set, like
+    the reference's sample kernels) and the batched planner (autotuned;
+    long requests split by jumps) on the first kind.  Device-resident
+    output, CUDA-event timed, median of `reps`; the first fill of the first
+    kind is kept with the windows it started from for the oracle's check."""
+    import torch
+    from mtgp_gb300.api import Pool, work_items
+    from mtgp_gb300.params import load_table
+    tbl = load_table(table)
+    plist = [tbl[i] for i in range(nsets)]
+    bank = Pool.create(plist, np.arange(nsets) + seed0)
+    dt = torch.int32 if bits == 32 else torch.int64
+    bout = torch.empty(nsets * n, dtype=dt, device="cuda")
+    nbytes = nsets * n * bits // 8
+    res = {"workload": BANK_WORKLOADS[bits], "bytes_per_step": nbytes}
+    start = bank.windows()
+    bank.fill(kinds[0][0], bout, n, stream=s)
+    s.synchronize()
+    first = bout.view(-1).cpu().numpy().copy()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            ev0.record(s)
+            fn()
+            ev1.record(s)
+            s.synchronize()
+            ts.append(ev0.elapsed_time(ev1))
+        return sorted(ts)[len(ts) // 2]
+
+    for kind, name in kinds:
+        bank.fill(kind, bout, n, stream=s)  # warm-up
+        ms = timed(lambda: bank.fill(kind, bout, n, stream=s))
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        res["plain " + name] = {"value": round(gbs, 2), "unit": "GB/s", "ms": round(ms, 4),
+                                "pct_hbm": round(100 * gbs / hbm, 2),
+                                "launch": "%d CTAs, one per set" % nsets}
+    kind, name = kinds[0]
+    items = work_items(np.arange(nsets), np.full(nsets, kind), np.full(nsets, n),
+                       np.arange(nsets) * n * bits // 8)
+    t0 = time.perf_counter()
+    plan, _ = bank.autotune(items, bout, stream=s, reps=3)
+    setup_s = time.perf_counter() - t0
+    plan.launch(bout, s)
+    ms = timed(lambda: plan.launch(bout, s))
+    gbs = nbytes / (ms * 1e-3) / 1e9
+    res["batched " + name] = {"value": round(gbs, 2), "unit": "GB/s", "ms": round(ms, 4),
+                              "pct_hbm": round(100 * gbs / hbm, 2), "plan": plan.describe(),
+                              "setup_s": round(setup_s, 2)}
+    res["_check"] = (bits, plist, start, n, kinds[0][0], first)
+    return res
+
+
+def bank_cpu(orc, bank, seconds, sample=16):
+    """Oracle rate on the first `sample` sets of a bank (OpenMP over sets),
+    and the GPU's first fill of those sets against it."""
+    bits, plist, start, n, kind, first = bank.pop("_check")
+    esz = bits // 8
+    gbs, reps, nb = cpu_rate(orc, bits, plist[:sample], np.arange(sample), start[:sample],
+                             np.full(sample, n), np.full(sample, kind), seconds)
+    from mtgp_gb300.params import MTGP32Params, MTGP64Params, params_array
+    parr = params_array(MTGP32Params if bits == 32 else MTGP64Params, plist)
+    nsets = len(plist)
+    win = np.ascontiguousarray(start.copy())
+    ref = np.empty(nsets * n * esz, dtype=np.uint8)
+    offs = (np.arange(nsets) * n * esz).astype(np.uint64)
+    orc.multi_fill(bits, parr, win, np.full(nsets, n, np.uint64), np.full(nsets, kind, np.int32),
+                   offs, ref, param_idx=np.arange(nsets, dtype=np.int32))
+    ok = bool(np.array_equal(first.view(np.uint8), ref))
+    bank["cpu_baseline"] = {"value": gbs, "unit": "GB/s", "cores": orc.max_threads(),
+                            "kind": "port", "sample": "first %d sets x %d values, %d repetitions"
+                                                      % (sample, n, reps)}
+    bank["first_fill_bit_exact_all_sets"] = ok
 
 
 def main():
@@ -453,6 +701,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-slots", type=int, default=8,
                     help="batches the server keeps in flight (CUDA streams)")
+    ap.add_argument("--serve-sample", type=int, default=10,
+                    help="requests of each output type checked per timed serving trace")
     ap.add_argument("--uniform", type=int, default=0,
                     help="profiling runs: every substream requests this many values "
                          "(steady-state throughput instead of the lognormal workload)")
@@ -510,6 +760,25 @@ def main():
 
     items = work_items(np.arange(nsub), np.zeros(nsub), lens, offs)
     out = torch.empty(total_bytes // 4, dtype=torch.int32, device="cuda")
+
+    # --- cold: a fresh pool's substream setup, a plan with the library's
+    # defaults and its first launch (the library's kernels already loaded) ---
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cpool = Pool.substreams(p, replica_seed(rank), nsub, jump_table(32), stream=s)
+    s.synchronize()
+    t1 = time.perf_counter()
+    cplan = cpool.plan(items)
+    t2 = time.perf_counter()
+    cplan.launch(out, s)
+    s.synchronize()
+    t3 = time.perf_counter()
+    cold = {"value": round(total_bytes / (t3 - t0) / 1e9, 2), "unit": "GB/s",
+            "ms": round(1e3 * (t3 - t0), 2), "setup_ms": round(1e3 * (t1 - t0), 2),
+            "plan_ms": round(1e3 * (t2 - t1), 2), "first_launch_ms": round(1e3 * (t3 - t2), 2),
+            "what": "fresh pool: substream setup (GPU jumps) + plan (library defaults, first "
+                    "use of the parameter set's jump tables) + first launch, host-timed"}
+    del cplan, cpool
     # the library's autotuner picks the plan (core, split chunk, grid) on this
     # workload; the pool's windows are left as they were
     t0 = time.perf_counter()
@@ -521,14 +790,15 @@ def main():
     plan_tasks, plan_chunk = plan.info()
     plan_cfg = plan.describe()
     # plans made later (the e2e leg) use the same configuration
-    set_tuning("core", plan_cfg["core"])
-    set_tuning("split_chunk", plan_cfg["split_chunk"] or -1)
-    set_tuning("batch_grid", plan_cfg["grid"])
+    pool.set_tuning("core", plan_cfg["core"])
+    pool.set_tuning("split_chunk", plan_cfg["split_chunk"] or -1)
+    pool.set_tuning("batch_grid", plan_cfg["grid"])
+    pool.set_tuning("jump_overlap", plan_cfg["overlap"])
 
-    # first step, kept for the CPU-baseline leg's bit-exact check
+    # first step, kept for the bit-exact checks
     plan.launch(out, s)
     s.synchronize()
-    first_step = out[:int(lens[:256].sum())].cpu().numpy().view(np.uint32).copy()
+    first_step = out.cpu().numpy().view(np.uint32).copy()
     if args.only in ("bank", "serve"):
         args.steps = 0
 
@@ -549,6 +819,10 @@ def main():
         barrier()
     ms = max_over_ranks(max(ev0.elapsed_time(ev1) / max(args.steps, 1), 1e-6), world)
     value = job_value(world, total_bytes, ms)
+    # the last timed step's output and the windows after it, for the check
+    last_step = out.cpu().numpy().view(np.uint32).copy() if args.steps else None
+    end_windows = pool.windows()
+    nlaunched = 1 + args.warmup + args.steps
     # the persistent kernel (+ the staged-window copy of split plans) per
     # step; the work-counter reset is a memset, not a kernel
     launches = plan_cfg["kernels_per_launch"] * args.steps
@@ -588,9 +862,10 @@ def main():
     s.synchronize()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / max(e2e_steps, 1), world)
     e2e = job_value(world, total_bytes, e2e_s * 1e3)
+    del outs, host_out, plans
     # the plain and bank legs run on the default generation core, not on the
     # batched plan's
-    set_tuning("core", 2)
+    pool.set_tuning("core", 2)
 
     # --- plain: one launch (one CTA) per substream ---
     plain_ms = None
@@ -603,45 +878,21 @@ def main():
         ev1.record(s)
         s.synchronize()
         plain_ms = ev0.elapsed_time(ev1) / args.plain_steps
+    # the same launches spread over 32 CUDA streams, from a CUDA graph
+    plain_conc_ms = None
+    if args.plain_steps > 0:
+        plain_conc_ms = plain_concurrent(pool, lens, offs, out, nstreams=32,
+                                         steps=max(args.plain_steps, 3))
 
-    # --- bank: 128 parameter sets, 2^21 uint32 each, one CTA per set ---
-    bank_reps = 0 if args.only in ("batched", "serve") else 5
-    tbl = load_table("mtgp32_fast_11213")
-    bank = Pool.create([tbl[i] for i in range(128)], np.arange(128) + 1234)
-    nb = 1 << 21
-    bout = torch.empty(128 * nb, dtype=torch.int32, device="cuda")
-    for _ in range(2):
-        bank.fill(0, bout, nb, stream=s)
-    s.synchronize()
-    ev0.record(s)
-    for _ in range(bank_reps):
-        bank.fill(0, bout, nb, stream=s)
-    ev1.record(s)
-    s.synchronize()
-    bank_ms = max(ev0.elapsed_time(ev1) / max(bank_reps, 1), 1e-6)
-    bank_gbs = 128 * nb * 4 / (bank_ms * 1e-3) / 1e9
-    # the same bank through the batched planner: each set's 2^21 values split
-    # into chunks that start with in-kernel jumps (autotuned; the first plan
-    # computes 128 characteristic and jump polynomials, outside the timing)
-    bank_b = None
-    if bank_reps:
-        bitems = work_items(np.arange(128), np.zeros(128), np.full(128, nb),
-                            np.arange(128) * nb * 4)
-        t0 = time.perf_counter()
-        bplan, _ = bank.autotune(bitems, bout, stream=s, reps=3)
-        setup_s = time.perf_counter() - t0
-        for _ in range(3):
-            bplan.launch(bout, s)
-        s.synchronize()
-        ev0.record(s)
-        for _ in range(bank_reps):
-            bplan.launch(bout, s)
-        ev1.record(s)
-        s.synchronize()
-        bb_ms = max(ev0.elapsed_time(ev1) / bank_reps, 1e-6)
-        bank_b = {"value": round(128 * nb * 4 / (bb_ms * 1e-3) / 1e9, 2), "unit": "GB/s",
-                  "ms": round(bb_ms, 3), "plan": bplan.describe(),
-                  "setup_s": round(setup_s, 2)}
+    # --- banks: one CTA per parameter set (the reference sample's launch
+    # shape), then the same work through the batched planner ---
+    hbm, peak_kind = peaks()
+    banks = {}
+    if args.only in ("all", "bank"):
+        banks["bank32"] = run_bank(s, 32, "mtgp32_fast_11213", 128, 1234, 1 << 21,
+                                   ((0, "uint32"), (2, "float32 [0,1)")), hbm)
+        banks["bank64"] = run_bank(s, 64, "mtgp64dc_fast_11213", 200, 5678, 1 << 20,
+                                   ((0, "uint64"), (1, "float64 [1,2)")), hbm)
 
     # --- jump polynomials for arbitrary offsets, on the GPU ---
     polys, single = None, None
@@ -654,22 +905,25 @@ def main():
     if rank == 0 and not args.no_serve and args.only in ("all", "serve"):
         serve, serve_chk = run_serving(args, s, local)
 
-    hbm, peak_kind = peaks()
+    # --- store-only HBM bandwidth, beside the copy peak of the roofline ---
+    wpeak = write_peak() if rank == 0 and args.only == "all" else None
+
     state_bytes = 2 * nsub * 351 * 4
     achieved = (total_bytes + state_bytes) / (ms * 1e-3) / 1e9
     chosen = [l for l in tune_report.splitlines() if l.startswith("chosen:")]
     kernel = chosen[0][len("chosen:"):].split(", chunk=")[0].strip() if chosen else None
-    # DRAM bytes (read + write) of one launch of the batched kernel on this
-    # workload, measured once with ncu (dram__bytes_read.sum +
-    # dram__bytes_write.sum = 11.58 MB + 1.69 GB); only valid for the full
-    # default workload
-    traffic = 1.70e9 if (nsub == N_SUB and args.uniform <= 0) else None
+    # DRAM bytes (read + write) per step of the plan's kernels, from an ncu
+    # capture of the same plan on the same workload (profiles/); reported
+    # only when the autotuner chose the captured plan
+    plan_key = (kernel, plan_cfg["split_chunk"], plan_cfg["grid"])
+    cap = CAPTURED_TRAFFIC.get(plan_key) if (nsub == N_SUB and args.uniform <= 0) else None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
-                "traffic": traffic, "algorithmic_bytes": total_bytes + state_bytes,
-                "kernel": kernel}
+                "traffic": cap["bytes"] if cap else None,
+                "traffic_source": cap["source"] if cap else "no capture of this plan",
+                "algorithmic_bytes": total_bytes + state_bytes, "kernel": kernel}
 
-    cpu = None
+    cpu, check = None, None
     if rank == 0 and not args.no_cpu:
         from oracle.bind import Oracle, build as obuild
         obuild()
@@ -681,11 +935,18 @@ def main():
                "sample": "first 256 substreams of the workload (%d uint32), %d repetitions"
                          % (words, reps),
                "gpu_first_step_bit_exact": ok}
+        if last_step is not None:
+            check = full_check(orc, p, start_windows, lens, first_step, last_step, end_windows,
+                               nlaunched)
+        for bk in banks.values():
+            bank_cpu(orc, bk, min(args.cpu_seconds, 3.0))
         if serve_chk is not None:
             serve["check"] = serve_check(orc, serve_chk)
         if polys is not None:
             polys["cpu_baseline"] = poly_cpu_baseline(orc, min(args.cpu_seconds, 5.0))
 
+    for bk in banks.values():
+        bk.pop("_check", None)
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": "GB/s",
@@ -700,11 +961,22 @@ def main():
             "plain": None if plain_ms is None else {
                 "value": round(world * total_bytes / (plain_ms * 1e-3) / 1e9, 3), "unit": "GB/s",
                 "ms_per_step": round(plain_ms, 2), "launches_per_step": nsub},
+            "plain_concurrent": None if plain_conc_ms is None else {
+                "value": round(world * total_bytes / (plain_conc_ms * 1e-3) / 1e9, 3),
+                "unit": "GB/s", "ms_per_step": round(plain_conc_ms, 3),
+                "launches_per_step": nsub,
+                "how": "one CTA per substream, launches dealt to 32 CUDA streams, replayed "
+                       "from one CUDA graph"},
             "batched_over_plain": None if plain_ms is None else round(plain_ms / ms, 2),
-            "bank_batched": bank_b,
-            "bank": None if not bank_reps else {
-                "value": round(bank_gbs, 2), "unit": "GB/s", "ms": round(bank_ms, 3),
-                "workload": "128 sets x 2^21 uint32, seeds 1234+i, one CTA per set"},
+            "batched_over_plain_concurrent": None if plain_conc_ms is None
+            else round(plain_conc_ms / ms, 2),
+            "write_peak": None if wpeak is None else {
+                "value": wpeak, "unit": "GB/s",
+                "how": "4 GiB written by one torch fill kernel, best of 10",
+                "pct_of_write_peak": round(100 * value / world / wpeak, 2)},
+            "check": check,
+            "cold": cold,
+            "banks": banks or None,
             "single": single,
             "jump_setup": {"ms": round(jump_ms, 2), "us_per_substream": round(1e3 * jump_ms / nsub, 2)},
             "plan": {"tasks": plan_tasks, "split_chunk": plan_chunk, "config": plan_cfg,

@@ -287,8 +287,10 @@ int mtgp32_gpu_pool_create_by_str(mtgp32_gpu_pool_t **out,
 /* Substream pool: stream j = (para, seed) jumped ahead by j * step, where
  * jump_table row k (nwords words each) is X^(4^k * step) mod chi, the layout
  * of the reference's jump tables (cuda-sample/mtgp32-jump-table.h:6-13).
- * count <= 4^rows.  The jumps run on the GPU (mirrors
- * cuda-sample/mtgp32-jump-kernel.cuh:383-423). */
+ * count <= 4^rows.  The jumps run on the GPU: the same rows in the same
+ * order as the reference's table walk (cuda-sample/mtgp32-jump-kernel.cuh:
+ * 383-423), so the windows are identical to it, but made by doubling (level
+ * k jumps windows [0, 2^k) into [2^k, 2^(k+1))), one jump per substream. */
 int mtgp32_gpu_pool_create_substreams(mtgp32_gpu_pool_t **out,
                                       const mtgp32_params_fast_t *para,
                                       uint32_t seed, int count,
@@ -406,13 +408,22 @@ int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *plan, int64_t *tasks,
  * length (0 = none), [2] generation core (1, 2 or 4), [3] grid (0 = all
  * resident CTAs), [4] kernels one launch runs, [5] 1 if tasks start with
  * in-kernel jumps, [6] tasks that start from a window jumped ahead of the
- * launch (by jump parts, before the persistent kernel).  Passing [1]-[3] to
- * mtgp_gpu_set_tuning ("core", "split_chunk" (-1 for 0), "batch_grid")
- * makes plans of the same kind. */
+ * launch (by jump parts, before the persistent kernel), [7] 1 if those
+ * tasks run in a second launch beside the first ("jump_overlap").  Passing
+ * [1]-[3] and [7] to mtgp32/64_gpu_pool_set_tuning ("core", "split_chunk"
+ * (-1 for 0), "batch_grid", "jump_overlap") makes plans of the same kind. */
 int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
                            int n);
-/* Process-wide tuning knobs for plans made afterwards (no reference
- * counterpart; the autotuner and tests use them):
+/* Tuning knobs (no reference counterpart; the autotuner and tests use
+ * them).  Every pool and single generator carries its own knobs:
+ * mtgp_gpu_set_tuning sets the process-wide defaults that pools and
+ * generators created afterwards start from (existing handles keep theirs),
+ * and the *_set_tuning calls below change one handle's knobs for the plans
+ * and fills it makes afterwards.  Tuning one handle never changes another's
+ * plans, so a server's scheduler thread is not affected by tuning calls on
+ * other threads.  A handle's own knobs follow the handle's single-owner
+ * rule: do not change them while another thread plans with the handle.
+ * Keys:
  *   "split_chunk"  0 = automatic, < 0 = never split, > 0 = chunk length
  *   "batch_grid"   0 = one CTA per resident slot, > 0 = that many CTAs
  *   "core"         32-bit generation core: 2 = two adjacent words per
@@ -427,8 +438,21 @@ int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *plan, int64_t *values,
  *                  such a fill, and batched tasks that start with one jump):
  *                  CTAs per jump, 0 = automatic (4), > 0 = that many (at
  *                  most one per tap chunk of the jump kernel); -1 = such
- *                  jumps run inside the batched kernel instead */
+ *                  jumps run inside the batched kernel instead
+ *   "jump_overlap" 0 = the jump parts run before the persistent launch;
+ *                  1 = they run on a side stream of the plan, followed there
+ *                  by a second persistent launch of the tasks that start
+ *                  from their windows, while the caller's stream runs the
+ *                  other tasks (fork and join by events) */
 int mtgp_gpu_set_tuning(const char *key, int64_t value);
+int mtgp32_gpu_pool_set_tuning(mtgp32_gpu_pool_t *pool, const char *key,
+                               int64_t value);
+int mtgp64_gpu_pool_set_tuning(mtgp64_gpu_pool_t *pool, const char *key,
+                               int64_t value);
+int mtgp32_gpu_gen_set_tuning(mtgp32_gpu_t *gen, const char *key,
+                              int64_t value);
+int mtgp64_gpu_gen_set_tuning(mtgp64_gpu_t *gen, const char *key,
+                              int64_t value);
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
 
 /* ========================================================================= */
@@ -449,10 +473,16 @@ void mtgp_gpu_plan_free(mtgp_gpu_plan_t *plan);
  * every GPU that loads the library until the process exits): at most 16
  * parameter sets and 2048 items per call, larger requests are rejected with
  * MTGP_ERR_INVALID.  The first call on a device looks up the array's device
- * address, so it should come before any stream capture.  Every call
- * overwrites the array: calls whose GPU work overlaps (other streams, other
- * host threads) race and must be serialised by the caller.  The call returns
- * once the descriptors are uploaded; generation runs on `stream`. */
+ * address and keeps it for the life of the process, so it should come
+ * before any stream capture, and no call may follow a cudaDeviceReset of
+ * that device.  Every call overwrites the array: calls whose GPU work
+ * overlaps (other streams, other host threads) race and must be serialised
+ * by the caller.  Each call first waits for all work already queued on
+ * `stream` (a host-side synchronisation: the descriptors come from host
+ * memory, and the previous call may still be reading the array), uploads
+ * the descriptors and returns; generation then runs on `stream`.  On a
+ * stream that is being captured, which cannot be synchronised, it returns
+ * MTGP_ERR_UNSUPPORTED and leaves the stream untouched. */
 int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
                              const int *param_idx, uint32_t *dev_windows,
                              int nstreams, const mtgp_work_item_t *items,
@@ -518,9 +548,10 @@ int mtgp_server_results(mtgp_server_t *s, double *latency, int *status,
                         uint64_t cap, uint64_t *n);
 int mtgp_server_stats(mtgp_server_t *s, uint64_t *completed, uint64_t *bytes,
                       uint64_t *batches);
-/* Time the scheduler thread spent so far, in seconds: [0] admitting
- * requests, [1] planning and launching batches, [2] retiring batches,
- * [3] waiting for work (the first n of these four). */
+/* Host time spent so far, in seconds: [0] admitting requests (the
+ * scheduler thread), [1] planning and launching batches and [2] retiring
+ * them (summed over the slots' worker threads, which run in parallel),
+ * [3] the scheduler waiting for work (the first n of these four). */
 int mtgp_server_profile(mtgp_server_t *s, double *seconds, int n);
 /* Submit n requests at their arrival times (seconds after the call starts),
  * then drain; wall_s receives the elapsed time. */

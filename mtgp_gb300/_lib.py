@@ -68,6 +68,8 @@ for B, P, W in ((32, P32, c_u32), (64, P64, c_u64)):
     pre = "mtgp%d_gpu_" % B
     SIGS.update({
         pre + "init": (c_int, [pp, P, W]),
+        pre + "gen_set_tuning": (c_int, [vp, cp, ctypes.c_int64]),
+        pre + "pool_set_tuning": (c_int, [vp, cp, ctypes.c_int64]),
         pre + "init_by_array": (c_int, [pp, P, vp, c_int]),
         pre + "init_by_str": (c_int, [pp, P, cp]),
         pre + "free": (None, [vp]),

@@ -77,6 +77,10 @@ class _Gen:
         out = torch.empty(n, dtype=_dtype(self.bits, kind), device=device)
         return self.fill_into(kind, out, n, stream)
 
+    def set_tuning(self, key, value):
+        """This generator's tuning knob (the keys of set_tuning)."""
+        check(getattr(self._L, self.pre + "gen_set_tuning")(self.h, key.encode(), int(value)))
+
     def skip(self, n, stream=None):
         check(getattr(self._L, self.pre + "skip")(self.h, n, _stream(stream)))
 
@@ -165,13 +169,13 @@ class Plan:
 
     def describe(self):
         """Configuration: tasks, split chunk, core, grid, kernels per launch,
-        in-kernel jumps, tasks from windows jumped ahead of the launch (see
-        mtgp_gpu_plan_describe)."""
-        v = np.zeros(7, dtype=np.int64)
-        check(lib().mtgp_gpu_plan_describe(self.h, v.ctypes.data_as(ctypes.c_void_p), 7))
+        in-kernel jumps, tasks from windows jumped ahead of the launch, and
+        whether those run beside the others (see mtgp_gpu_plan_describe)."""
+        v = np.zeros(8, dtype=np.int64)
+        check(lib().mtgp_gpu_plan_describe(self.h, v.ctypes.data_as(ctypes.c_void_p), 8))
         return {"tasks": int(v[0]), "split_chunk": int(v[1]), "core": int(v[2]),
                 "grid": int(v[3]), "kernels_per_launch": int(v[4]), "jumps": bool(v[5]),
-                "prejumps": int(v[6])}
+                "prejumps": int(v[6]), "overlap": int(v[7])}
 
     def launch(self, out, stream=None):
         check(lib().mtgp_gpu_plan_launch(self.h, ctypes.c_void_p(out.data_ptr()), _stream(stream)))
@@ -193,8 +197,12 @@ class Plan:
 
 
 def set_tuning(key, value):
-    """Process-wide knobs for plans made afterwards: "split_chunk" (0 auto,
-    <0 never, >0 chunk length) and "batch_grid" (0 auto, >0 CTAs)."""
+    """Process-wide default knobs, taken by pools and generators created
+    afterwards (existing ones keep theirs; Pool.set_tuning and
+    MTGP32.set_tuning change one handle's): "split_chunk" (0 auto, <0 never,
+    >0 chunk length), "batch_grid" (0 auto, >0 CTAs), "core" (1, 2, 4),
+    "poly_window" (0, 2, 4), "single_chunk" (0 auto), "jump_parts" (0 auto,
+    -1 in-kernel)."""
     check(lib().mtgp_gpu_set_tuning(key.encode(), int(value)))
 
 
@@ -299,6 +307,11 @@ class Pool:
     def fill_stream(self, s, kind, out, n, stream=None, byte_offset=0):
         check(getattr(lib(), self.pre + "fill_stream")(
             self.h, s, kind, ctypes.c_void_p(out.data_ptr() + byte_offset), n, _stream(stream)))
+
+    def set_tuning(self, key, value):
+        """This pool's tuning knob for the plans and fills it makes afterwards
+        (the keys of set_tuning)."""
+        check(getattr(lib(), self.pre + "set_tuning")(self.h, key.encode(), int(value)))
 
     def plan(self, items):
         ph = ctypes.c_void_p()

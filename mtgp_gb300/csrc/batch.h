@@ -64,6 +64,12 @@ cudaError_t launchBatch32(const BatchLaunch &b, const DevParams32 *params, uint3
                           cudaStream_t s);
 cudaError_t launchBatch64(const BatchLaunch &b, const DevParams64 *params, uint64_t *states,
                           cudaStream_t s);
+// Staged final windows back to their streams (the copy launchBatch runs
+// after its kernel when nstage > 0), on its own.
+cudaError_t launchUnstage32(int mexp, uint32_t *states, const void *stage,
+                            const int32_t *streams, int nstage, cudaStream_t s);
+cudaError_t launchUnstage64(int mexp, uint64_t *states, const void *stage,
+                            const int32_t *streams, int nstage, cudaStream_t s);
 // Number of CTAs of the batched kernel resident at once on the device
 // (32-bit: for the given generation core, 1, 2 or 4).
 int batchResident32(int mexp, bool split, int core);

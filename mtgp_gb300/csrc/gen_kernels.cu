@@ -10,10 +10,6 @@
 
 namespace mtgp {
 
-static int g_core32 = 2;  // the fastest per generator and in steady state
-int genCore32() { return g_core32; }
-void setGenCore32(int c) { g_core32 = (c == 1 || c == 4) ? c : 2; }
-
 bool shape32(int mexp, Shape *s) {
 #define X(M, N, T, B) \
     if (mexp == M) { *s = {M, N, T, B}; return true; }
@@ -111,10 +107,10 @@ k_gen64(const DevParams64 *__restrict__ params, const int *__restrict__ pidx,
 template <int N, int TN, int B>
 static cudaError_t gen32_kind(int kind, const DevParams32 *params, const int *pidx,
                               uint32_t *states, int ngen, void *out, uint64_t n,
-                              uint64_t os, cudaStream_t s) {
+                              uint64_t os, cudaStream_t s, int core) {
     dim3 grid(ngen), block(TN);
-    if (genCore32() == 4) return gen32xk<N, TN, B, 4>(kind, params, pidx, states, ngen, out, n, os, s);
-    if (genCore32() == 2) return gen32xk<N, TN, B, 2>(kind, params, pidx, states, ngen, out, n, os, s);
+    if (core == 4) return gen32xk<N, TN, B, 4>(kind, params, pidx, states, ngen, out, n, os, s);
+    if (core != 1) return gen32xk<N, TN, B, 2>(kind, params, pidx, states, ngen, out, n, os, s);
     switch (kind) {
     case -1: k_gen32<N, TN, B, -1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
     case 0: k_gen32<N, TN, B, 0><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
@@ -146,10 +142,10 @@ static cudaError_t gen64_kind(int kind, const DevParams64 *params, const int *pi
 
 cudaError_t launchGen32(int mexp, int kind, const DevParams32 *params, const int *pidx,
                         uint32_t *states, int ngen, void *out, uint64_t n,
-                        uint64_t os, cudaStream_t s) {
+                        uint64_t os, cudaStream_t s, int core) {
     if (ngen <= 0 || n == 0) return cudaSuccess;
 #define X(M, N, T, B) \
-    if (mexp == M) return gen32_kind<N, T, B>(kind, params, pidx, states, ngen, out, n, os, s);
+    if (mexp == M) return gen32_kind<N, T, B>(kind, params, pidx, states, ngen, out, n, os, s, core);
     MTGP_SHAPES32(X)
 #undef X
     return cudaErrorInvalidValue;

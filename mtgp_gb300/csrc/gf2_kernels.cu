@@ -241,13 +241,10 @@ __global__ void k_gather_pow2(const uint32_t *blk, size_t tw, int W, uint32_t *o
 }
 
 constexpr size_t kPowSmemMax = 200 * 1024;
-int g_pow_window = 0;  // 0: 4 bits where the table fits, else 2
 
 }  // namespace
 
 bool powOpsFits(int W) { return W > 0 && powSmemWords<2>(W) * 4 <= kPowSmemMax; }
-
-void setPowWindow(int bits) { g_pow_window = bits; }
 
 cudaError_t launchMonomials(uint32_t *blk, size_t tw, int W, int n, int i0, cudaStream_t s) {
     if (n <= 0 || i0 <= 0) return cudaSuccess;
@@ -263,10 +260,10 @@ cudaError_t launchGatherPow2(const uint32_t *blk, size_t tw, int W, int n, uint3
 }
 
 cudaError_t launchPowOps(const PowOp *ops, int n, const uint32_t *scratch, int W,
-                         cudaStream_t s) {
+                         cudaStream_t s, int window) {
     if (n <= 0) return cudaSuccess;
     if (!powOpsFits(W)) return cudaErrorInvalidValue;
-    const bool wide = g_pow_window != 2 && powSmemWords<4>(W) * 4 <= kPowSmemMax;
+    const bool wide = window != 2 && powSmemWords<4>(W) * 4 <= kPowSmemMax;
     const size_t smem = 4 * (wide ? powSmemWords<4>(W) : powSmemWords<2>(W));
     auto kern = wide ? k_powops<4> : k_powops<2>;
     static std::atomic<size_t> seen[2][16];

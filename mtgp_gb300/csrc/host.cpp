@@ -10,9 +10,12 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -24,6 +27,35 @@
 #include "pow_sched.h"
 
 namespace mtgp {
+
+// Allocation wrappers with the test hook MTGP_TEST_FAIL_ALLOC (internal.h).
+namespace {
+std::atomic<long long> g_alloc_count{0};
+long long failAllocAt() {
+    static const long long k = [] {
+        const char *v = std::getenv("MTGP_TEST_FAIL_ALLOC");
+        return v && *v ? std::atoll(v) : -1LL;
+    }();
+    return k;
+}
+bool injectFailure() {
+    const long long k = failAllocAt();
+    return k >= 0 && g_alloc_count.fetch_add(1) == k;
+}
+}  // namespace
+
+cudaError_t devMallocRaw(void **p, size_t bytes) {
+    if (injectFailure()) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+cudaError_t devMallocAsyncRaw(void **p, size_t bytes, cudaStream_t s) {
+    if (injectFailure()) return cudaErrorMemoryAllocation;
+    return cudaMallocAsync(p, bytes, s);
+}
+cudaError_t hostAllocRaw(void **p, size_t bytes) {
+    if (injectFailure()) return cudaErrorMemoryAllocation;
+    return cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+}
 
 void toDev(const mtgp32_params_fast_t &p, DevParams32 *d) {
     std::memset(d, 0, sizeof *d);
@@ -72,7 +104,9 @@ int mtgp::recordError(int code, const char *msg) { return setErr(code, "%s", msg
 namespace {
 
 int cudaErr(cudaError_t e, const char *what) {
-    return setErr(MTGP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    // an allocation that failed is the reference's -1 (mtgp32-fast.c:47-51)
+    return setErr(e == cudaErrorMemoryAllocation ? MTGP_ERR_ALLOC : MTGP_ERR_CUDA, "%s: %s", what,
+                  cudaGetErrorString(e));
 }
 
 #define CK(call, what)                                   \
@@ -98,13 +132,61 @@ constexpr uint64_t kMaxGenSkip = uint64_t(1) << 34;
 // (split single fills, and batched tasks that start with one jump): 0 =
 // four, at most one per tap chunk of the jump kernel; -1 = such jumps run
 // inside the batched kernel instead.
+// core: the 32-bit generation core (2 = two words per thread, 4 = four, 1
+// = one); poly_window: bits per comb window of the GPU's polynomial
+// products (0 = automatic, 2, 4).  Every pool and single generator carries
+// its own copy, taken from the process defaults when it is created, so
+// tuning one handle (or changing the defaults) never changes another's plans.
 struct Tuning {
     int64_t split_chunk = 0;
     int64_t batch_grid = 0;
     int64_t single_chunk = 0;
     int64_t jump_parts = 0;
+    int core = 2;
+    int poly_window = 0;
+    // jump_overlap: 1 = tasks that start from windows jumped ahead of the
+    // launch run in a second persistent launch on a side stream right after
+    // the jump parts, while the first launch runs every other task
+    int jump_overlap = 0;
 };
-Tuning g_tune;
+std::mutex g_tune_mu;
+Tuning g_tune_default;  // mtgp_gpu_set_tuning: defaults for new handles
+
+Tuning tuningDefaults() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return g_tune_default;
+}
+
+// One tuning key applied to t (the keys of mtgp_gpu_set_tuning).
+int applyTuning(Tuning &t, const char *key, int64_t value) {
+    if (!key) return setErr(MTGP_ERR_INVALID, "null key");
+    if (!std::strcmp(key, "split_chunk")) {
+        t.split_chunk = value;
+    } else if (!std::strcmp(key, "core")) {
+        if (value != 1 && value != 2 && value != 4)
+            return setErr(MTGP_ERR_INVALID, "core must be 1, 2 or 4");
+        t.core = (int)value;
+    } else if (!std::strcmp(key, "poly_window")) {
+        if (value != 0 && value != 2 && value != 4)
+            return setErr(MTGP_ERR_INVALID, "poly_window must be 0, 2 or 4");
+        t.poly_window = (int)value;
+    } else if (!std::strcmp(key, "batch_grid")) {
+        if (value < 0) return setErr(MTGP_ERR_INVALID, "batch_grid must be >= 0");
+        t.batch_grid = value;
+    } else if (!std::strcmp(key, "single_chunk")) {
+        if (value < 0) return setErr(MTGP_ERR_INVALID, "single_chunk must be >= 0");
+        t.single_chunk = value;
+    } else if (!std::strcmp(key, "jump_parts")) {
+        if (value < -1) return setErr(MTGP_ERR_INVALID, "jump_parts must be >= -1");
+        t.jump_parts = value;
+    } else if (!std::strcmp(key, "jump_overlap")) {
+        if (value != 0 && value != 1) return setErr(MTGP_ERR_INVALID, "jump_overlap must be 0 or 1");
+        t.jump_overlap = (int)value;
+    } else {
+        return setErr(MTGP_ERR_INVALID, "unknown tuning key '%s'", key);
+    }
+    return MTGP_OK;
+}
 
 // Jumps made ahead of a batched launch run as four CTAs each: every part
 // regenerates the sequence up to its taps, so one CTA per tap chunk (11 for
@@ -113,8 +195,8 @@ constexpr int kJumpParts = 4;
 
 // CTAs per jump made ahead of a batched launch, for a jump of tchunks tap
 // chunks (tuning knob jump_parts).
-int jumpParts(int tchunks) {
-    const int64_t p = g_tune.jump_parts > 0 ? g_tune.jump_parts : kJumpParts;
+int jumpParts(const Tuning &t, int tchunks) {
+    const int64_t p = t.jump_parts > 0 ? t.jump_parts : kJumpParts;
     return (int)std::min<int64_t>(p, tchunks);
 }
 
@@ -129,8 +211,8 @@ struct T32 {
     static constexpr int kBits = 32;
     static bool shape(int mexp, Shape *s) { return shape32(mexp, s); }
     static cudaError_t gen(int mexp, int kind, const DP *p, const int *pi, W *st, int ng,
-                           void *out, uint64_t n, uint64_t os, cudaStream_t s) {
-        return launchGen32(mexp, kind, p, pi, st, ng, out, n, os, s);
+                           void *out, uint64_t n, uint64_t os, cudaStream_t s, int core) {
+        return launchGen32(mexp, kind, p, pi, st, ng, out, n, os, s, core);
     }
     static cudaError_t jump(int mexp, const DP *p, W *st, const JumpDesc *d, int nd, int nw,
                             cudaStream_t s) {
@@ -138,6 +220,10 @@ struct T32 {
     }
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch32(b, p, st, s);
+    }
+    static cudaError_t unstage(int mexp, W *st, const void *stage, const int32_t *streams, int n,
+                               cudaStream_t s) {
+        return launchUnstage32(mexp, st, stage, streams, n, s);
     }
     static cudaError_t parts(int mexp, const DP *p, const W *st, const uint32_t *polys, int nw,
                              W *dst, int stride, const JumpPart *d, int nd, cudaStream_t s) {
@@ -175,7 +261,7 @@ struct T64 {
     static constexpr int kBits = 64;
     static bool shape(int mexp, Shape *s) { return shape64(mexp, s); }
     static cudaError_t gen(int mexp, int kind, const DP *p, const int *pi, W *st, int ng,
-                           void *out, uint64_t n, uint64_t os, cudaStream_t s) {
+                           void *out, uint64_t n, uint64_t os, cudaStream_t s, int) {
         return launchGen64(mexp, kind, p, pi, st, ng, out, n, os, s);
     }
     static cudaError_t jump(int mexp, const DP *p, W *st, const JumpDesc *d, int nd, int nw,
@@ -184,6 +270,10 @@ struct T64 {
     }
     static cudaError_t batch(const BatchLaunch &b, const DP *p, W *st, cudaStream_t s) {
         return launchBatch64(b, p, st, s);
+    }
+    static cudaError_t unstage(int mexp, W *st, const void *stage, const int32_t *streams, int n,
+                               cudaStream_t s) {
+        return launchUnstage64(mexp, st, stage, streams, n, s);
     }
     static cudaError_t parts(int mexp, const DP *p, const W *st, const uint32_t *polys, int nw,
                              W *dst, int stride, const JumpPart *d, int nd, cudaStream_t s) {
@@ -248,10 +338,12 @@ struct Pool {
     std::vector<std::vector<gf2::Poly>> pow2;
     // X^steps mod chi, keyed by (parameter set, steps); bounded
     std::map<std::pair<int, uint64_t>, gf2::Poly> jcache;
-    PlanResult plan_scratch;  // reused by every plan of this pool
-    PowSchedule pow_scratch;
-    std::vector<PowOp> powop_scratch;
-    std::vector<JumpPart> part_scratch;
+    // Plans of one pool may be made on several threads at once (a server
+    // plans each slot's batch on its own thread): the polynomial caches and
+    // tables above are read and filled under cache_mu; everything else a
+    // plan needs is the plan's own or thread-local.
+    std::recursive_mutex cache_mu;
+    Tuning tune = tuningDefaults();  // this pool's tuning knobs
 
     ~Pool() {
         for (uint32_t *b : gpow_blocks) cudaFree(b);
@@ -288,15 +380,16 @@ struct Pool {
         }
         std::vector<typename T::DP> dp(np);
         for (int k = 0; k < np; k++) toDev(params[k], &dp[k]);
-        CK(cudaMalloc(&d_params, sizeof(typename T::DP) * np), "cudaMalloc(params)");
-        CK(cudaMalloc(&d_pidx, sizeof(int) * n), "cudaMalloc(pidx)");
-        CK(cudaMalloc(&d_states, sizeof(W) * (size_t)stride * n), "cudaMalloc(states)");
+        CK(devMalloc(&d_params, sizeof(typename T::DP) * np), "devMalloc(params)");
+        CK(devMalloc(&d_pidx, sizeof(int) * n), "devMalloc(pidx)");
+        CK(devMalloc(&d_states, sizeof(W) * (size_t)stride * n), "devMalloc(states)");
         CK(cudaMemcpy(d_params, dp.data(), sizeof(typename T::DP) * np, cudaMemcpyHostToDevice),
            "upload params");
         CK(cudaMemcpy(d_pidx, hpidx.data(), sizeof(int) * n, cudaMemcpyHostToDevice), "upload pidx");
         CK(cudaMemset(d_states, 0, sizeof(W) * (size_t)stride * n), "clear states");
         chi.assign(np, gf2::Poly());
         chideg.assign(np, -1);
+        powWidth();  // set now: plans read it on several threads
         return MTGP_OK;
     }
 
@@ -323,7 +416,7 @@ struct Pool {
     // Integer seeds, seeded on the device (mtgp32-fast.c:119-137).
     int seedAll(const W *seeds) {
         W *d_seeds = nullptr;
-        CK(cudaMalloc(&d_seeds, sizeof(W) * count), "cudaMalloc(seeds)");
+        CK(devMalloc(&d_seeds, sizeof(W) * count), "devMalloc(seeds)");
         cudaError_t e = cudaDeviceSynchronize();
         if (e == cudaSuccess)
             e = cudaMemcpy(d_seeds, seeds, sizeof(W) * count, cudaMemcpyHostToDevice);
@@ -343,8 +436,8 @@ struct Pool {
                 return setErr(MTGP_ERR_INVALID, "bad key offsets at stream %d", i);
         W *d_keys = nullptr;
         uint64_t *d_off = nullptr;
-        cudaError_t e = cudaMalloc(&d_keys, sizeof(W) * (nk ? nk : 1));
-        if (e == cudaSuccess) e = cudaMalloc(&d_off, sizeof(uint64_t) * (count + 1));
+        cudaError_t e = devMalloc(&d_keys, sizeof(W) * (nk ? nk : 1));
+        if (e == cudaSuccess) e = devMalloc(&d_off, sizeof(uint64_t) * (count + 1));
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
         if (e == cudaSuccess && nk)
             e = cudaMemcpy(d_keys, keys, sizeof(W) * nk, cudaMemcpyHostToDevice);
@@ -375,7 +468,8 @@ struct Pool {
         int rc = checkKind(kind);
         if (!rc) rc = checkOut(out, n);
         if (rc) return rc;
-        CK(T::gen(sh.mexp, kind, d_params, d_pidx, d_states, count, out, n, n, S(s)), "generate");
+        CK(T::gen(sh.mexp, kind, d_params, d_pidx, d_states, count, out, n, n, S(s), tune.core),
+           "generate");
         return MTGP_OK;
     }
 
@@ -385,7 +479,7 @@ struct Pool {
         if (!rc && kind >= 0) rc = checkOut(out, n);
         if (rc) return rc;
         CK(T::gen(sh.mexp, kind, d_params, d_pidx + i, d_states + (size_t)i * stride, 1, out, n, n,
-                  S(s)),
+                  S(s), tune.core),
            "generate");
         return MTGP_OK;
     }
@@ -396,13 +490,13 @@ struct Pool {
         if (words > poly_cap) {
             cudaFree(d_poly);
             d_poly = nullptr;
-            CK(cudaMalloc(&d_poly, sizeof(uint32_t) * words), "cudaMalloc(poly)");
+            CK(devMalloc(&d_poly, sizeof(uint32_t) * words), "devMalloc(poly)");
             poly_cap = words;
         }
         if (descs > desc_cap) {
             cudaFree(d_desc);
             d_desc = nullptr;
-            CK(cudaMalloc(&d_desc, sizeof(JumpDesc) * descs), "cudaMalloc(jump descriptors)");
+            CK(devMalloc(&d_desc, sizeof(JumpDesc) * descs), "devMalloc(jump descriptors)");
             desc_cap = descs;
         }
         return MTGP_OK;
@@ -469,9 +563,9 @@ struct Pool {
         W *d_out = nullptr;
         uint32_t *d_C = nullptr;
         int *d_L = nullptr;
-        cudaError_t e = cudaMalloc(&d_out, sizeof(W) * n2 * n);
-        if (e == cudaSuccess) e = cudaMalloc(&d_C, sizeof(uint32_t) * (size_t)nw * n);
-        if (e == cudaSuccess) e = cudaMalloc(&d_L, sizeof(int) * n);
+        cudaError_t e = devMalloc(&d_out, sizeof(W) * n2 * n);
+        if (e == cudaSuccess) e = devMalloc(&d_C, sizeof(uint32_t) * (size_t)nw * n);
+        if (e == cudaSuccess) e = devMalloc(&d_L, sizeof(int) * n);
         if (e == cudaSuccess) rc = tmp.fillAll(0, d_out, n2, nullptr);
         if (e == cudaSuccess && !rc) e = T::bm(d_out, (int)n2, n, nw, d_C, d_L);
         std::vector<uint32_t> C((size_t)nw * n);
@@ -605,10 +699,10 @@ struct Pool {
         PowOp *d_ops = nullptr;
         cudaStream_t st = nullptr;
         const size_t nstage = (size_t)n * 64 * W;  // >= n * W (chi)
-        cudaError_t e = cudaMalloc(&blk, sizeof(uint32_t) * TW * n);
-        if (e == cudaSuccess) e = cudaMalloc(&stage, sizeof(uint32_t) * nstage);
+        cudaError_t e = devMalloc(&blk, sizeof(uint32_t) * TW * n);
+        if (e == cudaSuccess) e = devMalloc(&stage, sizeof(uint32_t) * nstage);
         if (e == cudaSuccess)
-            e = cudaMalloc(&d_ops, sizeof(PowOp) * (size_t)(sq.steps() + tabs.steps()));
+            e = devMalloc(&d_ops, sizeof(PowOp) * (size_t)(sq.steps() + tabs.steps()));
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaMemsetAsync(blk, 0, sizeof(uint32_t) * TW * n, st);
         if (e == cudaSuccess)
@@ -631,7 +725,7 @@ struct Pool {
         for (const PowSchedule *sc : {&sq, &tabs})
             for (size_t l = 0; e == cudaSuccess && l < sc->levels.size(); l++) {
                 const int m = (int)sc->levels[l].size();
-                e = launchPowOps(d_ops + first, m, nullptr, W, st);
+                e = launchPowOps(d_ops + first, m, nullptr, W, st, tune.poly_window);
                 first += (size_t)m;
             }
         // host copies of X^(2^i)
@@ -749,8 +843,8 @@ struct Pool {
         const size_t bytes = ((out_bytes + 255) & ~size_t(255)) + ops_bytes +
                              sizeof(uint32_t) * (size_t)sch.nscratch * W;
         unsigned char *d = nullptr;
-        CK(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, cache_stream),
-           "cudaMallocAsync(cache products)");
+        CK(devMallocAsync(reinterpret_cast<void **>(&d), bytes, cache_stream),
+           "devMallocAsync(cache products)");
         uint32_t *d_out = reinterpret_cast<uint32_t *>(d);
         PowOp *d_ops = reinterpret_cast<PowOp *>(d + ((out_bytes + 255) & ~size_t(255)));
         uint32_t *d_scratch = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(d_ops) +
@@ -762,7 +856,7 @@ struct Pool {
         size_t first = 0;
         for (size_t l = 0; e == cudaSuccess && l < sch.levels.size(); l++) {
             const int m = (int)sch.levels[l].size();
-            e = launchPowOps(d_ops + first, m, d_scratch, W, cache_stream);
+            e = launchPowOps(d_ops + first, m, d_scratch, W, cache_stream, tune.poly_window);
             first += (size_t)m;
         }
         std::vector<uint32_t> h((size_t)n * W);
@@ -798,7 +892,7 @@ struct Pool {
         unsigned char *d = nullptr;
         const size_t ops_bytes = (sizeof(PowOp) * (size_t)sch.steps() + 255) & ~size_t(255);
         const size_t bytes = ops_bytes + sizeof(uint32_t) * (size_t)sch.nscratch * W;
-        CK(cudaMallocAsync(reinterpret_cast<void **>(&d), bytes, S(s)), "cudaMallocAsync(products)");
+        CK(devMallocAsync(reinterpret_cast<void **>(&d), bytes, S(s)), "devMallocAsync(products)");
         uint32_t *scratch = reinterpret_cast<uint32_t *>(d + ops_bytes);
         std::vector<PowOp> ops;
         powOps(sch, [t](int) { return t; }, out, scratch, chideg[k], ops);
@@ -807,7 +901,8 @@ struct Pool {
         size_t first = 0;
         for (size_t l = 0; e == cudaSuccess && l < sch.levels.size(); l++) {
             const int m = (int)sch.levels[l].size();
-            e = launchPowOps(reinterpret_cast<const PowOp *>(d) + first, m, scratch, W, S(s));
+            e = launchPowOps(reinterpret_cast<const PowOp *>(d) + first, m, scratch, W, S(s),
+                             tune.poly_window);
             first += (size_t)m;
         }
         cudaError_t f = cudaFreeAsync(d, S(s));
@@ -907,28 +1002,43 @@ struct Pool {
         CK(cudaStreamSynchronize(S(s)), "synchronize");
         CK(cudaMemcpy(d_poly, table, sizeof(uint32_t) * rows * nwords, cudaMemcpyHostToDevice),
            "upload jump table");
+        // Doubling: level k makes windows [2^k, 2^(k+1)) from windows
+        // [0, 2^k), each by one jump of X^(2^k * step) = table row k/2,
+        // applied twice for odd k (the table holds the steps 4^r * step).
+        // Window j then went through the rows of the reference's table walk
+        // (cuda-sample/mtgp32-jump-kernel.cuh:383-401: bit b of j applies
+        // row b/2 once or twice, lowest bit first) in the same order, so the
+        // windows are bit-identical to it, with one jump per substream
+        // instead of up to 2 * rows; the levels run one launch each.
         std::vector<JumpDesc> descs;
         descs.reserve(count);
-        for (int j = 1; j < count; j++) {
-            JumpDesc d{};
-            for (int b = 0; b < 31; b++) {
-                if (!((j >> b) & 1)) continue;
-                if (d.nchain + 2 > kMaxChain)
-                    return setErr(MTGP_ERR_INVALID, "substream %d needs more than %d jumps", j,
-                                  kMaxChain);
-                const uint32_t *row = d_poly + (size_t)(b / 2) * nwords;
+        std::vector<int> level_end;
+        for (int k = 0; k < 31 && (1 << k) < count; k++) {
+            if (k / 2 >= rows)
+                return setErr(MTGP_ERR_INVALID, "%d substreams need more than %d table rows",
+                              count, rows);
+            const uint32_t *row = d_poly + (size_t)(k / 2) * nwords;
+            for (int j = 0; j < (1 << k) && j + (1 << k) < count; j++) {
+                JumpDesc d{};
                 d.poly[d.nchain++] = row;
-                if (b & 1) d.poly[d.nchain++] = row;
+                if (k & 1) d.poly[d.nchain++] = row;
+                d.pidx = hpidx[j];
+                d.src = (uint64_t)j * stride;
+                d.dst = (uint64_t)(j + (1 << k)) * stride;
+                descs.push_back(d);
             }
-            d.pidx = hpidx[j];
-            d.src = d.dst = (uint64_t)j * stride;
-            descs.push_back(d);
+            level_end.push_back((int)descs.size());
         }
         if (descs.empty()) return MTGP_OK;
         CK(cudaMemcpy(d_desc, descs.data(), sizeof(JumpDesc) * descs.size(),
                       cudaMemcpyHostToDevice),
            "upload descriptors");
-        CK(T::jump(sh.mexp, d_params, d_states, d_desc, (int)descs.size(), nwords, S(s)), "jump");
+        int first = 0;
+        for (int end : level_end) {
+            CK(T::jump(sh.mexp, d_params, d_states, d_desc + first, end - first, nwords, S(s)),
+               "jump");
+            first = end;
+        }
         return MTGP_OK;
     }
 
@@ -1038,11 +1148,22 @@ struct mtgp_gpu_plan {
     void *d_prewin = nullptr;
     size_t cap_prewin = 0;
     bool prewin_fresh = false;  // allocated, not yet zeroed
+    // jump_overlap: tasks [nmain, ntasks) start from pre-jumped windows and
+    // run in a second persistent launch on `side`, after the jump parts
+    // there, beside the launch of tasks [0, nmain) on the caller's stream
+    // (fork and join by events, so a graph capture takes both)
+    bool overlap = false;
+    int nmain = 0;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
 
     cudaGraphExec_t exec = nullptr;
     void *graph_out = nullptr;
     ~mtgp_gpu_plan() {
         if (exec) cudaGraphExecDestroy(exec);
+        if (side) cudaStreamDestroy(side);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
         cudaFree(d_stage);
         cudaFree(d_prewin);
         cudaFree(d_pscratch);
@@ -1059,6 +1180,7 @@ struct GpuJob {
     int pidx;
     uint64_t steps;
     int32_t slot;
+    const uint32_t *tab;  // the device tables of parameter set pidx
 };
 
 template <class T>
@@ -1073,7 +1195,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     o.can_jump = T::splits(P.sh.mexp);
     o.jump_min = kJumpMinSkip;
     o.max_gen_skip = kMaxGenSkip;
-    o.chunk_tune = force_chunk ? force_chunk : g_tune.split_chunk;
+    o.chunk_tune = force_chunk ? force_chunk : P.tune.split_chunk;
     // Plans whose generated values mix kinds (a generated skip counts as
     // kind -1) run on the one-word core, whose per-kind loops are out of line
     // at no cost.  The same rule as planCore's mode, decided up front because
@@ -1091,10 +1213,11 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (it.count) addKind(it.kind);
         }
     }
-    const int core = force_core ? force_core : (T::kBits == 32 && kinds == -2) ? 1 : genCore32();
+    const int core = force_core ? force_core : (T::kBits == 32 && kinds == -2) ? 1 : P.tune.core;
     // with jumps made ahead of the launch, the kernel without the jump code
-    o.resident = o.can_jump ? T::resident(P.sh.mexp, g_tune.jump_parts < 0, core) : 1;
-    PlanResult &R = P.plan_scratch;
+    o.resident = o.can_jump ? T::resident(P.sh.mexp, P.tune.jump_parts < 0, core) : 1;
+    // scratch reused by every plan made on this thread
+    static thread_local PlanResult R;
     std::string msg;
     int rc = planCore(items, nitems, o, &R, &msg);
     if (rc) return setErr(rc, "%s", msg.c_str());
@@ -1115,6 +1238,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     constexpr int32_t kGpuSlot = 1 << 29;
     std::vector<GpuJob> gjobs;
     auto polyIndex = [&](int pidx, uint64_t steps, int32_t *idx, bool gpu_ok) -> int {
+        std::lock_guard<std::recursive_mutex> lk(P.cache_mu);
         auto hit = poly_at.find({pidx, steps});
         if (hit == poly_at.end()) {
             int slot;
@@ -1124,7 +1248,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
                 int rc2 = P.gpuPowTables(pidx, &t);  // made now, never during a launch
                 if (rc2) return rc2;
                 slot = kGpuSlot + (int)gjobs.size();
-                gjobs.push_back(GpuJob{pidx, steps, slot});
+                gjobs.push_back(GpuJob{pidx, steps, slot, t});
             } else {
                 const gf2::Poly *p = nullptr;
                 int rc2 = P.jumpPoly(pidx, steps, &p);
@@ -1149,6 +1273,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (std::find(sets.begin(), sets.end(), k) == sets.end()) sets.push_back(k);
             if (pt.off && __builtin_popcountll(pt.off) >= 2) offs.emplace_back(k, pt.off);
         }
+        std::lock_guard<std::recursive_mutex> lk(P.cache_mu);
         rc = P.prepare(sets);
         if (!rc) rc = P.fillCache(offs);
         if (rc) return rc;
@@ -1193,7 +1318,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         remap[(size_t)(gjobs[q].slot - kGpuSlot)] = nhost + (int32_t)q;
         job_steps[q] = gjobs[q].steps;
     }
-    PowSchedule &sch = P.pow_scratch;
+    static thread_local PowSchedule sch;
     powSchedule(job_steps.data(), (int)job_steps.size(), job_steps.empty() ? 1 : P.powWidth(),
                 sch);
     for (BatchTask &t : tasks) {
@@ -1205,12 +1330,12 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     // ahead of the launch by jump parts (jumpParts() CTAs per jump, all
     // SMs at once), so no jump runs inside the persistent kernel; a chain of
     // two (a run start, then a chunk offset) still jumps inside it.
-    std::vector<JumpPart> &jparts = P.part_scratch;
+    static thread_local std::vector<JumpPart> jparts;
     jparts.clear();
     int npre = 0;
-    if (g_tune.jump_parts >= 0 && npolys > 0) {
+    if (P.tune.jump_parts >= 0 && npolys > 0) {
         const int tch = T::jumpChunks(P.sh.mexp, (int)pw);
-        const int parts = jumpParts(tch);
+        const int parts = jumpParts(P.tune, tch);
         for (BatchTask &t : tasks) {
             if (t.j0 < 0 || t.j1 >= 0) continue;
             for (int q = 0; q < parts; q++) {
@@ -1226,6 +1351,15 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             t.pre = ++npre;
             t.j0 = -1;
         }
+    }
+    // jump_overlap: the tasks that start from a pre-jumped window go last,
+    // each group in its longest-first order (a second launch runs them)
+    int nmain = (int)tasks.size();
+    if (P.tune.jump_overlap > 0 && npre > 0) {
+        std::stable_partition(tasks.begin(), tasks.end(),
+                              [](const BatchTask &t) { return t.pre == 0; });
+        nmain = 0;
+        while (nmain < (int)tasks.size() && tasks[(size_t)nmain].pre == 0) nmain++;
     }
     bool split = false;  // the kernel variant with the jump code
     for (const BatchTask &t : tasks) split = split || t.j0 >= 0;
@@ -1247,13 +1381,15 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->ntasks = (int)tasks.size();
     pl->mode = mode;
     pl->out_bytes = out_bytes;
-    pl->grid = (int)g_tune.batch_grid;
+    pl->grid = (int)P.tune.batch_grid;
     pl->split = split;
     pl->core = pl->mode == -2 ? 1 : core;
     pl->chunk = cut ? chunk : 0;
     pl->nstage = (int)stage_streams.size();
     pl->npre = npre;
     pl->nparts = (int)jparts.size();
+    pl->overlap = nmain < (int)tasks.size();
+    pl->nmain = nmain;
     auto align = [](size_t n) { return (n + 255) & ~size_t(255); };
     const size_t off_items = align(sizeof(BatchTask) * tasks.size());
     const size_t off_polys = off_items + align(sizeof(BatchItem) * bitems.size());
@@ -1262,19 +1398,24 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     const size_t off_ss = off_parts + align(sizeof(JumpPart) * jparts.size());
     const size_t bytes = off_ss + sizeof(int32_t) * stage_streams.size();
     cudaError_t e = cudaSuccess;
-    if (!pl->d_counter) e = cudaMalloc(&pl->d_counter, sizeof(unsigned));
+    if (!pl->d_counter) e = devMalloc(&pl->d_counter, 2 * sizeof(unsigned));
+    if (e == cudaSuccess && pl->overlap && !pl->side) {
+        e = cudaStreamCreateWithFlags(&pl->side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->join, cudaEventDisableTiming);
+    }
     if (e == cudaSuccess && bytes > pl->cap_d) {
         cudaFree(pl->d_blob);
         pl->d_blob = nullptr;
         pl->cap_d = 0;
-        e = cudaMalloc(&pl->d_blob, bytes + bytes / 4);
+        e = devMalloc(&pl->d_blob, bytes + bytes / 4);
         if (e == cudaSuccess) pl->cap_d = bytes + bytes / 4;
     }
     if (e == cudaSuccess && bytes > pl->cap_h) {
         cudaFreeHost(pl->h_blob);
         pl->h_blob = nullptr;
         pl->cap_h = 0;
-        e = cudaHostAlloc(&pl->h_blob, bytes + bytes / 4, cudaHostAllocDefault);
+        e = hostAlloc(&pl->h_blob, bytes + bytes / 4);
         if (e == cudaSuccess) pl->cap_h = bytes + bytes / 4;
     }
     if (e == cudaSuccess && (size_t)sch.nscratch * pw > pl->cap_pscratch) {
@@ -1282,7 +1423,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         cudaFree(pl->d_pscratch);
         pl->d_pscratch = nullptr;
         pl->cap_pscratch = 0;
-        e = cudaMalloc(&pl->d_pscratch, sizeof(uint32_t) * (need + need / 4));
+        e = devMalloc(&pl->d_pscratch, sizeof(uint32_t) * (need + need / 4));
         if (e == cudaSuccess) pl->cap_pscratch = need + need / 4;
     }
     if (e == cudaSuccess && pl->nstage) {
@@ -1291,7 +1432,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             cudaFree(pl->d_stage);
             pl->d_stage = nullptr;
             pl->cap_stage = 0;
-            e = cudaMalloc(&pl->d_stage, need + need / 4);
+            e = devMalloc(&pl->d_stage, need + need / 4);
             if (e == cudaSuccess) pl->cap_stage = need + need / 4;
         }
     }
@@ -1301,7 +1442,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             cudaFree(pl->d_prewin);
             pl->d_prewin = nullptr;
             pl->cap_prewin = 0;
-            e = cudaMalloc(&pl->d_prewin, need + need / 4);
+            e = devMalloc(&pl->d_prewin, need + need / 4);
             if (e == cudaSuccess) pl->cap_prewin = need + need / 4;
             pl->prewin_fresh = true;
         }
@@ -1325,10 +1466,10 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     if (!polys.empty()) std::memcpy(h + off_polys, polys.data(), sizeof(uint32_t) * polys.size());
     pl->pow_levels.clear();
     if (sch.steps()) {  // GPU job q writes polynomial nhost + q
-        std::vector<PowOp> &ops = P.powop_scratch;
+        static thread_local std::vector<PowOp> ops;
         uint32_t *dst = reinterpret_cast<uint32_t *>(pl->d_blob + off_polys) + (size_t)nhost * pw;
         std::vector<const uint32_t *> tabs(gjobs.size());
-        for (size_t q = 0; q < gjobs.size(); q++) tabs[q] = P.gpow.at(gjobs[q].pidx);
+        for (size_t q = 0; q < gjobs.size(); q++) tabs[q] = gjobs[q].tab;
         P.powOps(sch, [&tabs](int j) { return tabs[(size_t)j]; }, dst, pl->d_pscratch,
                  P.sh.mexp, ops);
         std::memcpy(h + off_ops, ops.data(), sizeof(PowOp) * ops.size());
@@ -1372,11 +1513,12 @@ int uploadPlan(mtgp_gpu_plan *pl, void *s) {
 // The plan's GPU-made jump polynomials (after the host-made ones in the
 // blob), on s after the upload; they stay valid for later launches until
 // the plan is refilled.
-int powJobs(mtgp_gpu_plan *pl, int pw, void *s) {
+int powJobs(mtgp_gpu_plan *pl, int pw, int window, void *s) {
     if (pl->pow_ready) return MTGP_OK;
     size_t first = 0;
     for (int n : pl->pow_levels) {
-        CK(launchPowOps(pl->d_powops + first, n, pl->d_pscratch, pw, S(s)), "jump polynomials");
+        CK(launchPowOps(pl->d_powops + first, n, pl->d_pscratch, pw, S(s), window),
+           "jump polynomials");
         first += (size_t)n;
     }
     pl->pow_ready = true;
@@ -1389,14 +1531,21 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     if (pl->ntasks == 0) return MTGP_OK;
     if (pl->out_bytes && !out) return setErr(MTGP_ERR_INVALID, "null output pointer");
     int rc = uploadPlan(pl, s);
-    if (!rc) rc = powJobs(pl, P.polyWords(), s);
+    if (!rc) rc = powJobs(pl, P.polyWords(), P.tune.poly_window, s);
     if (!rc) rc = clearPrewin(pl, s);
     if (rc) return rc;
+    // with jump_overlap the jump parts and the tasks that wait for them go
+    // to the side stream
+    cudaStream_t js = pl->overlap ? pl->side : S(s);
+    if (pl->overlap) {
+        CK(cudaEventRecord(pl->fork, S(s)), "fork");
+        CK(cudaStreamWaitEvent(pl->side, pl->fork, 0), "fork");
+    }
     if (pl->nparts) {  // the start windows jumped ahead of the launch, into zeroed slots
         using W = typename T::W;
         W *pre = static_cast<W *>(pl->d_prewin);
         CK(T::parts(P.sh.mexp, P.d_params, P.d_states, pl->d_polys, P.polyWords(), pre, P.stride,
-                    pl->d_parts, pl->nparts, S(s)),
+                    pl->d_parts, pl->nparts, js),
            "jumps ahead of the launch");
     }
     BatchLaunch b{};
@@ -1416,7 +1565,26 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
     b.stage_streams = pl->d_stage_streams;
     b.nstage = pl->nstage;
     b.prewin = pl->d_prewin;
-    const cudaError_t e = T::batch(b, P.d_params, P.d_states, S(s));
+    cudaError_t e = cudaSuccess;
+    if (pl->overlap) {
+        BatchLaunch b2 = b;
+        b2.tasks = pl->d_tasks + pl->nmain;
+        b2.ntasks = pl->ntasks - pl->nmain;
+        b2.counter = pl->d_counter + 1;
+        b2.nstage = 0;
+        b2.grid = 0;
+        b.ntasks = pl->nmain;
+        b.nstage = 0;
+        e = T::batch(b2, P.d_params, P.d_states, pl->side);
+        if (e == cudaSuccess) e = T::batch(b, P.d_params, P.d_states, S(s));
+        if (e == cudaSuccess) e = cudaEventRecord(pl->join, pl->side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(S(s), pl->join, 0);
+        if (e == cudaSuccess && pl->nstage)
+            e = T::unstage(P.sh.mexp, P.d_states, pl->d_stage, pl->d_stage_streams, pl->nstage,
+                           S(s));
+    } else {
+        e = T::batch(b, P.d_params, P.d_states, S(s));
+    }
     if (e != cudaSuccess) {
         pl->prewin_fresh = pl->npre > 0;  // the slots may hold jump parts: zero them again
         return cudaErr(e, "batched launch");
@@ -1483,7 +1651,7 @@ int fillSplitPlan(Obj *h, int kind, void *out, size_t n, void *s, int sms) {
     it.stream = 0;
     it.kind = kind;
     it.count = n;
-    int64_t chunk = g_tune.split_chunk;
+    int64_t chunk = P.tune.split_chunk;
     if (chunk == 0) {
         chunk = 1 << 17;
         while ((uint64_t)chunk * 2 * (uint64_t)sms < n) chunk <<= 1;
@@ -1510,8 +1678,8 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_tune.jump_parts < 0) return fillSplitPlan<T>(h, kind, out, n, s, sms);
-    int64_t chunk = g_tune.single_chunk > 0 ? g_tune.single_chunk : singleChunk(n, P.sh.mexp);
+    if (P.tune.jump_parts < 0) return fillSplitPlan<T>(h, kind, out, n, s, sms);
+    int64_t chunk = P.tune.single_chunk > 0 ? P.tune.single_chunk : singleChunk(n, P.sh.mexp);
     if ((n + chunk - 1) / chunk > (uint64_t)kMaxFillChunks)
         chunk = (int64_t)((n + kMaxFillChunks - 1) / kMaxFillChunks);
     const int nch = (int)((n + chunk - 1) / chunk);
@@ -1534,7 +1702,7 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
             cudaFree(F.d_polys);
             F.d_polys = nullptr;
             F.cap_polys = 0;
-            CK(cudaMalloc(&F.d_polys, sizeof(uint32_t) * words), "cudaMalloc(chunk polynomials)");
+            CK(devMalloc(&F.d_polys, sizeof(uint32_t) * words), "devMalloc(chunk polynomials)");
             F.cap_polys = words;
         }
         std::vector<uint64_t> steps((size_t)nch - 1);
@@ -1554,13 +1722,13 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
         cudaFree(L.d_win);
         L.d_win = nullptr;
         L.cap_win = 0;
-        CK(cudaMalloc(&L.d_win, win_bytes), "cudaMalloc(chunk windows)");
+        CK(devMalloc(&L.d_win, win_bytes), "devMalloc(chunk windows)");
         L.cap_win = win_bytes;
     }
-    if (!L.d_counter) CK(cudaMalloc(&L.d_counter, sizeof(unsigned)), "cudaMalloc(counter)");
+    if (!L.d_counter) CK(devMalloc(&L.d_counter, sizeof(unsigned)), "devMalloc(counter)");
     W *win = static_cast<W *>(L.d_win);
     const int tchunks = T::jumpChunks(P.sh.mexp, pw);
-    const int parts = jumpParts(tchunks);
+    const int parts = jumpParts(P.tune, tchunks);
     const int nparts = (nch - 1) * parts;
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t off_items = al(sizeof(BatchTask) * (size_t)nch);
@@ -1574,8 +1742,8 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
             cudaFree(L.d_desc);
             L.h_desc = L.d_desc = nullptr;
             L.cap_desc = 0;
-            CK(cudaMallocHost(&L.h_desc, bytes), "cudaMallocHost(fill descriptors)");
-            CK(cudaMalloc(&L.d_desc, bytes), "cudaMalloc(fill descriptors)");
+            CK(hostAlloc(&L.h_desc, bytes), "cudaMallocHost(fill descriptors)");
+            CK(devMalloc(&L.d_desc, bytes), "devMalloc(fill descriptors)");
             L.cap_desc = bytes;
         }
         BatchTask *t = reinterpret_cast<BatchTask *>(L.h_desc);
@@ -1688,23 +1856,24 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
     struct Cand {
         int core;
         int64_t chunk, grid;
+        int overlap;
     };
     std::vector<Cand> cands;
     const int cores[3] = {4, 2, 1};
     const int ncores = T::kBits == 32 ? 3 : 1;
-    for (int c = 0; c < ncores; c++) cands.push_back({cores[c], -1, 0});
+    for (int c = 0; c < ncores; c++) cands.push_back({cores[c], -1, 0, 0});
     if (T::splits(P.sh.mexp))
-        for (int c = 0; c < ncores; c++)
-            for (int64_t ch = 1 << 17; ch <= (1 << 20); ch += 1 << 17)
-                cands.push_back({cores[c], ch, 0});
+        for (int ov = 0; ov < (P.tune.jump_parts >= 0 ? 2 : 1); ov++)
+            for (int c = 0; c < ncores; c++)
+                for (int64_t ch = 1 << 17; ch <= (1 << 20); ch += 1 << 17)
+                    cands.push_back({cores[c], ch, 0, ov});
     const size_t sbytes = sizeof(W) * (size_t)P.stride * P.count;
     W *snap = nullptr;
-    CK(cudaMalloc(&snap, sbytes), "cudaMalloc(autotune snapshot)");
+    CK(devMalloc(&snap, sbytes), "devMalloc(autotune snapshot)");
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const Tuning saved = g_tune;
-    const int saved_core = genCore32();
+    const Tuning saved = P.tune;
     std::string rep;
     float best_ms = 0;
     int rc = MTGP_OK;
@@ -1735,13 +1904,15 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
     for (size_t k = 0; k < cands.size() && !rc; k++) {
         static const int kGridEighths[] = {8, 7, 6, 5, 4};  // of the resident CTAs
         for (int g = 0; g < 5 && !rc; g++) {
-            g_tune.split_chunk = cands[k].chunk;
-            g_tune.batch_grid = 0;
-            setGenCore32(cands[k].core);
+            P.tune.split_chunk = cands[k].chunk;
+            P.tune.batch_grid = 0;
+            P.tune.core = cands[k].core;
+            P.tune.jump_overlap = cands[k].overlap;
             mtgp_gpu_plan *pl = nullptr;
             rc = makePlan(P, items, nitems, &pl);
             if (rc) break;
-            if (cands[k].chunk > 0 && pl->chunk == 0) {  // nothing long enough to split
+            if ((cands[k].chunk > 0 && pl->chunk == 0) ||       // nothing long enough to split
+                (cands[k].overlap && !pl->overlap)) {           // nothing jumped ahead
                 delete pl;
                 break;
             }
@@ -1759,8 +1930,9 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
                 break;
             }
             char line[160];
-            std::snprintf(line, sizeof line, "core=%d chunk=%lld grid=%s tasks=%d: %.4f ms\n",
+            std::snprintf(line, sizeof line, "core=%d chunk=%lld%s grid=%s tasks=%d: %.4f ms\n",
                           T::kBits == 64 ? 1 : pl->core, (long long)pl->chunk,
+                          pl->overlap ? " overlap" : "",
                           g == 0 ? "all" : g == 1 ? "7/8" : g == 2 ? "3/4" : g == 3 ? "5/8" : "1/2",
                           pl->ntasks, ms);
             rep += line;
@@ -1773,8 +1945,7 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
             }
         }
     }
-    g_tune = saved;
-    setGenCore32(saved_core);
+    P.tune = saved;
     ce = cudaMemcpyAsync(P.d_states, snap, sbytes, cudaMemcpyDeviceToDevice, S(s));
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(S(s));
     if (!rc && ce != cudaSuccess) rc = cudaErr(ce, "autotune restore");
@@ -1802,7 +1973,8 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
         else std::snprintf(grid, sizeof grid, "all resident");
         if (b->npre)
             // k_jump_part5 is the 48-register form for 32-bit MEXP 11213
-            std::snprintf(pre, sizeof pre, " after %s (%d windows jumped ahead)",
+            std::snprintf(pre, sizeof pre, " %s %s (%d windows jumped ahead)",
+                          b->overlap ? "beside" : "after",
                           T::kBits == 32 && P.sh.mexp == 11213 ? "k_jump_part5" : "k_jump_part",
                           b->npre);
         std::snprintf(line, sizeof line, "chosen: %s%s, chunk=%lld, grid=%s, tasks=%d: %.4f ms\n",
@@ -2193,7 +2365,9 @@ int mtgp_gpu_plan_graph_launch(mtgp_gpu_plan_t *pl, void *out, void *s) {
         if (!up) {
             const int pw = pl->bits == 32 ? static_cast<Pool<T32> *>(pl->pool)->polyWords()
                                           : static_cast<Pool<T64> *>(pl->pool)->polyWords();
-            up = powJobs(pl, pw, s);
+            const int win = pl->bits == 32 ? static_cast<Pool<T32> *>(pl->pool)->tune.poly_window
+                                           : static_cast<Pool<T64> *>(pl->pool)->tune.poly_window;
+            up = powJobs(pl, pw, win, s);
         }
         if (!up) up = clearPrewin(pl, s);
         if (up) return up;
@@ -2225,38 +2399,38 @@ int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *pl, int64_t *tasks, int64_t *chunk
 
 int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *pl, int64_t *values, int n) {
     if (!pl || (n > 0 && !values)) return setErr(MTGP_ERR_INVALID, "null plan or values");
-    const int64_t v[7] = {pl->ntasks, pl->chunk, pl->bits == 64 ? 1 : pl->core, pl->grid,
-                          pl->ntasks ? 1 + (pl->nstage > 0) + (pl->nparts > 0) : 0,
-                          pl->split ? 1 : 0, pl->npre};
-    for (int k = 0; k < n && k < 7; k++) values[k] = v[k];
+    const int64_t v[8] = {pl->ntasks, pl->chunk, pl->bits == 64 ? 1 : pl->core, pl->grid,
+                          pl->ntasks ? 1 + (pl->nstage > 0) + (pl->nparts > 0) +
+                                           (pl->overlap && pl->nmain > 0)
+                                     : 0,
+                          pl->split ? 1 : 0, pl->npre, pl->overlap ? 1 : 0};
+    for (int k = 0; k < n && k < 8; k++) values[k] = v[k];
     return MTGP_OK;
 }
 
 int mtgp_gpu_set_tuning(const char *key, int64_t value) {
-    if (!key) return setErr(MTGP_ERR_INVALID, "null key");
-    if (!std::strcmp(key, "split_chunk")) {
-        g_tune.split_chunk = value;
-    } else if (!std::strcmp(key, "core")) {
-        if (value != 1 && value != 2 && value != 4)
-            return setErr(MTGP_ERR_INVALID, "core must be 1, 2 or 4");
-        setGenCore32((int)value);
-    } else if (!std::strcmp(key, "poly_window")) {
-        if (value != 0 && value != 2 && value != 4)
-            return setErr(MTGP_ERR_INVALID, "poly_window must be 0, 2 or 4");
-        setPowWindow((int)value);
-    } else if (!std::strcmp(key, "batch_grid")) {
-        if (value < 0) return setErr(MTGP_ERR_INVALID, "batch_grid must be >= 0");
-        g_tune.batch_grid = value;
-    } else if (!std::strcmp(key, "single_chunk")) {
-        if (value < 0) return setErr(MTGP_ERR_INVALID, "single_chunk must be >= 0");
-        g_tune.single_chunk = value;
-    } else if (!std::strcmp(key, "jump_parts")) {
-        if (value < -1) return setErr(MTGP_ERR_INVALID, "jump_parts must be >= -1");
-        g_tune.jump_parts = value;
-    } else {
-        return setErr(MTGP_ERR_INVALID, "unknown tuning key '%s'", key);
-    }
-    return MTGP_OK;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    Tuning t = g_tune_default;
+    const int rc = applyTuning(t, key, value);
+    if (!rc) g_tune_default = t;
+    return rc;
+}
+
+int mtgp32_gpu_pool_set_tuning(mtgp32_gpu_pool_t *p, const char *key, int64_t value) {
+    if (!p) return setErr(MTGP_ERR_INVALID, "null pool");
+    return applyTuning(p->pool.tune, key, value);
+}
+int mtgp64_gpu_pool_set_tuning(mtgp64_gpu_pool_t *p, const char *key, int64_t value) {
+    if (!p) return setErr(MTGP_ERR_INVALID, "null pool");
+    return applyTuning(p->pool.tune, key, value);
+}
+int mtgp32_gpu_gen_set_tuning(mtgp32_gpu_t *h, const char *key, int64_t value) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null generator");
+    return applyTuning(h->pool.tune, key, value);
+}
+int mtgp64_gpu_gen_set_tuning(mtgp64_gpu_t *h, const char *key, int64_t value) {
+    if (!h) return setErr(MTGP_ERR_INVALID, "null generator");
+    return applyTuning(h->pool.tune, key, value);
 }
 
 void mtgp_gpu_plan_free(mtgp_gpu_plan_t *pl) {

@@ -75,11 +75,28 @@ cudaError_t allowSmem(K kern, size_t smem, std::atomic<size_t> (&seen)[16]) {
 }
 
 bool shape32(int mexp, Shape *s);
-// Which 32-bit generation core the plain and batched kernels use: 2 = two
-// adjacent words per thread (default), 4 = four, 1 = one word per thread.
-int genCore32();
-void setGenCore32(int core);
 bool shape64(int mexp, Shape *s);
+
+// Every device and pinned host allocation of the library goes through
+// these.  With MTGP_TEST_FAIL_ALLOC=k in the environment (read once, for
+// tests of the error paths), allocation number k of the process (counted
+// from 0) fails with cudaErrorMemoryAllocation without calling CUDA; unset,
+// they are cudaMalloc, cudaMallocAsync and cudaHostAlloc.
+cudaError_t devMallocRaw(void **p, size_t bytes);
+cudaError_t devMallocAsyncRaw(void **p, size_t bytes, cudaStream_t s);
+cudaError_t hostAllocRaw(void **p, size_t bytes);
+template <class T>
+cudaError_t devMalloc(T **p, size_t bytes) {
+    return devMallocRaw(reinterpret_cast<void **>(p), bytes);
+}
+template <class T>
+cudaError_t devMallocAsync(T **p, size_t bytes, cudaStream_t s) {
+    return devMallocAsyncRaw(reinterpret_cast<void **>(p), bytes, s);
+}
+template <class T>
+cudaError_t hostAlloc(T **p, size_t bytes) {
+    return hostAllocRaw(reinterpret_cast<void **>(p), bytes);
+}
 __host__ __device__ constexpr int stateStride(int n) { return (n + 31) & ~31; }
 
 void toDev(const mtgp32_params_fast_t &p, DevParams32 *d);
@@ -139,14 +156,17 @@ bool powOpsFits(int W);
 cudaError_t launchMonomials(uint32_t *blk, size_t tw, int W, int n, int i0, cudaStream_t s);
 cudaError_t launchGatherPow2(const uint32_t *blk, size_t tw, int W, int n, uint32_t *out,
                              cudaStream_t s);
-void setPowWindow(int bits);  // comb window: 0 automatic, 2 or 4 bits
+// window: bits per comb window of the products, 0 = automatic (4 where the
+// table fits in shared memory, else 2), 2 or 4.
 cudaError_t launchPowOps(const PowOp *ops, int n, const uint32_t *scratch, int W,
-                         cudaStream_t s);
+                         cudaStream_t s, int window = 0);
 
+// core: the 32-bit generation core, 2 = two adjacent words per thread (the
+// default), 4 = four, 1 = one word per thread.
 cudaError_t launchGen32(int mexp, int kind, const DevParams32 *params,
                         const int *pidx, uint32_t *states, int ngen,
                         void *out, uint64_t n, uint64_t outStride,
-                        cudaStream_t s);
+                        cudaStream_t s, int core = 2);
 cudaError_t launchGen64(int mexp, int kind, const DevParams64 *params,
                         const int *pidx, uint64_t *states, int ngen,
                         void *out, uint64_t n, uint64_t outStride,

@@ -15,6 +15,13 @@
 // work overlaps (different streams, or several host threads) race and must
 // be serialised by the caller.  Every GPU that loads the library holds the
 // array until the process exits.
+//
+// Each call waits for all work already queued on its stream before it
+// launches (the descriptors are copied from host memory that must stay
+// valid until the copies have read it, and the previous call's kernel may
+// still be reading the array).  A stream that is being captured cannot be
+// synchronised, so on such a stream the call returns MTGP_ERR_UNSUPPORTED
+// and leaves the stream and its capture untouched.
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -48,8 +55,8 @@ std::mutex g_na_mu;
 unsigned char *g_na_ptr[kNaDevices] = {};
 
 // Device address of the scratch on the current device, looked up once per
-// device (the first call on each device does this, so it should come before
-// any stream capture).
+// device by the first call on it and kept for the life of the process (so
+// the calls must not continue after a cudaDeviceReset of that device).
 cudaError_t scratch(unsigned char **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -85,6 +92,12 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
         return fail(MTGP_ERR_INVALID, "null or empty argument");
     if (nparams > kNaParams) return fail(MTGP_ERR_INVALID, "more than 16 parameter sets");
     if (nitems > kNaItems) return fail(MTGP_ERR_INVALID, "more than 2048 work items");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess)
+        return fail(MTGP_ERR_CUDA, "cannot query the stream");
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(MTGP_ERR_UNSUPPORTED,
+                    "the call synchronises its stream, which is being captured");
     Shape sh;
     if (!shape32(params[0].mexp, &sh)) return fail(MTGP_ERR_UNSUPPORTED, "exponent not supported");
     DevParams32 dp[kNaParams];
@@ -160,7 +173,7 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
     b.mexp = sh.mexp;
     b.mode = mode == -3 ? -1 : mode;
     b.grid = 0;
-    b.core = b.mode == -2 ? 1 : genCore32();  // mixed kinds: the one-word core
+    b.core = b.mode == -2 ? 1 : 2;  // mixed kinds: the one-word core; else two words
     b.split = false;
     b.nwords = 0;
     b.polys = nullptr;

@@ -20,12 +20,20 @@
 //     released; the latency (completion - submission) is recorded.
 // A request's output depends only on its stream's position, so it is the
 // same alone and in any mix.
+//
+// Threads: the scheduler thread only admits (first-come-first-served, the
+// arena, the stream states) and hands each batch to a free slot; every slot
+// has a worker thread that plans and launches its batch (the pools' plans
+// can be made on several threads at once), waits for it on the GPU and
+// retires it (latencies, arena space, stream states).  So the host work of
+// up to `slots` batches runs in parallel instead of on one thread.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -49,8 +57,11 @@ struct Slot {
     cudaStream_t cs = nullptr;
     cudaEvent_t ev = nullptr;
     mtgp_gpu_plan_t *plan[2] = {nullptr, nullptr};
-    std::vector<Req> reqs;
-    bool busy = false;
+    std::vector<Req> reqs;  // the batch (owned by the worker while busy)
+    bool busy = false;      // holds a batch: handed over, launching or on the GPU
+    bool assigned = false;  // handed over, not yet taken by the worker
+    std::thread th;         // the slot's worker
+    std::condition_variable cv;
 };
 
 }  // namespace
@@ -62,7 +73,7 @@ struct mtgp_server {
     int device = 0;
     unsigned char *d_arena = nullptr;
     Arena arena;
-    std::vector<Slot> slots;
+    std::vector<std::unique_ptr<Slot>> slots;
     int max_batch = 4096;
     std::mutex mu;
     std::condition_variable cv, cv_done;
@@ -85,6 +96,7 @@ struct mtgp_server {
                 bool keep, uint64_t *ticket);
 
     void loop();
+    void work(Slot &sl);
     int launch(Slot &sl, std::vector<Req> &reqs);
     int launchBatch(Slot &sl, std::vector<Req> &reqs);
 };
@@ -137,70 +149,74 @@ void mtgp_server::loop() {
     std::unique_lock<std::mutex> lk(mu);
     while (!stop.load()) {
         bool progressed = false;
-        const Clock::time_point tr = Clock::now();
-        // retire finished batches
-        for (Slot &sl : slots) {
-            if (!sl.busy) continue;
-            const cudaError_t q = cudaEventQuery(sl.ev);
-            if (q == cudaErrorNotReady) continue;
-            const Clock::time_point now = Clock::now();
-            for (const Req &r : sl.reqs) {
-                latency[r.ticket - 1] = std::chrono::duration<double>(now - r.t_submit).count();
-                status[r.ticket - 1] = q == cudaSuccess ? MTGP_OK : MTGP_ERR_CUDA;
-                if (r.keep && r.bytes && q == cudaSuccess)
-                    kept[r.ticket] = {r.off, r.bytes};
-                else
-                    arena.release(r.off, r.bytes);
-                busy[r.pool][r.stream] = mtgp::kStreamFree;
-                completed++;
-                bytes_done += r.bytes;
-            }
-            sl.reqs.clear();
-            sl.busy = false;
-            progressed = true;
-        }
-        if (progressed) cv_done.notify_all();
-        prof[2] += std::chrono::duration<double>(Clock::now() - tr).count();
-        // admit pending requests into a free slot
-        Slot *fs = nullptr;
-        for (Slot &sl : slots)
-            if (!sl.busy) {
-                fs = &sl;
-                break;
-            }
-        if (fs && !pending.empty()) {
+        // admit pending requests into the free slots, one batch each
+        for (auto &sp : slots) {
+            if (pending.empty()) break;
+            Slot &sl = *sp;
+            if (sl.busy) continue;
             const Clock::time_point ta = Clock::now();
             std::vector<Req> take;
             mtgp::admitBatch(pending, busy, arena, max_batch, kJumpSkip, &take);
             prof[0] += std::chrono::duration<double>(Clock::now() - ta).count();
-            if (!take.empty()) {
-                lk.unlock();
-                const Clock::time_point tl = Clock::now();
-                const int rc = launch(*fs, take);
-                prof[1] += std::chrono::duration<double>(Clock::now() - tl).count();
-                lk.lock();
-                if (rc) {
-                    for (const Req &r : take) {
-                        latency[r.ticket - 1] = 0;
-                        status[r.ticket - 1] = rc;
-                        arena.release(r.off, r.bytes);
-                        busy[r.pool][r.stream] = mtgp::kStreamFree;
-                        completed++;
-                    }
-                    cv_done.notify_all();
-                } else {
-                    fs->reqs.swap(take);
-                    fs->busy = true;
-                    batches++;
-                }
-                progressed = true;
-            }
+            if (take.empty()) break;  // nothing fits until a batch retires
+            sl.reqs.swap(take);
+            sl.busy = sl.assigned = true;
+            batches++;
+            sl.cv.notify_one();
+            progressed = true;
         }
         if (!progressed) {
+            // woken by a submission, a retired batch or released space
             const Clock::time_point ti = Clock::now();
-            cv.wait_for(lk, std::chrono::microseconds(20));
+            cv.wait_for(lk, std::chrono::milliseconds(1));
             prof[3] += std::chrono::duration<double>(Clock::now() - ti).count();
         }
+    }
+}
+
+void mtgp_server::work(Slot &sl) {
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+        sl.cv.wait(lk, [&] { return sl.assigned || stop.load(); });
+        if (!sl.assigned) break;  // stopping
+        sl.assigned = false;
+        lk.unlock();
+        // plan and launch, then wait for the batch: a short spin, then
+        // sleeps, so the retire follows the GPU closely without holding a
+        // core for long batches
+        const Clock::time_point tl = Clock::now();
+        const int rc = launch(sl, sl.reqs);
+        const Clock::time_point tw = Clock::now();
+        cudaError_t q = cudaSuccess;
+        if (!rc) {
+            for (int spin = 0;; spin++) {
+                q = cudaEventQuery(sl.ev);
+                if (q != cudaErrorNotReady) break;
+                if (spin < 2000) std::this_thread::yield();
+                else std::this_thread::sleep_for(std::chrono::microseconds(20));
+            }
+        }
+        const Clock::time_point now = Clock::now();
+        lk.lock();
+        prof[1] += std::chrono::duration<double>(tw - tl).count();
+        const int st = rc ? rc : q == cudaSuccess ? MTGP_OK : MTGP_ERR_CUDA;
+        for (const Req &r : sl.reqs) {
+            latency[r.ticket - 1] = rc ? 0 : std::chrono::duration<double>(now - r.t_submit).count();
+            status[r.ticket - 1] = st;
+            if (!st && r.keep && r.bytes)
+                kept[r.ticket] = {r.off, r.bytes};
+            else
+                arena.release(r.off, r.bytes);
+            busy[r.pool][r.stream] = mtgp::kStreamFree;
+            completed++;
+            if (!st) bytes_done += r.bytes;
+        }
+        sl.reqs.clear();
+        sl.busy = false;
+        prof[2] += std::chrono::duration<double>(Clock::now() - now).count();
+        cv.notify_one();
+        cv_done.notify_all();
     }
 }
 
@@ -221,22 +237,32 @@ int mtgp_server_create(mtgp_server_t **out, mtgp32_gpu_pool_t *p32, mtgp64_gpu_p
     s->busy[1].assign(s->nstreams[1], 0);
     s->max_batch = max_batch;
     cudaError_t e = cudaGetDevice(&s->device);
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_arena, budget_bytes);
+    if (e == cudaSuccess) e = mtgp::devMalloc(&s->d_arena, budget_bytes);
     if (e != cudaSuccess) {
         delete s;
         return mtgp::recordError(MTGP_ERR_ALLOC, cudaGetErrorString(e));
     }
     s->arena.init(budget_bytes);
-    s->slots.resize(slots);
-    for (Slot &sl : s->slots) {
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.cs, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming);
+    for (int k = 0; k < slots; k++) {
+        s->slots.emplace_back(new (std::nothrow) Slot());
+        Slot *sl = s->slots.back().get();
+        if (!sl) {
+            s->slots.pop_back();
+            e = cudaErrorMemoryAllocation;
+            break;
+        }
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl->cs, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming);
     }
     if (e != cudaSuccess) {
         mtgp_server_destroy(s);
         return mtgp::recordError(MTGP_ERR_CUDA, cudaGetErrorString(e));
     }
     s->t0 = Clock::now();
+    for (auto &sp : s->slots) {
+        Slot *sl = sp.get();
+        sl->th = std::thread([s, sl] { s->work(*sl); });
+    }
     s->th = std::thread([s] { s->loop(); });
     *out = s;
     return MTGP_OK;
@@ -390,13 +416,18 @@ int mtgp_server_replay(mtgp_server_t *s, const mtgp_request_t *reqs, const doubl
 
 void mtgp_server_destroy(mtgp_server_t *s) {
     if (!s) return;
-    if (s->th.joinable()) {
-        mtgp_server_drain(s, 600.0);
+    if (s->th.joinable()) mtgp_server_drain(s, 600.0);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
         s->stop.store(true);
         s->cv.notify_all();
-        s->th.join();
+        for (auto &sp : s->slots) sp->cv.notify_all();
     }
-    for (Slot &sl : s->slots) {
+    if (s->th.joinable()) s->th.join();
+    for (auto &sp : s->slots)
+        if (sp->th.joinable()) sp->th.join();
+    for (auto &sp : s->slots) {
+        Slot &sl = *sp;
         if (sl.cs) cudaStreamSynchronize(sl.cs);
         for (int p = 0; p < 2; p++) mtgp_gpu_plan_free(sl.plan[p]);
         if (sl.ev) cudaEventDestroy(sl.ev);

@@ -97,4 +97,8 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # the reference checkout: argument, MTGP_REFERENCE_DIR, or a directory
+    # named "reference" beside this repository
+    default = os.environ.get("MTGP_REFERENCE_DIR", os.path.normpath(
+        os.path.join(HERE, "..", "..", "..", "reference")))
+    main(sys.argv[1] if len(sys.argv) > 1 else default)

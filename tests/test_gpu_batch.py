@@ -137,7 +137,7 @@ def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core, parts):
     made ahead of the batched kernel by jump parts (parts 0: four CTAs per
     jump) or inside it (parts -1), on each 32-bit generation core: bit-exact
     outputs and final states, across two launches of the same plan."""
-    from mtgp_gb300.api import Pool, set_tuning, work_items
+    from mtgp_gb300.api import Pool, work_items
     if bits == 64 and core != 4:
         pytest.skip("one 64-bit core")
     tbl = load_table(table)
@@ -157,15 +157,10 @@ def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core, parts):
     kinds = list(kinds) + [0]
     counts = list(counts) + [20000]
     offs = list(offs) + [int(sum(counts[:-1])) * esz]
-    set_tuning("split_chunk", 1500)
-    set_tuning("core", core)
-    set_tuning("jump_parts", parts)
-    try:
-        plan = pool.plan(work_items(streams, kinds, counts, offs))
-    finally:
-        set_tuning("split_chunk", 0)
-        set_tuning("core", 2)
-        set_tuning("jump_parts", 0)
+    pool.set_tuning("split_chunk", 1500)
+    pool.set_tuning("core", core)
+    pool.set_tuning("jump_parts", parts)
+    plan = pool.plan(work_items(streams, kinds, counts, offs))
     ntasks, chunk = plan.info()
     assert chunk == 1500 and ntasks > nstreams
     desc = plan.describe()
@@ -188,16 +183,13 @@ def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core, parts):
 def test_batch_split_graph(gpu, orc):
     """The split plan (batched kernel + staged-window copy) replays from a
     CUDA graph."""
-    from mtgp_gb300.api import Pool, set_tuning, work_items
+    from mtgp_gb300.api import Pool, work_items
     p = load_table("mtgp32_fast_11213")[0]
     pool = Pool.substreams(p, 1234, 16, jump_table(32))
     counts = np.array([100000, 5, 70000, 4096] + [3000] * 12)
     offs = np.concatenate([[0], np.cumsum(counts)[:-1]]) * 4
-    set_tuning("split_chunk", 16384)
-    try:
-        plan = pool.plan(work_items(np.arange(16), np.zeros(16), counts, offs))
-    finally:
-        set_tuning("split_chunk", 0)
+    pool.set_tuning("split_chunk", 16384)
+    plan = pool.plan(work_items(np.arange(16), np.zeros(16), counts, offs))
     assert plan.info()[1] == 16384
     start = pool.windows()
     out = torch.zeros(int(counts.sum()), dtype=torch.int32, device="cuda")
@@ -248,7 +240,7 @@ def test_batch_vector_cores_one_kind(gpu, orc, core, kind):
     """The two- and four-word cores on plans of one output kind (no split):
     uneven counts, outputs at every 4-byte alignment (the cores' alignment
     pre-step), a skip item, against the oracle."""
-    from mtgp_gb300.api import Pool, set_tuning, work_items
+    from mtgp_gb300.api import Pool, work_items
     tbl = load_table("mtgp32_fast_11213")
     nstreams = 20
     plist = [tbl[i] for i in range(4)]
@@ -267,13 +259,9 @@ def test_batch_vector_cores_one_kind(gpu, orc, core, kind):
         offs[k] = pos * 4
         if kind >= 0:
             pos += int(counts[k])
-    set_tuning("core", core)
-    set_tuning("split_chunk", -1)
-    try:
-        plan = pool.plan(work_items(np.arange(nstreams), np.full(nstreams, kind), counts, offs))
-    finally:
-        set_tuning("core", 2)
-        set_tuning("split_chunk", 0)
+    pool.set_tuning("core", core)
+    pool.set_tuning("split_chunk", -1)
+    plan = pool.plan(work_items(np.arange(nstreams), np.full(nstreams, kind), counts, offs))
     assert plan.describe()["core"] == core
     out = torch.zeros(pos + 8, dtype=torch.int32, device="cuda")
     plan.launch(out)

@@ -130,16 +130,17 @@ def test_substreams(gpu, orc, bits, table):
     the oracle walking the same table rows (bit b of j applies row b/2 once
     for even b, twice for odd b: cuda-sample/mtgp32-jump-kernel.cuh:383-401);
     equal as a state (word 0 under the mask, outputs exact) to j successive
-    JUMP3_162 jumps of the reference's CPU code."""
+    JUMP3_162 jumps of the reference's CPU code.  1000 substreams: the GPU
+    makes them by doubling in ten levels, the last one partial."""
     from mtgp_gb300.api import Pool
     p = load_table(table)[0]
     tbl = jump_table(bits)
-    count = 70
+    count = 1000
     pool = Pool.substreams(p, 1234, count, tbl)
     win = pool.windows()
     chain = orc.gen(p, seed=1234)
     js = jump_string(bits)
-    for j in list(range(count)):
+    for j in list(range(70)) + [255, 256, 511, 512, 513, 767, 998, 999]:
         o = orc.gen(p, seed=1234)
         for b in range(12):
             if (j >> b) & 1:
@@ -147,11 +148,12 @@ def test_substreams(gpu, orc, bits, table):
                 if b & 1:
                     o.jump_words(tbl[b // 2])
         assert np.array_equal(win[j], o.window()), j
-        c = chain.clone()
-        w = c.window()
-        assert (int(w[0]) ^ int(win[j][0])) & int(p.mask) == 0, j
-        assert np.array_equal(w[1:], win[j][1:]), j
-        chain.fast_jump(js)
+        if j < 70:
+            c = chain.clone()
+            w = c.window()
+            assert (int(w[0]) ^ int(win[j][0])) & int(p.mask) == 0, j
+            assert np.array_equal(w[1:], win[j][1:]), j
+            chain.fast_jump(js)
 
 
 @pytest.mark.parametrize("bits,table,idx,window", [(32, "mtgp32_fast_11213", 0, 0),

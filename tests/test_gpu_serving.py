@@ -150,11 +150,15 @@ def _trace(rng, n, nst32, nst64):
     return reqs
 
 
-def test_server_vs_oracle(gpu, orc):
+@pytest.mark.parametrize("retune", [False, True], ids=["quiet", "retuned"])
+def test_server_vs_oracle(gpu, orc, retune):
     """A random trace through the server (several batches in flight, both
     pools, skips, advance-only requests) equals each stream's sequence
-    replayed in submission order."""
-    from mtgp_gb300.api import Server
+    replayed in submission order.  "retuned": meanwhile another thread keeps
+    changing the process-wide tuning defaults and the knobs of an unrelated
+    pool, which must not touch the server's plans."""
+    import threading
+    from mtgp_gb300.api import Pool, Server, set_tuning
     a, b, p32, p64 = _server_pools()
     ga, gb = _oracle_streams(orc, a, p32), _oracle_streams(orc, b, p64)
     # the oracle's jump polynomials for the jumped skips
@@ -165,14 +169,37 @@ def test_server_vs_oracle(gpu, orc):
     rng = np.random.default_rng(11)
     trace = _trace(rng, 300, 32, 8)
     srv = Server(a, b, budget_bytes=64 << 20, slots=3, max_batch=64)
-    outs, tickets = [], []
-    for pool, st, kind, count, skip in trace:
-        dst = None if kind < 0 else torch.empty(count, dtype=DT[32 if pool == 0 else 64],
-                                                device="cuda")
-        outs.append(dst)
-        tickets.append(srv.submit(pool, st, kind, count, dst, skip=skip))
-    for t in tickets:
-        assert srv.wait(t, 120.0) == 0
+    stop = threading.Event()
+
+    def churn():
+        other = Pool.create([p32], [5], [0])
+        knobs = [("core", (1, 4, 2)), ("split_chunk", (-1, 1500, 0)),
+                 ("batch_grid", (7, 0)), ("jump_parts", (-1, 3, 0))]
+        k = 0
+        while not stop.is_set():
+            key, vals = knobs[k % len(knobs)]
+            set_tuning(key, vals[(k // len(knobs)) % len(vals)])
+            other.set_tuning(key, vals[(k // len(knobs) + 1) % len(vals)])
+            k += 1
+        for key, vals in knobs:
+            set_tuning(key, vals[-1])
+
+    th = threading.Thread(target=churn) if retune else None
+    if th:
+        th.start()
+    try:
+        outs, tickets = [], []
+        for pool, st, kind, count, skip in trace:
+            dst = None if kind < 0 else torch.empty(count, dtype=DT[32 if pool == 0 else 64],
+                                                    device="cuda")
+            outs.append(dst)
+            tickets.append(srv.submit(pool, st, kind, count, dst, skip=skip))
+        for t in tickets:
+            assert srv.wait(t, 120.0) == 0
+    finally:
+        stop.set()
+        if th:
+            th.join()
     lat, status = srv.results()
     assert (status == 0).all() and (lat >= 0).all()
     done, nbytes, batches = srv.stats()
@@ -285,7 +312,7 @@ def test_jumps_across_many_parameter_sets(gpu, orc):
     """Twenty parameter sets that all need in-kernel jumps (more than the
     pool keeps reduction tables for at once, so some are dropped and
     rebuilt): every split request and skip is still bit-exact."""
-    from mtgp_gb300.api import Pool, set_tuning, work_items
+    from mtgp_gb300.api import Pool, work_items
     tbl = load_table("mtgp32_fast_11213")
     n = 20
     plist = [tbl[i] for i in range(n)]
@@ -294,19 +321,16 @@ def test_jumps_across_many_parameter_sets(gpu, orc):
     counts = np.full(n, 5000)
     skips = np.where(np.arange(n) % 3 == 0, 1 << 17, 0)
     offs = np.arange(n) * 5000 * 4
-    set_tuning("split_chunk", 1200)
-    try:
-        for rep in range(2):
-            out = torch.zeros(n * 5000, dtype=torch.int32, device="cuda")
-            pool.submit(work_items(np.arange(n), np.zeros(n), counts, offs, skips), out)
-            torch.cuda.synchronize()
-            got = out.cpu().numpy().view(np.uint32)
-            for k in range(n):
-                o = orc.gen(plist[k], seed=int(seeds[k]))
-                o.skip(int(skips[k]) * (rep + 1) + 5000 * rep)
-                assert np.array_equal(got[k * 5000:(k + 1) * 5000], o.fill(0, 5000)), (rep, k)
-    finally:
-        set_tuning("split_chunk", 0)
+    pool.set_tuning("split_chunk", 1200)
+    for rep in range(2):
+        out = torch.zeros(n * 5000, dtype=torch.int32, device="cuda")
+        pool.submit(work_items(np.arange(n), np.zeros(n), counts, offs, skips), out)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().view(np.uint32)
+        for k in range(n):
+            o = orc.gen(plist[k], seed=int(seeds[k]))
+            o.skip(int(skips[k]) * (rep + 1) + 5000 * rep)
+            assert np.array_equal(got[k * 5000:(k + 1) * 5000], o.fill(0, 5000)), (rep, k)
 
 
 @pytest.mark.parametrize("bits,table", CASES)
@@ -418,3 +442,39 @@ def test_huge_arbitrary_skips(gpu, orc):
     g.skip(skips[0])
     o.jump_words(orc.powxmod(skips[0], chi, d).view(np.uint32)[:nw])
     assert np.array_equal(g.fill_uint32(2000).cpu().numpy().view(np.uint32), o.fill(0, 2000))
+
+
+def test_cancel_pending_request_frees_its_place(gpu, orc):
+    """A request that waits for budget can be cancelled: its status becomes
+    MTGP_ERR_BUSY, its stream is not advanced (it never ran), an admitted
+    request cannot be cancelled, and once the budget is released the next
+    request on the cancelled one's stream starts where that stream stood."""
+    from mtgp_gb300._lib import MTGPError
+    from mtgp_gb300.api import Pool, Server
+    p = load_table("mtgp32_fast_11213")[0]
+    pool = Pool.substreams(p, 1234, 4, jump_table(32))
+    start = pool.windows()
+    n = 200000
+    srv = Server(pool, None, budget_bytes=n * 4 + 4096, slots=2, max_batch=16)
+    try:
+        a = srv.submit(0, 0, 0, n)              # result kept in the arena
+        assert srv.wait(a) == 0
+        b = srv.submit(0, 1, 0, n)              # does not fit while a's result is kept
+        srv.cancel(b)
+        assert srv.wait(b) == -8                # MTGP_ERR_BUSY: cancelled before it ran
+        with pytest.raises(MTGPError):
+            srv.cancel(a)                       # already done
+        got_a = srv.result(a).cpu().numpy().view(np.uint32).copy()
+        srv.release(a)                          # the budget is free again
+        dst = torch.zeros(n, dtype=torch.int32, device="cuda")
+        c = srv.submit(0, 1, 0, n, dst)
+        assert srv.wait(c) == 0
+        got_c = dst.cpu().numpy().view(np.uint32)
+        srv.drain()
+    finally:
+        srv.close()
+    oa, oc = orc.gen(p, seed=1), orc.gen(p, seed=1)
+    oa.set_window(start[0])
+    oc.set_window(start[1])
+    assert np.array_equal(got_a, oa.fill(0, n))
+    assert np.array_equal(got_c, oc.fill(0, n))  # stream 1 was not advanced by b

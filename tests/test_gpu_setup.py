@@ -15,24 +15,21 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("bits,table,nsets", [(32, "mtgp32_fast_11213", 24),
                                               (64, "mtgp64dc_fast_11213", 12)])
 def test_many_sets_split_requests(gpu, orc, bits, table, nsets):
-    from mtgp_gb300.api import Pool, set_tuning, work_items
+    from mtgp_gb300.api import Pool, work_items
     tbl = load_table(table)
     plist = [tbl[i] for i in range(nsets)]
     seeds = np.arange(nsets) + 77
     pool = Pool.create(plist, seeds)
     n = (1 << 20) + 12345 if bits == 32 else (1 << 19) + 999
     esz = bits // 8
-    set_tuning("split_chunk", 1 << 17)
-    try:
-        items = work_items(np.arange(nsets), np.zeros(nsets), np.full(nsets, n),
-                           np.arange(nsets) * n * esz)
-        plan = pool.plan(items)
-        desc = plan.describe()
-        out = torch.zeros(nsets * n * esz // 4, dtype=torch.int32, device="cuda")
-        plan.launch(out)
-        torch.cuda.synchronize()
-    finally:
-        set_tuning("split_chunk", 0)
+    pool.set_tuning("split_chunk", 1 << 17)
+    items = work_items(np.arange(nsets), np.zeros(nsets), np.full(nsets, n),
+                       np.arange(nsets) * n * esz)
+    plan = pool.plan(items)
+    desc = plan.describe()
+    out = torch.zeros(nsets * n * esz // 4, dtype=torch.int32, device="cuda")
+    plan.launch(out)
+    torch.cuda.synchronize()
     assert desc["tasks"] > nsets and (desc["jumps"] or desc["prejumps"])
     got = as_np_bits(out.view(torch.int32 if bits == 32 else torch.int64), bits).reshape(nsets, n)
     for i in range(nsets):

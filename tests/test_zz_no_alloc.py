@@ -4,10 +4,12 @@ It serves callers that cannot allocate device memory: engines whose device
 memory is all reserved up front or under a hard budget, and plug-ins that may
 only use buffers handed to them.  They pass their own window and output
 buffers, and the library keeps the kernel's descriptors in a fixed device
-array.  This test calls it through the C ABI twice in a row and checks each
+array.  These tests call it through the C ABI twice in a row and check each
 call's output and advanced windows bit-exactly against the pool entry point
-(mtgp32_gpu_pool_submit) run on the same windows and items.  The file is
-named so that pytest collects it last.
+(mtgp32_gpu_pool_submit) run on the same windows and items: batches of one
+output kind (the two-word core), batches that mix kinds and advance-only
+items (the one-word core), another exponent, and the default parameter
+index.  The file is named so that pytest collects it last.
 """
 import ctypes
 
@@ -19,54 +21,74 @@ from mtgp_gb300.params import MTGP32Params, load_table
 
 pytestmark = pytest.mark.gpu
 
-STRIDE = 352  # roundup(11213/32 + 1, 32) words per window
+
+def _stride(mexp):
+    return ((mexp // 32 + 1) + 31) // 32 * 32
 
 
-def _items(rng, nstreams, nitems):
+def _items(rng, nstreams, nitems, kinds):
     from mtgp_gb300.api import work_items
     streams = rng.integers(0, nstreams, nitems)
-    kinds = rng.integers(0, 5, nitems)
+    kind = rng.choice(np.asarray(kinds), nitems)
     counts = rng.integers(0, 9000, nitems)
-    offs = np.concatenate([[0], np.cumsum(counts)[:-1]]) * 4
-    return work_items(streams, kinds, counts, offs), int(counts.sum())
+    # advance-only items (kind -1) write nothing
+    offs = np.concatenate([[0], np.cumsum(np.where(kind >= 0, counts, 0))[:-1]]) * 4
+    total = int(np.where(kind >= 0, counts, 0).sum())
+    return work_items(streams, kind, counts, offs), total
 
 
-def test_noalloc_matches_pool_submit_twice(gpu):
+def _compare(table, nparams, nstreams, kinds, use_pidx, seed0):
     from mtgp_gb300._lib import check, lib
     from mtgp_gb300.api import Pool
-    tbl = load_table("mtgp32_fast_11213")
-    nparams, nstreams = 3, 40
+    tbl = load_table(table)
+    mexp = tbl[0].mexp
+    size, stride = mexp // 32 + 1, _stride(mexp)
     plist = [tbl[i] for i in range(nparams)]
-    pidx = (np.arange(nstreams) % nparams).astype(np.int32)
-    seeds = np.arange(nstreams) + 501
-    pool = Pool.create(plist, seeds, pidx)
+    if use_pidx:
+        pidx = (np.arange(nstreams) % nparams).astype(np.int32)
+    else:
+        # without param_idx stream s uses set s (nparams == nstreams) or set 0
+        pidx = (np.arange(nstreams) if nparams == nstreams
+                else np.zeros(nstreams)).astype(np.int32)
+    pool = Pool.create(plist, np.arange(nstreams) + seed0, pidx)
     # the caller-owned windows: same start states as the pool's
-    win = np.zeros((nstreams, STRIDE), dtype=np.uint32)
-    win[:, :351] = pool.windows()
+    win = np.zeros((nstreams, stride), dtype=np.uint32)
+    win[:, :size] = pool.windows()
     dev_win = torch.from_numpy(win.view(np.int32)).cuda()
     parr = (MTGP32Params * nparams)(*plist)
-    rng = np.random.default_rng(11)
+    pptr = pidx.ctypes.data_as(ctypes.c_void_p) if use_pidx else None
+    rng = np.random.default_rng(seed0)
     for call in range(2):
-        items, total = _items(rng, nstreams, 150)
+        items, total = _items(rng, nstreams, 150, kinds)
         ref = torch.zeros(total + 8, dtype=torch.int32, device="cuda")
         got = torch.zeros(total + 8, dtype=torch.int32, device="cuda")
         pool.submit(items, ref)
         stream = torch.cuda.current_stream()
         check(lib().mtgp32_gpu_batch_noalloc(
-            parr, nparams, pidx.ctypes.data_as(ctypes.c_void_p),
-            ctypes.c_void_p(dev_win.data_ptr()), nstreams, items, len(items),
-            ctypes.c_void_p(got.data_ptr()), ctypes.c_void_p(stream.cuda_stream)))
+            parr, nparams, pptr, ctypes.c_void_p(dev_win.data_ptr()), nstreams, items,
+            len(items), ctypes.c_void_p(got.data_ptr()), ctypes.c_void_p(stream.cuda_stream)))
         torch.cuda.synchronize()
         assert torch.equal(got, ref), call
-        w = dev_win.cpu().numpy().view(np.uint32)[:, :351]
+        w = dev_win.cpu().numpy().view(np.uint32)[:, :size]
         assert np.array_equal(w, pool.windows()), call
+
+
+@pytest.mark.parametrize("kinds", [[0], [3], [0, 1, 2, 3, 4], [-1, 0, 2]],
+                         ids=["uint32", "open_close", "mixed", "mixed_advance"])
+def test_noalloc_matches_pool_submit_twice(gpu, kinds):
+    _compare("mtgp32_fast_11213", 3, 40, kinds, True, 501)
+
+
+def test_noalloc_other_exponent_and_default_index(gpu):
+    _compare("mtgp32_fast_23209", 4, 4, [0, 1], False, 901)
+    _compare("mtgp32_fast_11213", 2, 12, [0], False, 77)
 
 
 def test_noalloc_rejects_oversized_requests(gpu):
     from mtgp_gb300._lib import lib
     from mtgp_gb300.api import work_items
     tbl = load_table("mtgp32_fast_11213")
-    dev_win = torch.zeros(4 * STRIDE, dtype=torch.int32, device="cuda")
+    dev_win = torch.zeros(4 * 352, dtype=torch.int32, device="cuda")
     out = torch.zeros(16, dtype=torch.int32, device="cuda")
     many = work_items(np.zeros(2049), np.zeros(2049), np.ones(2049), np.zeros(2049))
     parr = (MTGP32Params * 1)(tbl[0])
@@ -78,3 +100,29 @@ def test_noalloc_rejects_oversized_requests(gpu):
     rc = lib().mtgp32_gpu_batch_noalloc(parr17, 17, None, ctypes.c_void_p(dev_win.data_ptr()), 4,
                                         one, 1, ctypes.c_void_p(out.data_ptr()), None)
     assert rc == -2 and b"16" in lib().mtgp_gpu_last_error()
+
+
+def test_noalloc_refuses_a_capturing_stream(gpu):
+    """The call synchronises its stream, which a stream under capture does
+    not allow: it returns MTGP_ERR_UNSUPPORTED and the caller's capture goes
+    on unharmed."""
+    from mtgp_gb300._lib import lib
+    from mtgp_gb300.api import work_items
+    tbl = load_table("mtgp32_fast_11213")
+    dev_win = torch.zeros(4 * 352, dtype=torch.int32, device="cuda")
+    out = torch.zeros(16, dtype=torch.int32, device="cuda")
+    x = torch.zeros(8, device="cuda")
+    parr = (MTGP32Params * 1)(tbl[0])
+    one = work_items([0], [0], [4], [0])
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        x += 1
+        rc = lib().mtgp32_gpu_batch_noalloc(
+            parr, 1, None, ctypes.c_void_p(dev_win.data_ptr()), 4, one, 1,
+            ctypes.c_void_p(out.data_ptr()),
+            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == -3 and b"captured" in lib().mtgp_gpu_last_error()
+    g.replay()
+    torch.cuda.synchronize()
+    assert float(x[0]) == 1.0
