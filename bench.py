@@ -46,9 +46,14 @@ N_SUB = 4096
 SEED = 1234
 L2_BYTES = 129 * 2 ** 20
 # DRAM bytes per step of the batched plan's kernels, from one ncu capture
-# each (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (kernel
-# description, split chunk, grid) of the plan captured; see profiles/
-CAPTURED_TRAFFIC = {}
+# of one launch each (dram__bytes_read.sum + dram__bytes_write.sum), keyed
+# by the captured plan's (core, split chunk, grid, windows jumped ahead)
+CAPTURED_TRAFFIC = {
+    (2, 393216, 760, 184): {
+        "bytes": 1677.8e6 + 6.85e6 + 0.52e6,
+        "source": "ncu capture of k_batch32xk<2> + k_jump_part5, one launch each, this plan "
+                  "(profiles/bench_default_plan_k_batch32xk2_k_jump_part5.md)"},
+}
 METRIC = "batched MTGP32-11213 output GB/s"
 WORKLOAD = ("batched: mtgp32_params_fast_11213[0], seed 1234, 4096 substreams j*3^162 "
             "(GPU jump), lognormal lengths median 2^16 sigma 1.0 seed 42 clip [2^10,2^22], uint32")
@@ -646,13 +651,14 @@ def run_bank(s, bits, table, nsets, seed0, n, kinds, hbm, reps=5):
     items = work_items(np.arange(nsets), np.full(nsets, kind), np.full(nsets, n),
                        np.arange(nsets) * n * bits // 8)
     t0 = time.perf_counter()
-    plan, _ = bank.autotune(items, bout, stream=s, reps=3)
+    plan, report = bank.autotune(items, bout, stream=s, reps=3)
     setup_s = time.perf_counter() - t0
     plan.launch(bout, s)
     ms = timed(lambda: plan.launch(bout, s))
     gbs = nbytes / (ms * 1e-3) / 1e9
     res["batched " + name] = {"value": round(gbs, 2), "unit": "GB/s", "ms": round(ms, 4),
                               "pct_hbm": round(100 * gbs / hbm, 2), "plan": plan.describe(),
+                              "autotune": [l for l in report.splitlines() if l.startswith("chosen")],
                               "setup_s": round(setup_s, 2)}
     res["_check"] = (bits, plist, start, n, kinds[0][0], first)
     return res
@@ -911,11 +917,13 @@ def main():
     state_bytes = 2 * nsub * 351 * 4
     achieved = (total_bytes + state_bytes) / (ms * 1e-3) / 1e9
     chosen = [l for l in tune_report.splitlines() if l.startswith("chosen:")]
-    kernel = chosen[0][len("chosen:"):].split(", chunk=")[0].strip() if chosen else None
+    kernel = (chosen[0][len("chosen:"):].split(", chunk=")[0].strip() if chosen else
+              "k_batch32xk<%d>%s" % (plan_cfg["core"], " after k_jump_part5 (%d windows jumped "
+                                     "ahead)" % plan_cfg["prejumps"] if plan_cfg["prejumps"] else ""))
     # DRAM bytes (read + write) per step of the plan's kernels, from an ncu
     # capture of the same plan on the same workload (profiles/); reported
     # only when the autotuner chose the captured plan
-    plan_key = (kernel, plan_cfg["split_chunk"], plan_cfg["grid"])
+    plan_key = (plan_cfg["core"], plan_cfg["split_chunk"], plan_cfg["grid"], plan_cfg["prejumps"])
     cap = CAPTURED_TRAFFIC.get(plan_key) if (nsub == N_SUB and args.uniform <= 0) else None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,

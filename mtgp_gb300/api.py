@@ -327,7 +327,7 @@ class Pool:
         """Fastest plan for these items on this output buffer (the pool's
         windows are left unchanged); returns (plan, report text)."""
         ph = ctypes.c_void_p()
-        buf = ctypes.create_string_buffer(8192)
+        buf = ctypes.create_string_buffer(1 << 17)
         check(getattr(lib(), self.pre + "autotune")(
             self.h, items, len(items), ctypes.c_void_p(out.data_ptr()), _stream(stream), reps,
             ctypes.byref(ph), buf, len(buf)))

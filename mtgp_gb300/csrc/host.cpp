@@ -146,7 +146,9 @@ struct Tuning {
     int poly_window = 0;
     // jump_overlap: 1 = tasks that start from windows jumped ahead of the
     // launch run in a second persistent launch on a side stream right after
-    // the jump parts, while the first launch runs every other task
+    // the jump parts, while the first launch runs every other task (off by
+    // default and not among the autotuner's candidates: those tasks are the
+    // longest, and starting them after the jumps lengthens the launch)
     int jump_overlap = 0;
 };
 std::mutex g_tune_mu;
@@ -1183,6 +1185,28 @@ struct GpuJob {
     const uint32_t *tab;  // the device tables of parameter set pidx
 };
 
+// Whether a pool's plans may start tasks from jumped windows: with the
+// in-kernel jump (MEXP 11213 and 23209), or else with jumps made ahead of
+// the launch by jump parts (every exponent, unless jump_parts = -1).
+template <class T>
+bool planJumps(const Pool<T> &P) {
+    return T::splits(P.sh.mexp) || P.tune.jump_parts >= 0;
+}
+
+// Shortest skip (and chunk) worth a jump.  A jump's correlation costs about
+// N * mexp word XORs (N window words; twice for 64-bit words), as much as
+// generating ~2^17 values at MEXP 11213; the exponents without the
+// in-kernel jump scale that by their cost, to a power of two (2^21 for
+// 44497, 2^24 for 64-bit 110503).
+template <class T>
+uint64_t jumpMinSkip(const Pool<T> &P) {
+    if (T::splits(P.sh.mexp)) return kJumpMinSkip;
+    const double rel = (double)P.sh.n * P.sh.mexp * (T::kBits / 32) / (351.0 * 11213.0);
+    uint64_t m = kJumpMinSkip;
+    while ((double)m < (double)kJumpMinSkip * rel) m <<= 1;
+    return m;
+}
+
 template <class T>
 int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_plan **out,
              int force_core = 0, int64_t force_chunk = 0) {
@@ -1192,8 +1216,11 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     PlanOptions o;
     o.nstreams = P.count;
     o.word_bytes = sizeof(W);
-    o.can_jump = T::splits(P.sh.mexp);
-    o.jump_min = kJumpMinSkip;
+    // without the in-kernel jump every jumped start is made ahead of the
+    // launch, from one polynomial (a run start and a chunk offset combined)
+    const bool kernel_jumps = T::splits(P.sh.mexp);
+    o.can_jump = planJumps(P);
+    o.jump_min = jumpMinSkip(P);
     o.max_gen_skip = kMaxGenSkip;
     o.chunk_tune = force_chunk ? force_chunk : P.tune.split_chunk;
     // Plans whose generated values mix kinds (a generated skip counts as
@@ -1292,7 +1319,9 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         // X^run then X^off: the run starts (a requested skip) and the chunk
         // offsets (shared by every long request) are each few, so few
         // distinct polynomials are needed
-        if (pt.run && pt.off) {
+        if (pt.run && pt.off && !kernel_jumps) {
+            rc = polyIndex(t.pidx, pt.run + pt.off, &t.j0, true);
+        } else if (pt.run && pt.off) {
             rc = polyIndex(t.pidx, pt.run, &t.j0, true);
             if (!rc) rc = polyIndex(t.pidx, pt.off, &t.j1, false);
         } else if (pt.run || pt.off) {
@@ -1862,11 +1891,15 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
     const int cores[3] = {4, 2, 1};
     const int ncores = T::kBits == 32 ? 3 : 1;
     for (int c = 0; c < ncores; c++) cands.push_back({cores[c], -1, 0, 0});
-    if (T::splits(P.sh.mexp))
-        for (int ov = 0; ov < (P.tune.jump_parts >= 0 ? 2 : 1); ov++)
-            for (int c = 0; c < ncores; c++)
-                for (int64_t ch = 1 << 17; ch <= (1 << 20); ch += 1 << 17)
-                    cands.push_back({cores[c], ch, 0, ov});
+    // chunk lengths: 1..8 times the shortest jumped piece (2^17 at MEXP
+    // 11213 and 23209)
+    const int64_t base = std::max<int64_t>(int64_t(1) << 17, (int64_t)jumpMinSkip(P));
+    // (jump_overlap is left out: on the bench workload and the 128-set bank
+    // it measured 1.3-2.7x slower, its jumped tasks being the longest ones)
+    if (planJumps(P))
+        for (int c = 0; c < ncores; c++)
+            for (int64_t ch = base; ch <= 8 * base; ch += base)
+                cands.push_back({cores[c], ch, 0, 0});
     const size_t sbytes = sizeof(W) * (size_t)P.stride * P.count;
     W *snap = nullptr;
     CK(devMalloc(&snap, sbytes), "devMalloc(autotune snapshot)");

@@ -150,7 +150,7 @@ int planCore(const mtgp_work_item_t *items, int nitems, const PlanOptions &o, Pl
             // a task longer than the average load of one CTA slot would set
             // the length of the whole launch
             const uint64_t per = grand / (uint64_t)std::max(o.resident, 1);
-            chunk = 1 << 17;
+            chunk = (int64_t)std::max<uint64_t>(uint64_t(1) << 17, o.jump_min);
             while ((uint64_t)chunk < per) chunk <<= 1;
         }
     }

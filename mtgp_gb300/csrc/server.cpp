@@ -26,7 +26,13 @@
 // has a worker thread that plans and launches its batch (the pools' plans
 // can be made on several threads at once), waits for it on the GPU and
 // retires it (latencies, arena space, stream states).  So the host work of
-// up to `slots` batches runs in parallel instead of on one thread.
+// up to `slots` batches runs in parallel instead of on one thread.  The
+// scheduler keeps admitting into the batch it is forming and hands it to a
+// free slot at once when no other batch is being planned (low load: a lone
+// request goes straight to the GPU), but while one is only once it holds a
+// quarter of a full batch: under load the backlog is mostly requests of
+// streams already in flight, and handing over whatever else is admissible at
+// every chance would split the work into many small launches.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -60,6 +66,7 @@ struct Slot {
     std::vector<Req> reqs;  // the batch (owned by the worker while busy)
     bool busy = false;      // holds a batch: handed over, launching or on the GPU
     bool assigned = false;  // handed over, not yet taken by the worker
+    bool planning = false;  // handed over and not yet launched
     std::thread th;         // the slot's worker
     std::condition_variable cv;
 };
@@ -75,6 +82,11 @@ struct mtgp_server {
     Arena arena;
     std::vector<std::unique_ptr<Slot>> slots;
     int max_batch = 4096;
+    int nplanning = 0;  // slots whose batch is handed over and not yet launched
+    // set when admission may take more: a submission, a retired batch or
+    // released space since the scheduler's last admission pass
+    bool dirty = false;
+    std::vector<Req> forming;  // admitted, not yet handed to a slot
     std::mutex mu;
     std::condition_variable cv, cv_done;
     std::deque<Req> pending;
@@ -147,23 +159,36 @@ int mtgp_server::launchBatch(Slot &sl, std::vector<Req> &reqs) {
 void mtgp_server::loop() {
     cudaSetDevice(device);
     std::unique_lock<std::mutex> lk(mu);
+    std::vector<Req> take;
     while (!stop.load()) {
         bool progressed = false;
-        // admit pending requests into the free slots, one batch each
-        for (auto &sp : slots) {
-            if (pending.empty()) break;
-            Slot &sl = *sp;
-            if (sl.busy) continue;
+        // admit pending requests into the batch being formed
+        if (dirty && !pending.empty() && forming.size() < (size_t)max_batch) {
+            dirty = false;
             const Clock::time_point ta = Clock::now();
-            std::vector<Req> take;
-            mtgp::admitBatch(pending, busy, arena, max_batch, kJumpSkip, &take);
+            mtgp::admitBatch(pending, busy, arena, max_batch - (int)forming.size(), kJumpSkip,
+                             &take, 4 * (size_t)max_batch);
+            if (!take.empty()) dirty = true;  // more may fit: look again
+            forming.insert(forming.end(), take.begin(), take.end());
             prof[0] += std::chrono::duration<double>(Clock::now() - ta).count();
-            if (take.empty()) break;  // nothing fits until a batch retires
-            sl.reqs.swap(take);
-            sl.busy = sl.assigned = true;
-            batches++;
-            sl.cv.notify_one();
-            progressed = true;
+            progressed = !take.empty();
+        }
+        // hand it to a free slot
+        const bool ready = !forming.empty() &&
+                           (nplanning == 0 || forming.size() >= (size_t)std::max(1, max_batch / 4));
+        if (ready) {
+            for (auto &sp : slots) {
+                Slot &sl = *sp;
+                if (sl.busy) continue;
+                sl.reqs.swap(forming);
+                forming.clear();
+                sl.busy = sl.assigned = sl.planning = true;
+                nplanning++;
+                batches++;
+                sl.cv.notify_one();
+                progressed = true;
+                break;
+            }
         }
         if (!progressed) {
             // woken by a submission, a retired batch or released space
@@ -182,20 +207,27 @@ void mtgp_server::work(Slot &sl) {
         if (!sl.assigned) break;  // stopping
         sl.assigned = false;
         lk.unlock();
-        // plan and launch, then wait for the batch: a short spin, then
-        // sleeps, so the retire follows the GPU closely without holding a
-        // core for long batches
+        // plan and launch, then wait for the batch: a short spin, so that
+        // the retire follows a short batch closely, then a blocking wait
+        // (the event is a blocking-sync one), so that long batches hold no
+        // core
         const Clock::time_point tl = Clock::now();
         const int rc = launch(sl, sl.reqs);
         const Clock::time_point tw = Clock::now();
+        lk.lock();
+        sl.planning = false;
+        nplanning--;
+        cv.notify_one();
+        lk.unlock();
         cudaError_t q = cudaSuccess;
         if (!rc) {
-            for (int spin = 0;; spin++) {
+            q = cudaEventQuery(sl.ev);
+            while (q == cudaErrorNotReady &&
+                   Clock::now() - tw < std::chrono::microseconds(100)) {
+                std::this_thread::yield();
                 q = cudaEventQuery(sl.ev);
-                if (q != cudaErrorNotReady) break;
-                if (spin < 2000) std::this_thread::yield();
-                else std::this_thread::sleep_for(std::chrono::microseconds(20));
             }
+            if (q == cudaErrorNotReady) q = cudaEventSynchronize(sl.ev);
         }
         const Clock::time_point now = Clock::now();
         lk.lock();
@@ -214,6 +246,7 @@ void mtgp_server::work(Slot &sl) {
         }
         sl.reqs.clear();
         sl.busy = false;
+        dirty = true;
         prof[2] += std::chrono::duration<double>(Clock::now() - now).count();
         cv.notify_one();
         cv_done.notify_all();
@@ -252,7 +285,8 @@ int mtgp_server_create(mtgp_server_t **out, mtgp32_gpu_pool_t *p32, mtgp64_gpu_p
             break;
         }
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl->cs, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming | cudaEventBlockingSync);
     }
     if (e != cudaSuccess) {
         mtgp_server_destroy(s);
@@ -296,6 +330,7 @@ int mtgp_server::enqueue(int pool, uint32_t stream, int kind, uint64_t skip, uin
     status.push_back(1);
     pending.push_back(r);
     *ticket = r.ticket;
+    dirty = true;
     cv.notify_one();
     return MTGP_OK;
 }
@@ -325,6 +360,7 @@ int mtgp_server_release(mtgp_server_t *s, uint64_t ticket) {
         return mtgp::recordError(MTGP_ERR_INVALID, "no result held for this ticket");
     s->arena.release(it->second.first, it->second.second);
     s->kept.erase(it);
+    s->dirty = true;
     s->cv.notify_one();
     return MTGP_OK;
 }

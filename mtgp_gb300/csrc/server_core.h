@@ -88,13 +88,18 @@ enum : char { kStreamFree = 0, kStreamBusy = 1, kStreamForming = 2, kStreamClose
 //     that a skip of at least `jump_skip` only opens a stream's part of a
 //     batch (its jump is then X^skip from the window, a polynomial shared by
 //     many requests, instead of X^(an arbitrary position));
-//   - at most `max_batch` requests.
+//   - at most `max_batch` requests, and at most `max_scan` pending requests
+//     looked at (a bound on the time the caller holds its lock when the
+//     backlog is long and mostly waits for streams on the GPU).
 // busy[pool][stream] holds the stream states; admitted streams end as busy.
 inline void admitBatch(std::deque<ServeReq> &pending, std::vector<char> *busy, Arena &arena,
-                       int max_batch, uint64_t jump_skip, std::vector<ServeReq> *take) {
+                       int max_batch, uint64_t jump_skip, std::vector<ServeReq> *take,
+                       size_t max_scan = ~size_t(0)) {
     take->clear();
     auto w = pending.begin(), it = pending.begin();
-    for (; it != pending.end() && (int)take->size() < max_batch; ++it) {
+    for (size_t scanned = 0;
+         it != pending.end() && (int)take->size() < max_batch && scanned < max_scan;
+         ++it, ++scanned) {
         char &b = busy[it->pool][it->stream];
         if (b == kStreamForming && it->skip >= jump_skip) b = kStreamClosed;
         if (b == kStreamBusy || b == kStreamClosed) {

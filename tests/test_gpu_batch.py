@@ -273,3 +273,51 @@ def test_batch_vector_cores_one_kind(gpu, orc, core, kind):
         if kind >= 0:
             assert np.array_equal(got[offs[k]:offs[k] + ref.size], ref), k
         assert np.array_equal(pool.windows()[k], o.window()), k
+
+
+@pytest.mark.parametrize("bits,table", [(32, "mtgp32_fast_44497"), (64, "mtgp64_fast_44497"),
+                                        (64, "mtgp64_fast_110503")])
+def test_batch_jumps_made_ahead_for_large_exponents(gpu, orc, bits, table):
+    """Exponents without the in-kernel jump still split long requests and
+    jump long skips in a batch: every jumped start (a run start and a chunk
+    offset combined into one polynomial made on the GPU) is made ahead of
+    the launch by jump parts.  Outputs and windows (word 0 under the mask)
+    against the oracle, which steps through the skips."""
+    from mtgp_gb300.api import Pool, work_items
+    tbl = load_table(table)
+    p = tbl[0]
+    nstreams = 4
+    plist = [tbl[i % len(tbl)] for i in range(2)]
+    pidx = np.arange(nstreams) % 2
+    seeds = np.arange(nstreams) + 91
+    pool = Pool.create(plist, seeds, pidx)
+    jmin = 1 << 21 if p.mexp == 44497 else 1 << 24      # the planner's shortest jump
+    pool.set_tuning("split_chunk", jmin)
+    esz = bits // 8
+    #        stream count             skip
+    spec = [(0, 2 * jmin + 777, 0),                       # split: offsets only
+            (1, 5000, jmin + 5),                          # one jumped skip
+            (2, jmin + 3000, jmin),                       # run start + offset, combined
+            (3, 4000, 0)]
+    offs, pos = [], 0
+    for _, c, _ in spec:
+        offs.append(pos)
+        pos += c * esz
+    items = work_items([x[0] for x in spec], np.zeros(len(spec)), [x[1] for x in spec], offs,
+                       [x[2] for x in spec])
+    plan = pool.plan(items)
+    desc = plan.describe()
+    assert desc["prejumps"] >= 3 and not desc["jumps"], desc
+    out = torch.zeros(pos // 4 + 16, dtype=torch.int32, device="cuda")
+    plan.launch(out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(np.uint8)
+    w = pool.windows()
+    for (s, c, sk), off in zip(spec, offs):
+        o = orc.gen(plist[pidx[s]], seed=int(seeds[s]))
+        o.skip(sk)
+        ref = np_bits(o.fill(0, c), bits).view(np.uint8)
+        assert np.array_equal(got[off:off + ref.size], ref), s
+        ow = o.window()
+        assert (int(ow[0]) ^ int(w[s][0])) & int(plist[pidx[s]].mask) == 0, s
+        assert np.array_equal(ow[1:], w[s][1:]), s
