@@ -26,13 +26,14 @@
 // has a worker thread that plans and launches its batch (the pools' plans
 // can be made on several threads at once), waits for it on the GPU and
 // retires it (latencies, arena space, stream states).  So the host work of
-// up to `slots` batches runs in parallel instead of on one thread.  The
-// scheduler keeps admitting into the batch it is forming and hands it to a
-// free slot at once when no other batch is being planned (low load: a lone
-// request goes straight to the GPU), but while one is only once it holds a
-// quarter of a full batch: under load the backlog is mostly requests of
-// streams already in flight, and handing over whatever else is admissible at
-// every chance would split the work into many small launches.
+// up to `slots` batches runs in parallel instead of on one thread.  A batch
+// is admitted (everything admissible, up to max_batch) when a slot is free
+// and no other batch is being planned (low load: a lone request goes
+// straight to the GPU; under load the next batch collects what arrives
+// while one is planned), or when a full batch is waiting: only then are
+// several batches planned at once.  Admitting at every chance instead splits
+// the work into many small launches and keeps the scheduler scanning a
+// backlog that is mostly requests of streams already on the GPU.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -86,7 +87,6 @@ struct mtgp_server {
     // set when admission may take more: a submission, a retired batch or
     // released space since the scheduler's last admission pass
     bool dirty = false;
-    std::vector<Req> forming;  // admitted, not yet handed to a slot
     std::mutex mu;
     std::condition_variable cv, cv_done;
     std::deque<Req> pending;
@@ -162,32 +162,27 @@ void mtgp_server::loop() {
     std::vector<Req> take;
     while (!stop.load()) {
         bool progressed = false;
-        // admit pending requests into the batch being formed
-        if (dirty && !pending.empty() && forming.size() < (size_t)max_batch) {
+        Slot *fs = nullptr;
+        for (auto &sp : slots)
+            if (!sp->busy) {
+                fs = sp.get();
+                break;
+            }
+        if (fs && dirty && !pending.empty() &&
+            (nplanning == 0 || pending.size() >= (size_t)max_batch)) {
             dirty = false;
             const Clock::time_point ta = Clock::now();
-            mtgp::admitBatch(pending, busy, arena, max_batch - (int)forming.size(), kJumpSkip,
-                             &take, 4 * (size_t)max_batch);
-            if (!take.empty()) dirty = true;  // more may fit: look again
-            forming.insert(forming.end(), take.begin(), take.end());
+            mtgp::admitBatch(pending, busy, arena, max_batch, kJumpSkip, &take,
+                             4 * (size_t)max_batch);
             prof[0] += std::chrono::duration<double>(Clock::now() - ta).count();
-            progressed = !take.empty();
-        }
-        // hand it to a free slot
-        const bool ready = !forming.empty() &&
-                           (nplanning == 0 || forming.size() >= (size_t)std::max(1, max_batch / 4));
-        if (ready) {
-            for (auto &sp : slots) {
-                Slot &sl = *sp;
-                if (sl.busy) continue;
-                sl.reqs.swap(forming);
-                forming.clear();
-                sl.busy = sl.assigned = sl.planning = true;
+            if (!take.empty()) {
+                fs->reqs.swap(take);
+                fs->busy = fs->assigned = fs->planning = true;
                 nplanning++;
                 batches++;
-                sl.cv.notify_one();
+                fs->cv.notify_one();
+                dirty = true;  // another free slot may take more
                 progressed = true;
-                break;
             }
         }
         if (!progressed) {
@@ -217,6 +212,7 @@ void mtgp_server::work(Slot &sl) {
         lk.lock();
         sl.planning = false;
         nplanning--;
+        dirty = true;  // the next batch may be admitted now
         cv.notify_one();
         lk.unlock();
         cudaError_t q = cudaSuccess;
