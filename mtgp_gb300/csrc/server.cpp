@@ -87,6 +87,7 @@ struct mtgp_server {
     // set when admission may take more: a submission, a retired batch or
     // released space since the scheduler's last admission pass
     bool dirty = false;
+    bool sched_waiting = false;  // the scheduler sleeps on cv (a submission wakes it)
     std::mutex mu;
     std::condition_variable cv, cv_done;
     std::deque<Req> pending;
@@ -106,6 +107,8 @@ struct mtgp_server {
 
     int enqueue(int pool, uint32_t stream, int kind, uint64_t skip, uint64_t count, void *dst,
                 bool keep, uint64_t *ticket);
+    int enqueueLocked(int pool, uint32_t stream, int kind, uint64_t skip, uint64_t count,
+                      void *dst, bool keep, uint64_t *ticket);
 
     void loop();
     void work(Slot &sl);
@@ -188,7 +191,9 @@ void mtgp_server::loop() {
         if (!progressed) {
             // woken by a submission, a retired batch or released space
             const Clock::time_point ti = Clock::now();
+            sched_waiting = true;
             cv.wait_for(lk, std::chrono::milliseconds(1));
+            sched_waiting = false;
             prof[3] += std::chrono::duration<double>(Clock::now() - ti).count();
         }
     }
@@ -300,6 +305,15 @@ int mtgp_server_create(mtgp_server_t **out, mtgp32_gpu_pool_t *p32, mtgp64_gpu_p
 
 int mtgp_server::enqueue(int pool, uint32_t stream, int kind, uint64_t skip, uint64_t count,
                          void *dst, bool keep, uint64_t *ticket) {
+    std::lock_guard<std::mutex> lk(mu);
+    return enqueueLocked(pool, stream, kind, skip, count, dst, keep, ticket);
+}
+
+// enqueue with mu held (replay submits all requests that are due under one
+// lock); the scheduler is woken only when it sleeps, so a burst of
+// submissions costs no wake-up each.
+int mtgp_server::enqueueLocked(int pool, uint32_t stream, int kind, uint64_t skip,
+                               uint64_t count, void *dst, bool keep, uint64_t *ticket) {
     if (!ticket) return mtgp::recordError(MTGP_ERR_INVALID, "null ticket");
     if (pool < 0 || pool > 1 || stream >= (uint32_t)nstreams[pool])
         return mtgp::recordError(MTGP_ERR_INVALID, "no such pool or stream");
@@ -310,7 +324,6 @@ int mtgp_server::enqueue(int pool, uint32_t stream, int kind, uint64_t skip, uin
     const uint64_t bytes = kind < 0 ? 0 : count * esz;
     if (Arena::round(bytes) > arena.size())
         return mtgp::recordError(MTGP_ERR_BUDGET, "request larger than the device budget");
-    std::lock_guard<std::mutex> lk(mu);
     Req r{};
     r.ticket = ++submitted;
     r.pool = pool;
@@ -327,7 +340,7 @@ int mtgp_server::enqueue(int pool, uint32_t stream, int kind, uint64_t skip, uin
     pending.push_back(r);
     *ticket = r.ticket;
     dirty = true;
-    cv.notify_one();
+    if (sched_waiting) cv.notify_one();
     return MTGP_OK;
 }
 
@@ -429,17 +442,27 @@ int mtgp_server_replay(mtgp_server_t *s, const mtgp_request_t *reqs, const doubl
     if (!s || n < 0 || (n > 0 && (!reqs || !arrival_s)))
         return mtgp::recordError(MTGP_ERR_INVALID, "bad trace");
     const Clock::time_point start = Clock::now();
-    for (int k = 0; k < n; k++) {
-        const Clock::time_point at =
-            start + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[k]));
+    auto due = [&](int k) {
+        return start + std::chrono::duration_cast<Clock::duration>(
+                           std::chrono::duration<double>(arrival_s[k]));
+    };
+    for (int k = 0; k < n;) {
+        const Clock::time_point at = due(k);
         while (Clock::now() < at) {
             const auto left = at - Clock::now();
             if (left > std::chrono::microseconds(200)) std::this_thread::sleep_for(left / 2);
         }
-        uint64_t t = 0;
-        const mtgp_request_t &r = reqs[k];
-        int rc = s->enqueue(r.pool, r.stream, r.kind, r.skip, r.count, r.dst, false, &t);
-        if (rc) return rc;
+        // every request already due (at most 1024), under one lock
+        std::lock_guard<std::mutex> lk(s->mu);
+        const Clock::time_point now = Clock::now();
+        const int k0 = k;
+        do {
+            uint64_t t = 0;
+            const mtgp_request_t &r = reqs[k];
+            int rc = s->enqueueLocked(r.pool, r.stream, r.kind, r.skip, r.count, r.dst, false, &t);
+            if (rc) return rc;
+            k++;
+        } while (k < n && k - k0 < 1024 && due(k) <= now);
     }
     int rc = mtgp_server_drain(s, 600.0);
     if (wall_s) *wall_s = std::chrono::duration<double>(Clock::now() - start).count();
