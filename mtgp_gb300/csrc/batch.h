@@ -73,7 +73,7 @@ cudaError_t launchUnstage64(int mexp, uint64_t *states, const void *stage,
 // Number of CTAs of the batched kernel resident at once on the device
 // (32-bit: for the given generation core, 1, 2 or 4).
 int batchResident32(int mexp, bool split, int core);
-int batchResident64(int mexp, bool split);
+int batchResident64(int mexp, bool split, int core = 1);
 // Whether split requests are supported for this exponent.
 bool batchSplits32(int mexp);
 bool batchSplits64(int mexp);

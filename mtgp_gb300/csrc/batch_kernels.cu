@@ -27,6 +27,7 @@
 #include "batch.h"
 #include "jump_device.cuh"
 #include "mtgp_device4.cuh"
+#include "mtgp_device64x2.cuh"
 
 namespace mtgp {
 
@@ -330,6 +331,51 @@ k_batch64(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
     }
 }
 
+// 64-bit two-words-per-thread core (W/2 threads per CTA): items of one
+// output kind (MODE >= -1), tasks that start from the stream's window or a
+// window jumped ahead of the launch (no jump code: plans on this core make
+// every jumped start ahead of the launch).
+template <int N, int W, int B, int MODE>
+__global__ void __launch_bounds__(W / 2)
+k_batch64x2(const DevParams64 *__restrict__ params, uint64_t *__restrict__ states,
+            const BatchTask *__restrict__ tasks, int ntasks,
+            const BatchItem *__restrict__ items, char *__restrict__ out,
+            unsigned *__restrict__ counter, uint64_t *__restrict__ stage,
+            const uint32_t *__restrict__ polys, int nwords, uint64_t *__restrict__ prewin) {
+    using C = Core64x2<N, W, B, MODE>;
+    constexpr int T = W / 2;
+    __shared__ __align__(16) uint64_t buf[C::G::BUF];
+    __shared__ int s_task;
+    (void)polys;
+    (void)nwords;
+    for (;;) {
+        if (threadIdx.x == 0) s_task = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int t = s_task;
+        __syncthreads();
+        if (t >= ntasks) break;
+        const BatchTask TK = tasks[t];
+        Lane64 L;
+        L.load(params[TK.pidx], threadIdx.x & 31);
+        const uint64_t *src = startWindow(TK, states, prewin, stateStride(N));
+        uint64_t *clr = preSlot(TK, prewin, stateStride(N));
+        for (int k = threadIdx.x; k < N; k += T) {
+            buf[C::at(k)] = src[k];
+            if (clr) clr[k] = 0;
+        }
+        __syncthreads();
+        for (int i = 0; i < TK.nitems; i++) {
+            const BatchItem I = items[TK.first + i];
+            C::run(buf, L, L.otab_lo(MODE < 0 ? 0 : MODE), L.otab_hi(MODE < 0 ? 0 : MODE),
+                   I.count, (typename C::OT *)(out + I.out_off));
+        }
+        uint64_t *dst = endWindow(TK, states, stage, stateStride(N));
+        if (dst)
+            for (int k = threadIdx.x; k < N; k += T) dst[k] = buf[C::at(k)];
+        __syncthreads();
+    }
+}
+
 // Staged windows back to their streams: block k copies slot k.
 template <typename W, int N>
 __global__ void k_unstage(W *__restrict__ states, const W *__restrict__ stage,
@@ -460,11 +506,28 @@ static cudaError_t run32x(const BatchLaunch &b, const DevParams32 *p, uint32_t *
     return cudaGetLastError();
 }
 
+template <int N, int W, int B>
+static cudaError_t mode64x2(const BatchLaunch &b, const DevParams64 *p, uint64_t *st,
+                            cudaStream_t s) {
+    constexpr int T = W / 2;
+    switch (b.mode) {
+    case -1: return go<uint64_t>(k_batch64x2<N, W, B, -1>, T, b, p, st, s);
+    case 0: return go<uint64_t>(k_batch64x2<N, W, B, 0>, T, b, p, st, s);
+    case 1: return go<uint64_t>(k_batch64x2<N, W, B, 1>, T, b, p, st, s);
+    case 2: return go<uint64_t>(k_batch64x2<N, W, B, 2>, T, b, p, st, s);
+    case 3: return go<uint64_t>(k_batch64x2<N, W, B, 3>, T, b, p, st, s);
+    case 4: return go<uint64_t>(k_batch64x2<N, W, B, 4>, T, b, p, st, s);
+    default: return cudaErrorInvalidValue;  // mixed kinds run on the one-word core
+    }
+}
+
 template <int N, int TN, int B>
 static cudaError_t run64x(const BatchLaunch &b, const DevParams64 *p, uint64_t *st,
                           cudaStream_t s) {
     cudaError_t e;
-    if (b.split) {
+    if (b.core != 1 && !b.split && b.mode != -2) {
+        e = mode64x2<N, TN, B>(b, p, st, s);
+    } else if (b.split) {
         if constexpr (kSplit64<N>) e = mode64<N, TN, B, true>(b, p, st, s);
         else return cudaErrorInvalidValue;
     } else {
@@ -557,11 +620,12 @@ int batchResident32(int mexp, bool split, int core) {
     return 0;
 }
 
-int batchResident64(int mexp, bool split) {
+int batchResident64(int mexp, bool split, int core) {
     int g = 0;
 #define X(M, N, T, B) \
     if (mexp == M) {                                                  \
-        if (split) resident(k_batch64<N, T, B, 0, true>, T, &g);      \
+        if (core != 1 && !split) resident(k_batch64x2<N, T, B, 0>, T / 2, &g); \
+        else if (split) resident(k_batch64<N, T, B, 0, true>, T, &g);  \
         else resident(k_batch64<N, T, B, 0, false>, T, &g);           \
     }
     MTGP_SHAPES64(X)

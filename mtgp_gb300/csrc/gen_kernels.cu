@@ -6,7 +6,7 @@
 // writes the advanced window back.  Unlike the sample it accepts any n (not
 // a multiple of 3*TN), any parameter set per CTA, all five output kinds and
 // every Mersenne exponent of the reference's tables.
-#include "mtgp_device4.cuh"
+#include "mtgp_device64x2.cuh"
 
 namespace mtgp {
 
@@ -104,6 +104,44 @@ k_gen64(const DevParams64 *__restrict__ params, const int *__restrict__ pidx,
     for (int k = threadIdx.x; k < N; k += TN) st[k] = ring[k];
 }
 
+// Same as k_gen64 with the two-words-per-thread core (W/2 threads per CTA).
+template <int N, int W, int B, int KIND>
+__global__ void __launch_bounds__(W / 2)
+k_gen64x2(const DevParams64 *__restrict__ params, const int *__restrict__ pidx,
+          uint64_t *__restrict__ states, void *__restrict__ out, uint64_t n,
+          uint64_t out_stride) {
+    using C = Core64x2<N, W, B, KIND>;
+    __shared__ __align__(16) uint64_t buf[C::G::BUF];
+    const int g = blockIdx.x;
+    const DevParams64 &P = params[pidx ? pidx[g] : g];
+    Lane64 L;
+    L.load(P, threadIdx.x & 31);
+    uint64_t *st = states + (size_t)g * stateStride(N);
+    for (int k = threadIdx.x; k < N; k += W / 2) buf[C::at(k)] = st[k];
+    __syncthreads();
+    using T = typename C::OT;
+    T *o = KIND < 0 ? nullptr : reinterpret_cast<T *>(out) + (size_t)g * out_stride;
+    C::run(buf, L, L.otab_lo(KIND < 0 ? 0 : KIND), L.otab_hi(KIND < 0 ? 0 : KIND), n, o);
+    for (int k = threadIdx.x; k < N; k += W / 2) st[k] = buf[C::at(k)];
+}
+
+template <int N, int W, int B>
+static cudaError_t gen64x2(int kind, const DevParams64 *params, const int *pidx,
+                           uint64_t *states, int ngen, void *out, uint64_t n, uint64_t os,
+                           cudaStream_t s) {
+    dim3 grid(ngen), b(W / 2);
+    switch (kind) {
+    case -1: k_gen64x2<N, W, B, -1><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 0: k_gen64x2<N, W, B, 0><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 1: k_gen64x2<N, W, B, 1><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 2: k_gen64x2<N, W, B, 2><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 3: k_gen64x2<N, W, B, 3><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    case 4: k_gen64x2<N, W, B, 4><<<grid, b, 0, s>>>(params, pidx, states, out, n, os); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 template <int N, int TN, int B>
 static cudaError_t gen32_kind(int kind, const DevParams32 *params, const int *pidx,
                               uint32_t *states, int ngen, void *out, uint64_t n,
@@ -126,8 +164,9 @@ static cudaError_t gen32_kind(int kind, const DevParams32 *params, const int *pi
 template <int N, int TN, int B>
 static cudaError_t gen64_kind(int kind, const DevParams64 *params, const int *pidx,
                               uint64_t *states, int ngen, void *out, uint64_t n,
-                              uint64_t os, cudaStream_t s) {
+                              uint64_t os, cudaStream_t s, int core) {
     dim3 grid(ngen), block(TN);
+    if (core != 1) return gen64x2<N, TN, B>(kind, params, pidx, states, ngen, out, n, os, s);
     switch (kind) {
     case -1: k_gen64<N, TN, B, -1><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
     case 0: k_gen64<N, TN, B, 0><<<grid, block, 0, s>>>(params, pidx, states, out, n, os); break;
@@ -153,10 +192,10 @@ cudaError_t launchGen32(int mexp, int kind, const DevParams32 *params, const int
 
 cudaError_t launchGen64(int mexp, int kind, const DevParams64 *params, const int *pidx,
                         uint64_t *states, int ngen, void *out, uint64_t n,
-                        uint64_t os, cudaStream_t s) {
+                        uint64_t os, cudaStream_t s, int core) {
     if (ngen <= 0 || n == 0) return cudaSuccess;
 #define X(M, N, T, B) \
-    if (mexp == M) return gen64_kind<N, T, B>(kind, params, pidx, states, ngen, out, n, os, s);
+    if (mexp == M) return gen64_kind<N, T, B>(kind, params, pidx, states, ngen, out, n, os, s, core);
     MTGP_SHAPES64(X)
 #undef X
     return cudaErrorInvalidValue;

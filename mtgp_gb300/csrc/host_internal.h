@@ -192,8 +192,8 @@ struct T64 {
     static constexpr int kBits = 64;
     static bool shape(int mexp, Shape *s) { return shape64(mexp, s); }
     static cudaError_t gen(int mexp, int kind, const DP *p, const int *pi, W *st, int ng,
-                           void *out, uint64_t n, uint64_t os, cudaStream_t s, int) {
-        return launchGen64(mexp, kind, p, pi, st, ng, out, n, os, s);
+                           void *out, uint64_t n, uint64_t os, cudaStream_t s, int core) {
+        return launchGen64(mexp, kind, p, pi, st, ng, out, n, os, s, core);
     }
     static cudaError_t jump(int mexp, const DP *p, W *st, const JumpDesc *d, int nd, int nw,
                             cudaStream_t s) {
@@ -214,7 +214,9 @@ struct T64 {
     static cudaError_t windows(const W *gen, W *win, int n, int stride, int nwin, cudaStream_t s) {
         return launchChunkWindows64(gen, win, n, stride, nwin, s);
     }
-    static int resident(int mexp, bool split, int) { return batchResident64(mexp, split); }
+    static int resident(int mexp, bool split, int core) {
+        return batchResident64(mexp, split, core);
+    }
     static bool splits(int mexp) { return batchSplits64(mexp); }
     static cudaError_t seed(const DP *p, const int *pi, const W *seeds, W *st, int n, int size,
                             int stride) {

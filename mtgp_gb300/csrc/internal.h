@@ -167,10 +167,12 @@ cudaError_t launchGen32(int mexp, int kind, const DevParams32 *params,
                         const int *pidx, uint32_t *states, int ngen,
                         void *out, uint64_t n, uint64_t outStride,
                         cudaStream_t s, int core = 2);
+// core (64-bit): 2 = two adjacent words per thread (the default, also for
+// core 4), 1 = one word per thread.
 cudaError_t launchGen64(int mexp, int kind, const DevParams64 *params,
                         const int *pidx, uint64_t *states, int ngen,
                         void *out, uint64_t n, uint64_t outStride,
-                        cudaStream_t s);
+                        cudaStream_t s, int core = 2);
 
 // ---- jump (jump_kernels.cu) ---------------------------------------------
 // One descriptor per jump.  The kernel reads the window at `src`, applies

@@ -23,9 +23,6 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     PlanOptions o;
     o.nstreams = P.count;
     o.word_bytes = sizeof(W);
-    // without the in-kernel jump every jumped start is made ahead of the
-    // launch, from one polynomial (a run start and a chunk offset combined)
-    const bool kernel_jumps = T::splits(P.sh.mexp);
     o.can_jump = planJumps(P);
     o.jump_min = jumpMinSkip(P);
     o.max_gen_skip = kMaxGenSkip;
@@ -47,7 +44,16 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (it.count) addKind(it.kind);
         }
     }
-    const int core = force_core ? force_core : (T::kBits == 32 && kinds == -2) ? 1 : P.tune.core;
+    int core = force_core ? force_core : kinds == -2 ? 1 : P.tune.core;
+    // 64-bit cores: two words per thread (knob 2 or 4) or one; the two-word
+    // kernel has no jump code, so plans with in-kernel jumps (jump_parts =
+    // -1) take the one-word core
+    if (T::kBits == 64) core = (core == 1 || P.tune.jump_parts < 0) ? 1 : 2;
+    // where the kernel has no jump code (the exponents without the in-kernel
+    // jump, the 64-bit two-word core) every jumped start is made ahead of
+    // the launch, from one polynomial (a run start and a chunk offset
+    // combined)
+    const bool kernel_jumps = T::splits(P.sh.mexp) && (T::kBits == 32 || core == 1);
     // with jumps made ahead of the launch, the kernel without the jump code
     o.resident = o.can_jump ? T::resident(P.sh.mexp, P.tune.jump_parts < 0, core) : 1;
     // scratch reused by every plan made on this thread
@@ -499,7 +505,7 @@ int mtgp_gpu_plan_info(const mtgp_gpu_plan_t *pl, int64_t *tasks, int64_t *chunk
 
 int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *pl, int64_t *values, int n) {
     if (!pl || (n > 0 && !values)) return setErr(MTGP_ERR_INVALID, "null plan or values");
-    const int64_t v[8] = {pl->ntasks, pl->chunk, pl->bits == 64 ? 1 : pl->core, pl->grid,
+    const int64_t v[8] = {pl->ntasks, pl->chunk, pl->core, pl->grid,
                           pl->ntasks ? 1 + (pl->nstage > 0) + (pl->nparts > 0) +
                                            (pl->overlap && pl->nmain > 0)
                                      : 0,

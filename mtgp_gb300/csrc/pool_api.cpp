@@ -27,8 +27,10 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
         int overlap;
     };
     std::vector<Cand> cands;
-    const int cores[3] = {4, 2, 1};
-    const int ncores = T::kBits == 32 ? 3 : 1;
+    // 32-bit: four, two or one words per thread; 64-bit: two or one
+    const int cores32[3] = {4, 2, 1}, cores64[2] = {2, 1};
+    const int *cores = T::kBits == 32 ? cores32 : cores64;
+    const int ncores = T::kBits == 32 ? 3 : 2;
     for (int c = 0; c < ncores; c++) cands.push_back({cores[c], -1, 0, 0});
     // chunk lengths: 1..8 times the shortest jumped piece (2^17 at MEXP
     // 11213 and 23209)
@@ -103,7 +105,7 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
             }
             char line[160];
             std::snprintf(line, sizeof line, "core=%d chunk=%lld%s grid=%s tasks=%d: %.4f ms\n",
-                          T::kBits == 64 ? 1 : pl->core, (long long)pl->chunk,
+                          pl->core, (long long)pl->chunk,
                           pl->overlap ? " overlap" : "",
                           g == 0 ? "all" : g == 1 ? "7/8" : g == 2 ? "3/4" : g == 3 ? "5/8" : "1/2",
                           pl->ntasks, ms);
@@ -132,8 +134,9 @@ int autotune(Pool<T> &P, const mtgp_work_item_t *items, int nitems, void *out, v
     if (*best) {
         const mtgp_gpu_plan *b = *best;
         const char *kern =
-            T::kBits == 64 ? (b->split ? "k_batch64 (one word per thread, in-CTA jumps)"
-                                       : "k_batch64 (one word per thread)")
+            T::kBits == 64 ? (b->core == 2 ? "k_batch64x2 (two words per thread)"
+                              : b->split ? "k_batch64 (one word per thread, in-CTA jumps)"
+                                         : "k_batch64 (one word per thread)")
             : b->core == 4 ? (b->split ? "k_batch32xk<4> (four words per thread, in-CTA jumps)"
                                        : "k_batch32xk<4> (four words per thread)")
             : b->core == 2 ? (b->split ? "k_batch32xk<2> (two words per thread, in-CTA jumps)"

@@ -30,8 +30,8 @@
 // is admitted (everything admissible, up to max_batch) when a slot is free
 // and no other batch is being planned (low load: a lone request goes
 // straight to the GPU; under load the next batch collects what arrives
-// while one is planned), or when a full batch is waiting: only then are
-// several batches planned at once.  Admitting at every chance instead splits
+// while one is planned), or when a quarter of a full batch is waiting:
+// only then are several batches planned at once.  Admitting at every chance instead splits
 // the work into many small launches and keeps the scheduler scanning a
 // backlog that is mostly requests of streams already on the GPU.
 #include <algorithm>
@@ -172,7 +172,7 @@ void mtgp_server::loop() {
                 break;
             }
         if (fs && dirty && !pending.empty() &&
-            (nplanning == 0 || pending.size() >= (size_t)max_batch)) {
+            (nplanning == 0 || pending.size() >= (size_t)std::max(1, max_batch / 4))) {
             dirty = false;
             const Clock::time_point ta = Clock::now();
             mtgp::admitBatch(pending, busy, arena, max_batch, kJumpSkip, &take,

@@ -138,8 +138,8 @@ def test_batch_split_long_requests(gpu, orc, bits, table, mixed, core, parts):
     jump) or inside it (parts -1), on each 32-bit generation core: bit-exact
     outputs and final states, across two launches of the same plan."""
     from mtgp_gb300.api import Pool, work_items
-    if bits == 64 and core != 4:
-        pytest.skip("one 64-bit core")
+    if bits == 64 and core == 4:
+        pytest.skip("64-bit cores: two and one words per thread")
     tbl = load_table(table)
     rng = np.random.default_rng(bits + mixed + tbl[0].mexp)
     nstreams = 24
@@ -234,20 +234,22 @@ def test_autotune_leaves_pool_and_picks_exact_plan(gpu, orc):
         assert np.array_equal(got[a:a + int(counts[j])], o.fill(0, int(counts[j]))), j
 
 
-@pytest.mark.parametrize("core", [4, 2])
+@pytest.mark.parametrize("bits,core", [(32, 4), (32, 2), (64, 2), (64, 1)])
 @pytest.mark.parametrize("kind", [0, 1, 2, 3, 4, -1])
-def test_batch_vector_cores_one_kind(gpu, orc, core, kind):
-    """The two- and four-word cores on plans of one output kind (no split):
-    uneven counts, outputs at every 4-byte alignment (the cores' alignment
+def test_batch_vector_cores_one_kind(gpu, orc, bits, core, kind):
+    """The vector cores (32-bit: two and four words per thread; 64-bit: two,
+    and the one-word core beside it) on plans of one output kind (no split):
+    uneven counts, outputs at every word alignment (the cores' alignment
     pre-step), a skip item, against the oracle."""
     from mtgp_gb300.api import Pool, work_items
-    tbl = load_table("mtgp32_fast_11213")
+    tbl = load_table("mtgp32_fast_11213" if bits == 32 else "mtgp64dc_fast_11213")
+    esz = bits // 8
     nstreams = 20
     plist = [tbl[i] for i in range(4)]
     pidx = np.arange(nstreams) % 4
     seeds = np.arange(nstreams) + 31
     pool = Pool.create(plist, seeds, pidx)
-    rng = np.random.default_rng(core * 10 + kind)
+    rng = np.random.default_rng(core * 10 + kind + bits)
     counts = rng.integers(1, 9000, nstreams)
     counts[:5] = [1, 2, 3, 255, 4097]
     # consecutive outputs; each item starts 0..3 words after the previous one
@@ -256,20 +258,20 @@ def test_batch_vector_cores_one_kind(gpu, orc, core, kind):
     pos = 0
     for k in range(nstreams):
         pos += int(gaps[k])
-        offs[k] = pos * 4
+        offs[k] = pos * esz
         if kind >= 0:
             pos += int(counts[k])
     pool.set_tuning("core", core)
     pool.set_tuning("split_chunk", -1)
     plan = pool.plan(work_items(np.arange(nstreams), np.full(nstreams, kind), counts, offs))
     assert plan.describe()["core"] == core
-    out = torch.zeros(pos + 8, dtype=torch.int32, device="cuda")
+    out = torch.zeros(pos * esz // 4 + 8, dtype=torch.int32, device="cuda")
     plan.launch(out)
     torch.cuda.synchronize()
     got = out.cpu().numpy().view(np.uint8)
     for k in range(nstreams):
         o = orc.gen(plist[pidx[k]], seed=int(seeds[k]))
-        ref = np_bits(o.fill(max(kind, 0), int(counts[k])), 32).view(np.uint8)
+        ref = np_bits(o.fill(max(kind, 0), int(counts[k])), bits).view(np.uint8)
         if kind >= 0:
             assert np.array_equal(got[offs[k]:offs[k] + ref.size], ref), k
         assert np.array_equal(pool.windows()[k], o.window()), k
