@@ -456,10 +456,12 @@ class Server:
         return c.value, b.value, k.value
 
     def profile(self):
-        """Scheduler seconds: admitting, planning + launching, retiring, idle."""
-        out = np.zeros(4, dtype=np.float64)
-        check(lib().mtgp_server_profile(self.h, out.ctypes.data_as(ctypes.c_void_p), 4))
-        return {"admit_s": out[0], "launch_s": out[1], "retire_s": out[2], "idle_s": out[3]}
+        """Host seconds: admitting, planning + launching (of which planning),
+        retiring (summed over the slot workers), scheduler idle."""
+        out = np.zeros(5, dtype=np.float64)
+        check(lib().mtgp_server_profile(self.h, out.ctypes.data_as(ctypes.c_void_p), 5))
+        return {"admit_s": out[0], "launch_s": out[1], "plan_s": out[4], "retire_s": out[2],
+                "idle_s": out[3]}
 
     def replay(self, requests, arrivals):
         """Submit `requests` (a REQUEST_DTYPE array) at `arrivals` (seconds

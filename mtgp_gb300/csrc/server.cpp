@@ -102,7 +102,8 @@ struct mtgp_server {
     std::deque<int> status;
     std::map<uint64_t, std::pair<uint64_t, uint64_t>> kept;  // ticket -> (offset, bytes)
     // scheduler time (s): admission, planning + launch, retiring, idle waits
-    double prof[4] = {0, 0, 0, 0};
+    // [4]: the planning part of [1] (pool_plan / pool_replan)
+    double prof[5] = {0, 0, 0, 0, 0};
     Clock::time_point t0;
 
     int enqueue(int pool, uint32_t stream, int kind, uint64_t skip, uint64_t count, void *dst,
@@ -112,19 +113,19 @@ struct mtgp_server {
 
     void loop();
     void work(Slot &sl);
-    int launch(Slot &sl, std::vector<Req> &reqs);
-    int launchBatch(Slot &sl, std::vector<Req> &reqs);
+    int launch(Slot &sl, std::vector<Req> &reqs, double *plan_s);
+    int launchBatch(Slot &sl, std::vector<Req> &reqs, double *plan_s);
 };
 
-int mtgp_server::launch(Slot &sl, std::vector<Req> &reqs) {
-    const int rc = launchBatch(sl, reqs);
+int mtgp_server::launch(Slot &sl, std::vector<Req> &reqs, double *plan_s) {
+    const int rc = launchBatch(sl, reqs, plan_s);
     // work already queued for this batch must end before its arena space is
     // handed to another batch
     if (rc) cudaStreamSynchronize(sl.cs);
     return rc;
 }
 
-int mtgp_server::launchBatch(Slot &sl, std::vector<Req> &reqs) {
+int mtgp_server::launchBatch(Slot &sl, std::vector<Req> &reqs, double *plan_s) {
     std::vector<mtgp_work_item_t> items[2];
     for (const Req &r : reqs) {
         mtgp_work_item_t it{};
@@ -139,6 +140,7 @@ int mtgp_server::launchBatch(Slot &sl, std::vector<Req> &reqs) {
         if (items[p].empty()) continue;
         int rc;
         const int n = (int)items[p].size();
+        const Clock::time_point tp = Clock::now();
         if (!sl.plan[p]) {
             rc = p == 0 ? mtgp32_gpu_pool_plan(p32, items[p].data(), n, &sl.plan[p])
                         : mtgp64_gpu_pool_plan(p64, items[p].data(), n, &sl.plan[p]);
@@ -146,6 +148,7 @@ int mtgp_server::launchBatch(Slot &sl, std::vector<Req> &reqs) {
             rc = p == 0 ? mtgp32_gpu_pool_replan(p32, items[p].data(), n, sl.plan[p])
                         : mtgp64_gpu_pool_replan(p64, items[p].data(), n, sl.plan[p]);
         }
+        *plan_s += std::chrono::duration<double>(Clock::now() - tp).count();
         if (!rc) rc = mtgp_gpu_plan_launch(sl.plan[p], d_arena, sl.cs);
         if (rc) return rc;
     }
@@ -212,7 +215,8 @@ void mtgp_server::work(Slot &sl) {
         // (the event is a blocking-sync one), so that long batches hold no
         // core
         const Clock::time_point tl = Clock::now();
-        const int rc = launch(sl, sl.reqs);
+        double plan_s = 0;
+        const int rc = launch(sl, sl.reqs, &plan_s);
         const Clock::time_point tw = Clock::now();
         lk.lock();
         sl.planning = false;
@@ -233,6 +237,7 @@ void mtgp_server::work(Slot &sl) {
         const Clock::time_point now = Clock::now();
         lk.lock();
         prof[1] += std::chrono::duration<double>(tw - tl).count();
+        prof[4] += plan_s;
         const int st = rc ? rc : q == cudaSuccess ? MTGP_OK : MTGP_ERR_CUDA;
         for (const Req &r : sl.reqs) {
             latency[r.ticket - 1] = rc ? 0 : std::chrono::duration<double>(now - r.t_submit).count();
@@ -433,7 +438,7 @@ int mtgp_server_stats(mtgp_server_t *s, uint64_t *completed, uint64_t *bytes, ui
 int mtgp_server_profile(mtgp_server_t *s, double *seconds, int n) {
     if (!s || (n > 0 && !seconds)) return mtgp::recordError(MTGP_ERR_INVALID, "bad profile");
     std::lock_guard<std::mutex> lk(s->mu);
-    for (int k = 0; k < n && k < 4; k++) seconds[k] = s->prof[k];
+    for (int k = 0; k < n && k < 5; k++) seconds[k] = s->prof[k];
     return MTGP_OK;
 }
 
