@@ -78,9 +78,11 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     constexpr int32_t kGpuSlot = 1 << 29;
     std::vector<GpuJob> gjobs;
     auto polyIndex = [&](int pidx, uint64_t steps, int32_t *idx, bool gpu_ok) -> int {
-        std::lock_guard<std::recursive_mutex> lk(P.cache_mu);
+        // the plan's own map first (most tasks of a plan share their
+        // polynomials), the pool's caches under its lock only on a miss
         auto hit = poly_at.find({pidx, steps});
         if (hit == poly_at.end()) {
+            std::lock_guard<std::recursive_mutex> lk(P.cache_mu);
             int slot;
             if (gpu_ok && P.jcache.find({pidx, steps}) == P.jcache.end() &&
                 __builtin_popcountll(steps) >= 2) {
