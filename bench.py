@@ -823,6 +823,8 @@ def main():
         s.synchronize()
         torch.cuda.synchronize()
         barrier()
+    # no timed steps (the bank- and serve-only runs): no headline number
+    timed = args.steps > 0
     ms = max_over_ranks(max(ev0.elapsed_time(ev1) / max(args.steps, 1), 1e-6), world)
     value = job_value(world, total_bytes, ms)
     # the last timed step's output and the windows after it, for the check
@@ -925,8 +927,9 @@ def main():
     # only when the autotuner chose the captured plan
     plan_key = (plan_cfg["core"], plan_cfg["split_chunk"], plan_cfg["grid"], plan_cfg["prejumps"])
     cap = CAPTURED_TRAFFIC.get(plan_key) if (nsub == N_SUB and args.uniform <= 0) else None
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 4), "peak_kind": peak_kind,
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1) if timed else None,
+                "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4) if timed else None, "peak_kind": peak_kind,
                 "traffic": cap["bytes"] if cap else None,
                 "traffic_source": cap["source"] if cap else "no capture of this plan",
                 "algorithmic_bytes": total_bytes + state_bytes, "kernel": kernel}
@@ -957,15 +960,15 @@ def main():
         bk.pop("_check", None)
     if rank == 0:
         line = {
-            "metric": METRIC, "value": round(value, 2), "unit": "GB/s",
+            "metric": METRIC, "value": round(value, 2) if timed else None, "unit": "GB/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": round(ms, 4) if timed else None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": WORKLOAD,
                        "output_bytes_per_step": total_bytes,
                        "l2": "no flush: each step writes %.2f GB, > 129 MB L2" % (total_bytes / 1e9),
                        "parallelism": "replicas" if world > 1 else "single"},
-            "pct_hbm": round(100 * value / world / hbm, 2),
+            "pct_hbm": round(100 * value / world / hbm, 2) if timed else None,
             "plain": None if plain_ms is None else {
                 "value": round(world * total_bytes / (plain_ms * 1e-3) / 1e9, 3), "unit": "GB/s",
                 "ms_per_step": round(plain_ms, 2), "launches_per_step": nsub},
@@ -975,13 +978,13 @@ def main():
                 "launches_per_step": nsub,
                 "how": "one CTA per substream, launches dealt to 32 CUDA streams, replayed "
                        "from one CUDA graph"},
-            "batched_over_plain": None if plain_ms is None else round(plain_ms / ms, 2),
-            "batched_over_plain_concurrent": None if plain_conc_ms is None
+            "batched_over_plain": None if plain_ms is None or not timed else round(plain_ms / ms, 2),
+            "batched_over_plain_concurrent": None if plain_conc_ms is None or not timed
             else round(plain_conc_ms / ms, 2),
             "write_peak": None if wpeak is None else {
                 "value": wpeak, "unit": "GB/s",
                 "how": "4 GiB written by one torch fill kernel, best of 10",
-                "pct_of_write_peak": round(100 * value / world / wpeak, 2)},
+                "pct_of_write_peak": round(100 * value / world / wpeak, 2) if timed else None},
             "check": check,
             "cold": cold,
             "banks": banks or None,
