@@ -279,6 +279,10 @@ struct Pool {
     Tuning tune = tuningDefaults();  // this pool's tuning knobs
 
     ~Pool() {
+        if (cache_stream) cudaStreamSynchronize(cache_stream);
+        if (afill.done) cudaEventDestroy(afill.done);
+        if (afill.h) cudaFreeHost(afill.h);
+        for (uint32_t *b : afill.old) cudaFreeHost(b);
         for (uint32_t *b : gpow_blocks) cudaFree(b);
         if (cache_stream) cudaStreamDestroy(cache_stream);
         cudaFree(d_params);
@@ -582,7 +586,7 @@ struct Pool {
     // The host keeps chi and copies of X^(2^i) (pow2) for its own paths.
     std::map<int, uint32_t *> gpow;
     std::vector<uint32_t *> gpow_blocks;  // allocations holding the tables
-    cudaStream_t cache_stream = nullptr;   // fillCache's products
+    cudaStream_t cache_stream = nullptr;   // startFill's products
     int prepare(const std::vector<int> &ks) {
         std::vector<int> miss;
         for (int k : ks)
@@ -746,31 +750,88 @@ struct Pool {
 
     // X^steps mod chi for (parameter set, steps) pairs not yet in the host
     // cache, computed on the GPU together (the tables of all their sets made
-    // first, in one prepare) and kept in the cache.
-    int fillCache(const std::vector<std::pair<int, uint64_t>> &want) {
+    // first, in one prepare) and put in the cache once they are back: a
+    // later plan's cache step (harvestFill) takes them.  No caller waits for
+    // the GPU here: products queued behind batches in flight would stall
+    // every plan of the pool.  One fill is in flight at a time; a plan that
+    // misses a polynomial makes it itself, on the GPU at its launch.
+    // harvestFill with cache_mu held; startFill takes it for its bookkeeping
+    // only, not while it queues the GPU work.
+    struct AsyncFill {
+        std::vector<std::pair<int, uint64_t>> keys;
+        uint32_t *h = nullptr;  // pinned: the products come back here
+        size_t cap = 0;         // words of h
+        std::vector<uint32_t *> old;  // smaller buffers, freed with the pool
+        cudaEvent_t done = nullptr;
+        bool busy = false;       // a fill is being queued or is in flight
+        bool submitted = false;  // ... and `done` is recorded after it
+    } afill;
+
+    void harvestFill() {
+        if (!afill.busy || !afill.submitted || cudaEventQuery(afill.done) != cudaSuccess) return;
+        const int W = polyWords();
+        if (jcache.size() + afill.keys.size() > 16384) jcache.clear();
+        for (size_t j = 0; j < afill.keys.size(); j++)
+            jcache[afill.keys[j]] = gf2::fromWords32(afill.h + j * (size_t)W, W);
+        afill.keys.clear();
+        afill.busy = false;
+        afill.submitted = false;
+    }
+
+    int startFill(const std::vector<std::pair<int, uint64_t>> &want) {
         std::vector<std::pair<int, uint64_t>> need;
-        for (const auto &q : want)
-            if (!jcache.count(q) && std::find(need.begin(), need.end(), q) == need.end())
-                need.push_back(q);
-        if (need.empty()) return MTGP_OK;
-        std::vector<int> sets;
-        for (const auto &q : need) sets.push_back(q.first);
-        int rc = prepare(sets);
-        if (rc) return rc;
-        const int W = polyWords(), n = (int)need.size();
-        std::vector<uint64_t> steps((size_t)n);
-        std::vector<const uint32_t *> tabs((size_t)n);
-        for (int j = 0; j < n; j++) {
-            steps[(size_t)j] = need[(size_t)j].second;
-            tabs[(size_t)j] = gpow.at(need[(size_t)j].first);
+        std::vector<const uint32_t *> tabs;
+        {
+            std::lock_guard<std::recursive_mutex> lk(cache_mu);
+            harvestFill();
+            if (afill.busy) return MTGP_OK;
+            for (const auto &q : want)
+                if (!jcache.count(q) && std::find(need.begin(), need.end(), q) == need.end())
+                    need.push_back(q);
+            if (need.empty()) return MTGP_OK;
+            std::vector<int> sets;
+            for (const auto &q : need) sets.push_back(q.first);
+            int rc = prepare(sets);
+            if (rc) return rc;
+            if (!cache_stream)
+                CK(cudaStreamCreateWithFlags(&cache_stream, cudaStreamNonBlocking),
+                   "cudaStreamCreate(cache)");
+            if (!afill.done)
+                CK(cudaEventCreateWithFlags(&afill.done, cudaEventDisableTiming),
+                   "cudaEventCreate(cache)");
+            for (const auto &q : need) tabs.push_back(gpow.at(q.first));
+            afill.busy = true;  // this thread owns afill until it is submitted
         }
+        int rc = queueFill(need, tabs);
+        std::lock_guard<std::recursive_mutex> lk(cache_mu);
+        if (rc) {
+            afill.busy = false;
+            return rc;
+        }
+        afill.keys = std::move(need);
+        afill.submitted = true;
+        return MTGP_OK;
+    }
+
+    // The GPU work of a fill (startFill owns afill meanwhile).
+    int queueFill(const std::vector<std::pair<int, uint64_t>> &need,
+                  const std::vector<const uint32_t *> &tabs) {
+        const int W = polyWords(), n = (int)need.size();
+        if ((size_t)n * W > afill.cap) {  // no fill in flight reads the old buffer
+            if (afill.h) afill.old.push_back(afill.h);
+            afill.h = nullptr;
+            afill.cap = 0;
+            const size_t cap = std::max<size_t>(2 * (size_t)n * W, (size_t)64 * W);
+            CK(hostAlloc(&afill.h, sizeof(uint32_t) * cap), "cudaMallocHost(cache products)");
+            afill.cap = cap;
+        }
+        std::vector<uint64_t> steps((size_t)n);
+        for (int j = 0; j < n; j++) steps[(size_t)j] = need[(size_t)j].second;
         PowSchedule sch;
         powSchedule(steps.data(), n, powWidth(), sch);
         // the pool's own stream and stream-ordered allocations: no
         // device-wide synchronization (a cudaFree would wait for every batch
-        // in flight), the host waits only for these products
-        if (!cache_stream) CK(cudaStreamCreateWithFlags(&cache_stream, cudaStreamNonBlocking),
-                              "cudaStreamCreate(cache)");
+        // in flight)
         const size_t out_bytes = sizeof(uint32_t) * (size_t)n * W;
         const size_t ops_bytes = (sizeof(PowOp) * (size_t)sch.steps() + 255) & ~size_t(255);
         const size_t bytes = ((out_bytes + 255) & ~size_t(255)) + ops_bytes +
@@ -782,8 +843,10 @@ struct Pool {
         PowOp *d_ops = reinterpret_cast<PowOp *>(d + ((out_bytes + 255) & ~size_t(255)));
         uint32_t *d_scratch = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(d_ops) +
                                                            ops_bytes);
-        std::vector<PowOp> ops;
+        std::vector<PowOp> &ops = afill_ops;
+        ops.clear();
         powOps(sch, [&tabs](int j) { return tabs[(size_t)j]; }, d_out, d_scratch, sh.mexp, ops);
+        // (a pageable source: the copy is staged before the call returns)
         cudaError_t e = cudaMemcpyAsync(d_ops, ops.data(), sizeof(PowOp) * ops.size(),
                                         cudaMemcpyHostToDevice, cache_stream);
         size_t first = 0;
@@ -792,18 +855,15 @@ struct Pool {
             e = launchPowOps(d_ops + first, m, d_scratch, W, cache_stream, tune.poly_window);
             first += (size_t)m;
         }
-        std::vector<uint32_t> h((size_t)n * W);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(h.data(), d_out, out_bytes, cudaMemcpyDeviceToHost, cache_stream);
+            e = cudaMemcpyAsync(afill.h, d_out, out_bytes, cudaMemcpyDeviceToHost, cache_stream);
         cudaError_t f = cudaFreeAsync(d, cache_stream);
         if (e == cudaSuccess) e = f;
-        if (e == cudaSuccess) e = cudaStreamSynchronize(cache_stream);
+        if (e == cudaSuccess) e = cudaEventRecord(afill.done, cache_stream);
         if (e != cudaSuccess) return cudaErr(e, "jump polynomials on the GPU");
-        if (jcache.size() + need.size() > 16384) jcache.clear();
-        for (int j = 0; j < n; j++)
-            jcache[need[(size_t)j]] = gf2::fromWords32(h.data() + (size_t)j * W, W);
         return MTGP_OK;
     }
+    std::vector<PowOp> afill_ops;
 
     // Public form: host exponents, device output (mtgp*_gpu_pool_jump_polys).
     int jumpPolysApi(int k, const uint64_t *steps, int n, uint32_t *out, void *s) {
@@ -1118,7 +1178,11 @@ struct mtgp_gpu_plan {
 
     cudaGraphExec_t exec = nullptr;
     void *graph_out = nullptr;
+    // buffers replaced by larger ones, freed with the plan
+    std::vector<void *> retired_dev, retired_host;
     ~mtgp_gpu_plan() {
+        for (void *b : retired_dev) cudaFree(b);
+        for (void *b : retired_host) cudaFreeHost(b);
         if (exec) cudaGraphExecDestroy(exec);
         if (side) cudaStreamDestroy(side);
         if (fork) cudaEventDestroy(fork);

@@ -102,6 +102,12 @@ __host__ __device__ constexpr int stateStride(int n) { return (n + 31) & ~31; }
 void toDev(const mtgp32_params_fast_t &p, DevParams32 *d);
 // Store msg as the calling thread's mtgp_gpu_last_error(); returns code.
 int recordError(int code, const char *msg);
+
+// The part of a plan's launch that reads no stream window and writes no
+// output: its descriptor upload, its GPU-made jump polynomials and the
+// zeroing of new pre-jumped window slots, queued on stream s.  The plan's
+// next launch (or graph capture) then skips them.
+int planPrepare(mtgp_gpu_plan_t *pl, void *s);
 void toDev(const mtgp64_params_fast_t &p, DevParams64 *d);
 
 // ---- generation (gen_kernels.cu) ----------------------------------------

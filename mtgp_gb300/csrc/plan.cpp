@@ -105,7 +105,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         return MTGP_OK;
     };
     // every parameter set that jumps gets its tables in one batch, and the
-    // chunk offsets not yet cached are computed together on the GPU
+    // chunk offsets not yet cached (with the run start where the two make
+    // one polynomial) go to the GPU together, for later plans
     {
         std::vector<int> sets;
         std::vector<std::pair<int, uint64_t>> offs;
@@ -113,11 +114,14 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (!pt.run && !pt.off) continue;
             const int k = P.hpidx[pt.stream];
             if (std::find(sets.begin(), sets.end(), k) == sets.end()) sets.push_back(k);
-            if (pt.off && __builtin_popcountll(pt.off) >= 2) offs.emplace_back(k, pt.off);
+            const uint64_t e = pt.run && !kernel_jumps ? pt.run + pt.off : pt.off;
+            if (pt.off && __builtin_popcountll(e) >= 2) offs.emplace_back(k, e);
         }
-        std::lock_guard<std::recursive_mutex> lk(P.cache_mu);
-        rc = P.prepare(sets);
-        if (!rc) rc = P.fillCache(offs);
+        {
+            std::lock_guard<std::recursive_mutex> lk(P.cache_mu);
+            rc = P.prepare(sets);
+        }
+        if (!rc) rc = P.startFill(offs);
         if (rc) return rc;
     }
     std::vector<BatchTask> tasks(R.tasks.size());
@@ -138,9 +142,9 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             rc = polyIndex(t.pidx, pt.run + pt.off, &t.j0, true);
         } else if (pt.run && pt.off) {
             rc = polyIndex(t.pidx, pt.run, &t.j0, true);
-            if (!rc) rc = polyIndex(t.pidx, pt.off, &t.j1, false);
+            if (!rc) rc = polyIndex(t.pidx, pt.off, &t.j1, true);
         } else if (pt.run || pt.off) {
-            rc = polyIndex(t.pidx, pt.run | pt.off, &t.j0, pt.run != 0);
+            rc = polyIndex(t.pidx, pt.run | pt.off, &t.j0, true);
         }
         if (rc) return rc;
     }
@@ -248,48 +252,40 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&pl->join, cudaEventDisableTiming);
     }
-    if (e == cudaSuccess && bytes > pl->cap_d) {
-        cudaFree(pl->d_blob);
-        pl->d_blob = nullptr;
-        pl->cap_d = 0;
-        e = devMalloc(&pl->d_blob, bytes + bytes / 4);
-        if (e == cudaSuccess) pl->cap_d = bytes + bytes / 4;
-    }
+    // Buffers only grow, to twice what is needed, and a buffer replaced by a
+    // larger one is freed with the plan: freeing it now (cudaFree,
+    // cudaFreeHost) would wait for every launch in flight on the device, and
+    // an earlier launch of this plan may still read it.
+    auto growDev = [pl](auto **buf, size_t *cap, size_t need) -> cudaError_t {
+        if (need <= *cap) return cudaSuccess;
+        if (*buf) pl->retired_dev.push_back(*buf);
+        *buf = nullptr;
+        *cap = 0;
+        const size_t n = std::max<size_t>(2 * need, 4096);
+        cudaError_t err = devMallocRaw(reinterpret_cast<void **>(buf), n);
+        if (err == cudaSuccess) *cap = n;
+        return err;
+    };
+    if (e == cudaSuccess) e = growDev(&pl->d_blob, &pl->cap_d, bytes);
     if (e == cudaSuccess && bytes > pl->cap_h) {
-        cudaFreeHost(pl->h_blob);
+        if (pl->h_blob) pl->retired_host.push_back(pl->h_blob);
         pl->h_blob = nullptr;
         pl->cap_h = 0;
-        e = hostAlloc(&pl->h_blob, bytes + bytes / 4);
-        if (e == cudaSuccess) pl->cap_h = bytes + bytes / 4;
+        const size_t n = std::max<size_t>(2 * bytes, 4096);
+        e = hostAlloc(&pl->h_blob, n);
+        if (e == cudaSuccess) pl->cap_h = n;
     }
-    if (e == cudaSuccess && (size_t)sch.nscratch * pw > pl->cap_pscratch) {
-        const size_t need = (size_t)sch.nscratch * pw;
-        cudaFree(pl->d_pscratch);
-        pl->d_pscratch = nullptr;
-        pl->cap_pscratch = 0;
-        e = devMalloc(&pl->d_pscratch, sizeof(uint32_t) * (need + need / 4));
-        if (e == cudaSuccess) pl->cap_pscratch = need + need / 4;
+    if (e == cudaSuccess) {
+        size_t cap = pl->cap_pscratch * sizeof(uint32_t);
+        e = growDev(&pl->d_pscratch, &cap, sizeof(uint32_t) * (size_t)sch.nscratch * pw);
+        pl->cap_pscratch = cap / sizeof(uint32_t);
     }
-    if (e == cudaSuccess && pl->nstage) {
-        const size_t need = sizeof(W) * (size_t)P.stride * pl->nstage;
-        if (need > pl->cap_stage) {
-            cudaFree(pl->d_stage);
-            pl->d_stage = nullptr;
-            pl->cap_stage = 0;
-            e = devMalloc(&pl->d_stage, need + need / 4);
-            if (e == cudaSuccess) pl->cap_stage = need + need / 4;
-        }
-    }
+    if (e == cudaSuccess && pl->nstage)
+        e = growDev(&pl->d_stage, &pl->cap_stage, sizeof(W) * (size_t)P.stride * pl->nstage);
     if (e == cudaSuccess && pl->npre) {
-        const size_t need = sizeof(W) * (size_t)P.stride * pl->npre;
-        if (need > pl->cap_prewin) {
-            cudaFree(pl->d_prewin);
-            pl->d_prewin = nullptr;
-            pl->cap_prewin = 0;
-            e = devMalloc(&pl->d_prewin, need + need / 4);
-            if (e == cudaSuccess) pl->cap_prewin = need + need / 4;
-            pl->prewin_fresh = true;
-        }
+        const size_t before = pl->cap_prewin;
+        e = growDev(&pl->d_prewin, &pl->cap_prewin, sizeof(W) * (size_t)P.stride * pl->npre);
+        if (pl->cap_prewin != before) pl->prewin_fresh = true;
     }
     if (e != cudaSuccess) {
         if (fresh) {
@@ -449,6 +445,21 @@ template int launchPlan<T32>(mtgp_gpu_plan *, void *, void *);
 template int launchPlan<T64>(mtgp_gpu_plan *, void *, void *);
 
 }  // namespace host
+
+int planPrepare(mtgp_gpu_plan_t *pl, void *s) {
+    if (!pl) return setErr(MTGP_ERR_INVALID, "null plan");
+    int rc = uploadPlan(pl, s);
+    if (!rc) {
+        const int pw = pl->bits == 32 ? static_cast<Pool<T32> *>(pl->pool)->polyWords()
+                                      : static_cast<Pool<T64> *>(pl->pool)->polyWords();
+        const int win = pl->bits == 32 ? static_cast<Pool<T32> *>(pl->pool)->tune.poly_window
+                                       : static_cast<Pool<T64> *>(pl->pool)->tune.poly_window;
+        rc = powJobs(pl, pw, win, s);
+    }
+    if (!rc) rc = clearPrewin(pl, s);
+    return rc;
+}
+
 }  // namespace mtgp
 
 extern "C" {
@@ -469,15 +480,7 @@ int mtgp_gpu_plan_graph_launch(mtgp_gpu_plan_t *pl, void *out, void *s) {
         cudaGraph_t g = nullptr;
         // before the capture: replays reuse the descriptors and the GPU-made
         // jump polynomials
-        int up = uploadPlan(pl, s);
-        if (!up) {
-            const int pw = pl->bits == 32 ? static_cast<Pool<T32> *>(pl->pool)->polyWords()
-                                          : static_cast<Pool<T64> *>(pl->pool)->polyWords();
-            const int win = pl->bits == 32 ? static_cast<Pool<T32> *>(pl->pool)->tune.poly_window
-                                           : static_cast<Pool<T64> *>(pl->pool)->tune.poly_window;
-            up = powJobs(pl, pw, win, s);
-        }
-        if (!up) up = clearPrewin(pl, s);
+        int up = mtgp::planPrepare(pl, s);
         if (up) return up;
         CK(cudaStreamBeginCapture(S(s), cudaStreamCaptureModeThreadLocal), "begin capture");
         int rc = planLaunch(pl, out, s);

@@ -1,11 +1,13 @@
 // server_core.h -- the serving loop's admission rules and output arena (no
 // CUDA), shared by server.cpp and the CPU tests.
 #pragma once
+#include <algorithm>
 #include <chrono>
 #include <cstdint>
 #include <deque>
 #include <iterator>
 #include <map>
+#include <utility>
 #include <vector>
 
 namespace mtgp {
@@ -75,47 +77,97 @@ struct ServeReq {
     std::chrono::steady_clock::time_point t_submit;
 };
 
-// Stream states during admission: free, in a batch on the GPU, in the batch
-// being formed, in the batch being formed but closed to more requests.
-enum : char { kStreamFree = 0, kStreamBusy = 1, kStreamForming = 2, kStreamClosed = 3 };
+inline std::vector<std::pair<int, uint32_t>> &waitingScratch() {
+    static thread_local std::vector<std::pair<int, uint32_t>> v;
+    return v;
+}
+
+// Per-stream marks during one admission pass (all kStreamFree between
+// passes): not in the batch being formed, in it, in it but closed to more
+// requests.
+enum : char { kStreamFree = 0, kStreamForming = 1, kStreamClosed = 2 };
 
 // Move the next batch's requests from `pending` to `take`, in one pass:
 //   - first come, first served: admission stops at the first request whose
-//     output does not fit in the arena;
-//   - a request whose stream has work on the GPU waits (it stays pending, in
-//     order, with every later request of that stream);
+//     output would take the batch past `limit` bytes, or past `soft` bytes
+//     when it is not the batch's first request.  The batch's outputs are laid
+//     out back to back, each rounded up to the arena's 256-byte granule;
+//     r.off is the offset in the batch's block, which is placed in the arena
+//     later (Arena::alloc);
+//   - a stream may have earlier batches still on the GPU: if `held(r)` says
+//     so for its first request in the pass, the stream waits (with all its
+//     later requests) for them to finish; otherwise its requests join, and
+//     the caller orders the new batch after those batches (StreamOrder);
 //   - several requests of one stream may join the batch, in order, except
 //     that a skip of at least `jump_skip` only opens a stream's part of a
 //     batch (its jump is then X^skip from the window, a polynomial shared by
-//     many requests, instead of X^(an arbitrary position));
+//     many requests, instead of X^(an arbitrary position)); the stream's
+//     later requests then wait for the next batch;
 //   - at most `max_batch` requests, and at most `max_scan` pending requests
-//     looked at (a bound on the time the caller holds its lock when the
-//     backlog is long and mostly waits for streams on the GPU).
-// busy[pool][stream] holds the stream states; admitted streams end as busy.
-inline void admitBatch(std::deque<ServeReq> &pending, std::vector<char> *busy, Arena &arena,
-                       int max_batch, uint64_t jump_skip, std::vector<ServeReq> *take,
-                       size_t max_scan = ~size_t(0)) {
+//     looked at (a bound on the time the caller holds its lock).
+// mark[pool][stream] is scratch.  Returns the block's size in bytes.
+template <class Held>
+uint64_t admitBatch(std::deque<ServeReq> &pending, std::vector<char> *mark, int max_batch,
+                    uint64_t jump_skip, uint64_t limit, uint64_t soft, Held held,
+                    std::vector<ServeReq> *take, size_t max_scan = ~size_t(0)) {
     take->clear();
+    std::vector<std::pair<int, uint32_t>> &waiting = waitingScratch();
+    waiting.clear();
+    uint64_t used = 0;
     auto w = pending.begin(), it = pending.begin();
     for (size_t scanned = 0;
          it != pending.end() && (int)take->size() < max_batch && scanned < max_scan;
          ++it, ++scanned) {
-        char &b = busy[it->pool][it->stream];
-        if (b == kStreamForming && it->skip >= jump_skip) b = kStreamClosed;
-        if (b == kStreamBusy || b == kStreamClosed) {
+        char &m = mark[it->pool][it->stream];
+        if (m == kStreamFree && held(*it)) {
+            m = kStreamClosed;
+            waiting.emplace_back(it->pool, it->stream);
+        }
+        if (m == kStreamForming && it->skip >= jump_skip) m = kStreamClosed;
+        if (m == kStreamClosed) {
             if (w != it) *w = *it;
             ++w;
             continue;
         }
-        uint64_t off = 0;
-        if (!arena.alloc(it->bytes, &off)) break;
-        it->off = off;
-        b = kStreamForming;
+        const uint64_t n = Arena::round(it->bytes);
+        if (n > limit - used || (!take->empty() && n > soft - std::min(used, soft))) break;
+        it->off = used;
+        used += n;
+        m = kStreamForming;
         take->push_back(*it);
     }
     pending.erase(w, it);
-    // (a stream is only closed after it joined, so this reaches all of them)
-    for (const ServeReq &r : *take) busy[r.pool][r.stream] = kStreamBusy;
+    for (const ServeReq &r : *take) mark[r.pool][r.stream] = kStreamFree;
+    for (const auto &ps : waiting) mark[ps.first][ps.second] = kStreamFree;
+    return used;
 }
+
+// The order of batches on the GPU: a batch that holds requests of a stream
+// must run after that stream's earlier batches, which read and write the
+// stream's window.  Each stream remembers its latest batch by a caller-chosen
+// tag (non-zero); deps[pool] receives the distinct tags of those earlier
+// batches, through the pool's streams, that `live(tag)` still reports in
+// flight.
+struct StreamOrder {
+    std::vector<uint64_t> last[2];
+    uint64_t latest(const ServeReq &r) const { return last[r.pool][r.stream]; }
+    void init(size_t n0, size_t n1) {
+        last[0].assign(n0, 0);
+        last[1].assign(n1, 0);
+    }
+    template <class Live>
+    void order(const std::vector<ServeReq> &take, uint64_t tag, Live live,
+               std::vector<uint64_t> deps[2]) {
+        deps[0].clear();
+        deps[1].clear();
+        for (const ServeReq &r : take) {
+            uint64_t &l = last[r.pool][r.stream];
+            std::vector<uint64_t> &d = deps[r.pool];
+            if (l && l != tag && live(l) && std::find(d.begin(), d.end(), l) == d.end())
+                d.push_back(l);
+            l = tag;
+        }
+    }
+};
 
 }  // namespace mtgp

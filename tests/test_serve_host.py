@@ -1,9 +1,11 @@
-"""The serving loop's admission rules and output arena
+"""The serving loop's admission rules, stream order and output arena
 (mtgp_gb300/csrc/server_core.h) on the CPU, through simulated traces: every
 request is admitted once; a stream's requests are admitted in submission
-order and never while the stream has a batch on the GPU; a long skip only
-opens a stream's part of a batch; batches respect max_batch; in-flight
-outputs never overlap in the arena nor exceed the budget; all space returns."""
+order; a batch holding a stream whose earlier batch is still in flight is
+ordered after that batch; a long skip only opens a stream's part of a batch;
+batches respect max_batch and half the budget; blocks are placed in
+admission order; in-flight outputs never overlap in the arena nor exceed the
+budget; all space returns."""
 import ctypes
 import os
 import subprocess
@@ -22,12 +24,13 @@ def probe(tmp_path_factory):
                     os.path.join(HERE, "serve_probe.cpp")], check=True)
     L = ctypes.CDLL(so)
     vp, ci = ctypes.c_void_p, ctypes.c_int
-    L.probe_serve.argtypes = [ci, vp, vp, vp, vp, ci, ci, ctypes.c_uint64, ci, ci, vp, ci,
-                              vp, vp, vp, vp, vp, vp]
+    L.probe_serve.argtypes = [ci, vp, vp, vp, vp, ci, ci, ctypes.c_uint64, ci, ci, ci, vp,
+                              ci, vp, vp, vp, vp, vp, vp, vp, vp]
     return L
 
 
-def simulate(probe, pool, stream, skip, nbytes, ns, budget, max_batch, slots, seed):
+def simulate(probe, pool, stream, skip, nbytes, ns, budget, max_batch, slots, seed,
+             pipe_backlog=0):
     n = len(pool)
     p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     pool = np.ascontiguousarray(pool, np.int32)
@@ -39,20 +42,27 @@ def simulate(probe, pool, stream, skip, nbytes, ns, budget, max_batch, slots, se
     off = np.zeros(n, np.uint64)
     rank = np.full(n, -1, np.int32)
     badm = np.zeros(n + 1, np.int32)
+    bplc = np.zeros(n + 1, np.int32)
     bret = np.zeros(n + 1, np.int32)
+    deps = np.full((n + 1) * slots, -1, np.int32)
     nb = ctypes.c_int()
     rc = probe.probe_serve(n, p(pool), p(stream), p(skip), p(nbytes), ns[0], ns[1], budget,
-                           max_batch, slots, p(retire), len(retire), p(batch), p(off), p(rank),
-                           p(badm), p(bret), ctypes.byref(nb))
-    return rc, batch, off, rank, badm[:nb.value], bret[:nb.value]
+                           max_batch, slots, pipe_backlog, p(retire), len(retire), p(batch),
+                           p(off), p(rank),
+                           p(badm), p(bplc), p(bret), p(deps), ctypes.byref(nb))
+    m = nb.value
+    return dict(rc=rc, batch=batch, off=off, rank=rank, admit=badm[:m], place=bplc[:m],
+                retire=bret[:m], deps=[set(d[d >= 0].tolist()) for d in deps[:m * slots]
+                                       .reshape(m, slots)] if m else [])
 
 
 def round256(x):
     return (int(x) + 255) // 256 * 256
 
 
+@pytest.mark.parametrize("pipe_backlog", [0, 100, 1 << 30])
 @pytest.mark.parametrize("seed", range(6))
-def test_admission_invariants(probe, seed):
+def test_admission_invariants(probe, seed, pipe_backlog):
     rng = np.random.default_rng(seed)
     n = 600
     ns = (int(rng.integers(1, 40)), int(rng.integers(1, 8)))
@@ -64,54 +74,90 @@ def test_admission_invariants(probe, seed):
     budget = 1 << 20
     max_batch = int(rng.integers(1, 64))
     slots = int(rng.integers(1, 5))
-    rc, batch, off, rank, badm, bret = simulate(probe, pool, stream, skip, nbytes, ns, budget,
-                                                max_batch, slots, seed)
-    assert rc == 0
+    r = simulate(probe, pool, stream, skip, nbytes, ns, budget, max_batch, slots, seed,
+                 pipe_backlog)
+    assert r["rc"] == 0
+    batch, off, rank = r["batch"], r["off"], r["rank"]
     assert (batch >= 0).all()
     assert len(set(rank.tolist())) == n
-    nb = len(badm)
+    nb = len(r["admit"])
     assert np.bincount(batch, minlength=nb).max() <= max_batch
-    # per stream: submission order == admission order
+    # blocks are placed in admission order
+    assert np.all(np.diff(r["place"]) >= 0)
+    assert np.all(r["place"] >= r["admit"]) and np.all(r["retire"] > r["place"])
     for q in (0, 1):
         for s in range(ns[q]):
             idx = np.nonzero((pool == q) & (stream == s))[0]
+            # per stream: submission order == admission order
             assert np.all(np.diff(rank[idx]) > 0)
-            # a long skip only as the first of its stream in a batch
             for k in range(1, len(idx)):
+                a, b = batch[idx[k - 1]], batch[idx[k]]
+                # a long skip only as the first of its stream in a batch
                 if skip[idx[k]] >= (1 << 17):
-                    assert batch[idx[k]] != batch[idx[k - 1]]
-    # batches that overlap in time share no stream and no arena bytes
-    live = [(badm[b], bret[b]) for b in range(nb)]
-    keys = [set(zip(pool[batch == b].tolist(), stream[batch == b].tolist())) for b in range(nb)]
+                    assert a != b
+                # a later batch of the stream runs after the earlier one: it
+                # was retired before the later one was admitted, or the
+                # later one is ordered after it
+                if a != b:
+                    assert a < b
+                    assert r["retire"][a] < r["admit"][b] or a in r["deps"][b]
+                    assert r["retire"][a] < r["retire"][b]
+                    if pipe_backlog > n:  # never pipelined: one batch of a stream at a time
+                        assert r["retire"][a] < r["admit"][b]
     spans = [[(int(off[k]), int(off[k]) + round256(nbytes[k])) for k in np.nonzero(batch == b)[0]
               if nbytes[k]] for b in range(nb)]
-    for a in range(nb):
-        for b in range(a + 1, nb):
-            if live[a][0] < live[b][1] and live[b][0] < live[a][1]:
-                assert not (keys[a] & keys[b])
-                for x0, x1 in spans[a]:
-                    for y0, y1 in spans[b]:
-                        assert x1 <= y0 or y1 <= x0
     for b in range(nb):
         sp = sorted(spans[b])
         assert all(sp[i][1] <= sp[i + 1][0] for i in range(len(sp) - 1))
         assert all(x1 <= budget for _, x1 in sp)
+        # at most half the budget, unless the batch is one request
+        size = sum(x1 - x0 for x0, x1 in sp)
+        assert size <= budget // 2 or len(sp) == 1
+    # batches in the arena at the same time share no bytes
+    for a in range(nb):
+        for b in range(a + 1, nb):
+            if r["place"][a] < r["retire"][b] and r["place"][b] < r["retire"][a]:
+                for x0, x1 in spans[a]:
+                    for y0, y1 in spans[b]:
+                        assert x1 <= y0 or y1 <= x0
 
 
 def test_first_come_first_served(probe):
-    # a request that does not fit blocks later ones (no overtaking by small
-    # requests), until space returns
-    pool = [0, 0, 0]
-    stream = [0, 1, 2]
-    nbytes = [700_000, 700_000, 1000]
-    rc, batch, off, rank, badm, bret = simulate(probe, pool, stream, [0, 0, 0], nbytes,
-                                                (3, 1), 1 << 20, 8, 4, 0)
-    assert rc == 0
-    assert batch[0] == 0 and batch[1] == batch[2] == 1
+    # a batch whose block does not fit holds back later ones (no overtaking by
+    # small requests) until space returns; a batch takes at most half the
+    # budget unless it is one request
+    r = simulate(probe, [0, 0, 0], [0, 1, 2], [0, 0, 0], [700_000, 700_000, 1000], (3, 1),
+                 1 << 20, 8, 4, 0)
+    assert r["rc"] == 0
+    assert r["batch"].tolist() == [0, 1, 2]
+    assert r["place"][1] > r["retire"][0] and r["place"][2] >= r["place"][1]
 
 
 def test_same_stream_shares_a_batch(probe):
-    rc, batch, off, rank, badm, bret = simulate(probe, [0] * 4, [5] * 4, [0, 0, 1 << 20, 0],
-                                                [100] * 4, (8, 1), 1 << 20, 8, 4, 0)
-    assert rc == 0
-    assert batch.tolist() == [0, 0, 1, 1]
+    r = simulate(probe, [0] * 4, [5] * 4, [0, 0, 1 << 20, 0], [100] * 4, (8, 1), 1 << 20, 8,
+                 4, 0)
+    assert r["rc"] == 0
+    assert r["batch"].tolist() == [0, 0, 1, 1]
+
+
+def test_stream_in_flight_waits_without_backlog(probe):
+    # the same trace without a backlog: the stream's second request waits for
+    # its first batch, and the other stream's request goes ahead of it
+    r = simulate(probe, [0, 0, 0], [3, 3, 4], [0, 0, 0], [100, 100, 100], (8, 1), 1 << 20, 1,
+                 4, 0, pipe_backlog=1 << 30)
+    assert r["rc"] == 0
+    assert r["batch"].tolist() == [0, 2, 1]
+    assert r["admit"][2] > r["retire"][0]
+    assert r["deps"] == [set(), set(), set()]
+
+
+def test_stream_in_flight_joins_the_next_batch(probe):
+    # one request per batch: the stream's second request is admitted while its
+    # first batch is in flight and ordered after it; another stream's is not
+    r = simulate(probe, [0, 0, 0], [3, 3, 4], [0, 0, 0], [100, 100, 100], (8, 1), 1 << 20, 1,
+                 4, 0)
+    assert r["rc"] == 0
+    assert r["batch"].tolist() == [0, 1, 2]
+    assert r["admit"][1] < r["retire"][0]
+    assert r["deps"] == [set(), {0}, set()]
+    assert r["retire"][1] > r["retire"][0]
