@@ -495,11 +495,16 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
  * one launch per request).  A server owns a device output arena of
  * `budget_bytes` (the memory budget) and a scheduler thread that admits
  * pending requests first-come-first-served into batches of at most
- * `max_batch` requests, keeps up to `slots` batches in flight on their own
- * CUDA streams, and copies each result to its destination when the batch
- * completes.  Requests of one stream run in submission order; a request's
- * values depend only on its stream's position, so they are the same alone and
- * in any mix.  While a server runs, its pools must not be used otherwise. */
+ * `max_batch` requests (and half the budget), keeps up to `slots` (at most
+ * 256) batches in flight on their own CUDA streams, and copies each result
+ * to its destination when the batch completes.  A batch's outputs take one
+ * block of the arena, placed in admission order; results kept in the arena
+ * (mtgp_server_submit without destination) hold their part of a block until
+ * released, so long-kept results fragment the arena.  Requests of one
+ * stream run in submission order (a batch that holds a stream runs on the
+ * GPU after the stream's earlier batches); a request's values depend only
+ * on its stream's position, so they are the same alone and in any mix.
+ * While a server runs, its pools must not be used otherwise. */
 typedef struct mtgp_server mtgp_server_t;
 
 /* One request of a trace (mtgp_server_replay). */
@@ -533,7 +538,9 @@ int mtgp_server_result(mtgp_server_t *s, uint64_t ticket, void **dev_ptr,
                        uint64_t *bytes);
 int mtgp_server_release(mtgp_server_t *s, uint64_t ticket);
 /* Remove a request that has not been admitted yet; its status becomes
- * MTGP_ERR_BUSY.  Fails with MTGP_ERR_INVALID once it is admitted. */
+ * MTGP_ERR_BUSY.  Fails with MTGP_ERR_INVALID once it is admitted.  (A
+ * request is not admitted while the arena, less the results kept in it and
+ * the batches admitted but not yet placed, cannot hold it.) */
 int mtgp_server_cancel(mtgp_server_t *s, uint64_t ticket);
 /* Wait until a request is done (its destination holds the result);
  * `status` receives MTGP_OK or the error it ended with (a request whose batch

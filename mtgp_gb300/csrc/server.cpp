@@ -6,13 +6,16 @@
 // persistent launch per pool (the batched kernels, through the public plan
 // API):
 //   - up to `slots` batches are in flight at once, each on its own CUDA
-//     stream, so a batch admitted while others run overlaps them on the GPU;
+//     streams (one per pool), so a batch admitted while others run overlaps
+//     them on the GPU, and a batch's two pools run side by side;
 //   - admission is first-come, first-served; requests of one stream run in
 //     submission order, each seeing the stream where the previous one left
-//     it: several may share a batch (run in order by the plan), and a stream
-//     whose earlier requests are still on the GPU may join a new batch, which
-//     the GPU then runs after those batches (an event wait per earlier batch
-//     on the new batch's CUDA stream, made once they are launched);
+//     it.  Several may share a batch (run in order by the plan).  A stream
+//     whose earlier requests are still on the GPU waits for them under a
+//     light load (so that batches share no stream and run side by side);
+//     under a backlog it joins the new batch, which the GPU then runs after
+//     those batches: an event wait per earlier batch on the new batch's
+//     CUDA stream of that pool, made once they are launched;
 //   - a batch's outputs take one block of the device output arena (the
 //     memory budget), placed in admission order once the batch is planned;
 //   - a request's skip is done by generation when short and by a GF(2) jump
@@ -31,12 +34,12 @@
 // several threads at once), places it in the arena, launches it, waits for
 // it on the GPU and retires it (latencies, arena space).  So the host work
 // of up to `slots` batches runs in parallel, and the lock they share is held
-// for a few word writes per request.  A batch is admitted (everything
-// admissible, up to max_batch requests and half the arena) when a slot is
-// free and no other batch is being planned (low load: a lone request goes
-// straight to the GPU; under load the next batch collects what arrives
-// while one is planned), or when a quarter of a full batch is waiting: only
-// then are several batches planned at once.
+// for a few word writes per request.  A batch is admitted (up to max_batch
+// requests and half the arena; under a backlog, half of what waits) when a
+// slot is free and no other batch is being planned (low load: a lone
+// request goes straight to the GPU; under load the next batch collects what
+// arrives while one is planned), or when a quarter of a full batch is
+// waiting: only then are several batches planned at once.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -265,8 +268,16 @@ void mtgp_server::loop() {
             // waits, so that batches of a light load share no stream and
             // run side by side on the GPU instead of one after another.
             const bool pipe = pending.size() >= (size_t)std::max(1, max_batch / 4);
+            // Under a backlog a batch takes half of what waits (at least a
+            // quarter of max_batch): a burst still gets full batches, while a
+            // steady load near capacity gets batches just large enough to
+            // keep up.  Taking all that waits there locks the loop into
+            // batches whose formation and GPU time double the latency.
+            const int cap = pipe ? std::min(max_batch, std::max(max_batch / 4,
+                                                                (int)(pending.size() / 2)))
+                                 : max_batch;
             fs->block_bytes = mtgp::admitBatch(
-                pending, mark, max_batch, kJumpSkip, arena.size() - kept_bytes - ahead,
+                pending, mark, cap, kJumpSkip, arena.size() - kept_bytes - ahead,
                 arena.size() / 2,
                 [&](const Req &r) {
                     const uint64_t l = order.latest(r);
