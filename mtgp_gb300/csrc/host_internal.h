@@ -283,6 +283,10 @@ struct Pool {
         if (afill.done) cudaEventDestroy(afill.done);
         if (afill.h) cudaFreeHost(afill.h);
         for (uint32_t *b : afill.old) cudaFreeHost(b);
+        if (afill.h_ops) cudaFreeHost(afill.h_ops);
+        for (unsigned char *b : afill.old_h) cudaFreeHost(b);
+        cudaFree(afill.d);
+        for (unsigned char *b : afill.old_d) cudaFree(b);
         for (uint32_t *b : gpow_blocks) cudaFree(b);
         if (cache_stream) cudaStreamDestroy(cache_stream);
         cudaFree(d_params);
@@ -762,6 +766,11 @@ struct Pool {
         uint32_t *h = nullptr;  // pinned: the products come back here
         size_t cap = 0;         // words of h
         std::vector<uint32_t *> old;  // smaller buffers, freed with the pool
+        // device buffer (products | ops | scratch) and pinned ops, kept and
+        // grown (an allocation on the way could wait for the GPU)
+        unsigned char *d = nullptr, *h_ops = nullptr;
+        size_t dcap = 0, h_ops_cap = 0;
+        std::vector<unsigned char *> old_d, old_h;
         cudaEvent_t done = nullptr;
         bool busy = false;       // a fill is being queued or is in flight
         bool submitted = false;  // ... and `done` is recorded after it
@@ -829,16 +838,27 @@ struct Pool {
         for (int j = 0; j < n; j++) steps[(size_t)j] = need[(size_t)j].second;
         PowSchedule sch;
         powSchedule(steps.data(), n, powWidth(), sch);
-        // the pool's own stream and stream-ordered allocations: no
-        // device-wide synchronization (a cudaFree would wait for every batch
-        // in flight)
+        // on the pool's own stream, in buffers that only grow (freeing one
+        // would wait for every batch in flight; no fill is in flight here)
         const size_t out_bytes = sizeof(uint32_t) * (size_t)n * W;
         const size_t ops_bytes = (sizeof(PowOp) * (size_t)sch.steps() + 255) & ~size_t(255);
         const size_t bytes = ((out_bytes + 255) & ~size_t(255)) + ops_bytes +
                              sizeof(uint32_t) * (size_t)sch.nscratch * W;
-        unsigned char *d = nullptr;
-        CK(devMallocAsync(reinterpret_cast<void **>(&d), bytes, cache_stream),
-           "devMallocAsync(cache products)");
+        if (bytes > afill.dcap) {
+            if (afill.d) afill.old_d.push_back(afill.d);
+            afill.d = nullptr;
+            afill.dcap = 0;
+            CK(devMalloc(&afill.d, 2 * bytes), "cudaMalloc(cache products)");
+            afill.dcap = 2 * bytes;
+        }
+        if (ops_bytes > afill.h_ops_cap) {
+            if (afill.h_ops) afill.old_h.push_back(afill.h_ops);
+            afill.h_ops = nullptr;
+            afill.h_ops_cap = 0;
+            CK(hostAlloc(&afill.h_ops, 2 * ops_bytes), "cudaMallocHost(cache ops)");
+            afill.h_ops_cap = 2 * ops_bytes;
+        }
+        unsigned char *d = afill.d;
         uint32_t *d_out = reinterpret_cast<uint32_t *>(d);
         PowOp *d_ops = reinterpret_cast<PowOp *>(d + ((out_bytes + 255) & ~size_t(255)));
         uint32_t *d_scratch = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(d_ops) +
@@ -846,8 +866,8 @@ struct Pool {
         std::vector<PowOp> &ops = afill_ops;
         ops.clear();
         powOps(sch, [&tabs](int j) { return tabs[(size_t)j]; }, d_out, d_scratch, sh.mexp, ops);
-        // (a pageable source: the copy is staged before the call returns)
-        cudaError_t e = cudaMemcpyAsync(d_ops, ops.data(), sizeof(PowOp) * ops.size(),
+        std::memcpy(afill.h_ops, ops.data(), sizeof(PowOp) * ops.size());
+        cudaError_t e = cudaMemcpyAsync(d_ops, afill.h_ops, sizeof(PowOp) * ops.size(),
                                         cudaMemcpyHostToDevice, cache_stream);
         size_t first = 0;
         for (size_t l = 0; e == cudaSuccess && l < sch.levels.size(); l++) {
@@ -857,8 +877,6 @@ struct Pool {
         }
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(afill.h, d_out, out_bytes, cudaMemcpyDeviceToHost, cache_stream);
-        cudaError_t f = cudaFreeAsync(d, cache_stream);
-        if (e == cudaSuccess) e = f;
         if (e == cudaSuccess) e = cudaEventRecord(afill.done, cache_stream);
         if (e != cudaSuccess) return cudaErr(e, "jump polynomials on the GPU");
         return MTGP_OK;

@@ -268,14 +268,10 @@ void mtgp_server::loop() {
             // waits, so that batches of a light load share no stream and
             // run side by side on the GPU instead of one after another.
             const bool pipe = pending.size() >= (size_t)std::max(1, max_batch / 4);
-            // Under a backlog a batch takes half of what waits (at least a
-            // quarter of max_batch): a burst still gets full batches, while a
-            // steady load near capacity gets batches just large enough to
-            // keep up.  Taking all that waits there locks the loop into
-            // batches whose formation and GPU time double the latency.
-            const int cap = pipe ? std::min(max_batch, std::max(max_batch / 4,
-                                                                (int)(pending.size() / 2)))
-                                 : max_batch;
+            // (Taking all that waits under a backlog locks a steady load near
+            // capacity into batches whose formation and GPU time double the
+            // latency.)
+            const int cap = mtgp::batchCap(pending.size(), max_batch, pipe);
             fs->block_bytes = mtgp::admitBatch(
                 pending, mark, cap, kJumpSkip, arena.size() - kept_bytes - ahead,
                 arena.size() / 2,

@@ -142,6 +142,17 @@ uint64_t admitBatch(std::deque<ServeReq> &pending, std::vector<char> *mark, int 
     return used;
 }
 
+// Requests the next batch may take: max_batch; under a backlog (`backlog`)
+// half of what waits, at least a quarter of max_batch and at least one, so
+// that a burst gets full batches while a steady load near capacity gets
+// batches just large enough to keep up.
+inline int batchCap(size_t pending, int max_batch, bool backlog) {
+    if (!backlog) return max_batch;
+    const size_t half = pending / 2;
+    const int want = half > (size_t)max_batch ? max_batch : (int)half;
+    return std::min(max_batch, std::max({1, max_batch / 4, want}));
+}
+
 // The order of batches on the GPU: a batch that holds requests of a stream
 // must run after that stream's earlier batches, which read and write the
 // stream's window.  Each stream remembers its latest batch by a caller-chosen

@@ -120,3 +120,8 @@ extern "C" int probe_serve(int nreq, const int32_t *pool, const uint32_t *stream
     *nbatches = (int)all.size();
     return arena.free_bytes() == budget ? 0 : -3;  // everything returned
 }
+
+// The next batch's request cap (batchCap).
+extern "C" int probe_batch_cap(uint64_t pending, int max_batch, int backlog) {
+    return batchCap((size_t)pending, max_batch, backlog != 0);
+}

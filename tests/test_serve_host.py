@@ -24,6 +24,7 @@ def probe(tmp_path_factory):
                     os.path.join(HERE, "serve_probe.cpp")], check=True)
     L = ctypes.CDLL(so)
     vp, ci = ctypes.c_void_p, ctypes.c_int
+    L.probe_batch_cap.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
     L.probe_serve.argtypes = [ci, vp, vp, vp, vp, ci, ci, ctypes.c_uint64, ci, ci, ci, vp,
                               ci, vp, vp, vp, vp, vp, vp, vp, vp]
     return L
@@ -161,3 +162,12 @@ def test_stream_in_flight_joins_the_next_batch(probe):
     assert r["admit"][1] < r["retire"][0]
     assert r["deps"] == [set(), {0}, set()]
     assert r["retire"][1] > r["retire"][0]
+
+
+def test_batch_cap(probe):
+    cap = probe.probe_batch_cap
+    assert cap(5, 8192, 0) == 8192            # no backlog: max_batch
+    assert cap(100000, 8192, 1) == 8192       # a burst: full batches
+    assert cap(6000, 8192, 1) == 3000         # near capacity: half of what waits
+    assert cap(3000, 8192, 1) == 2048         # at least a quarter of max_batch
+    assert cap(1, 1, 1) == 1 and cap(0, 2, 1) == 1  # never zero
