@@ -118,6 +118,12 @@ __device__ __noinline__ void mix32(Lane32 L, uint64_t n, char *o) {
     run32<N, TN, B, KIND>(g_mix32, L, L.otab(KIND < 0 ? 0 : KIND), n, (OT *)o);
 }
 
+template <int N, int W, int B, int KIND, int K>
+__device__ __noinline__ void mixk32(Lane32 L, uint64_t n, char *o) {
+    using C = CoreK<N, W, B, KIND, K>;
+    C::run(g_mix32, L, L.otab(KIND < 0 ? 0 : KIND), n, (typename C::OT *)o);
+}
+
 template <int N, int TN, int B, int KIND>
 __device__ __noinline__ void mix64(Lane64 L, uint64_t n, char *o) {
     using OT = typename Out64<(KIND < 0 ? 0 : KIND)>::T;
@@ -189,9 +195,15 @@ k_batch32(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
 
 // K-words-per-thread core (W/K threads per CTA, K = 4 or 2).  SPLIT: tasks
 // may start with a jump; the jump works on the window laid out linearly,
-// which is then moved into the K planes of the generation buffer.
+// which is then moved into the K planes of the generation buffer.  MODE ==
+// -2: items of any kind, each kind's loop out of line on the generation
+// buffer in dynamic shared memory, as in k_batch32.
 template <int N, int W, int B, int MODE, bool SPLIT, int K>
-__global__ void __launch_bounds__(W / K, MODE == -2 ? 1 : 1280 * K / W)
+__global__ void __launch_bounds__(W / K,
+                                  MODE == -2
+                                      ? mixBlocks(1280 * K / W,
+                                                  sizeof(uint32_t) * GeoK<N, W, B, K>::BUF)
+                                      : 1280 * K / W)
 k_batch32xk(const DevParams32 *__restrict__ params, uint32_t *__restrict__ states,
             const BatchTask *__restrict__ tasks, int ntasks,
             const BatchItem *__restrict__ items, char *__restrict__ out,
@@ -200,7 +212,9 @@ k_batch32xk(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
             uint32_t *__restrict__ prewin) {
     constexpr int T = W / K;
     constexpr int PW = GeoK<N, W, B, K>::PW;
-    __shared__ __align__(16) uint32_t buf[GeoK<N, W, B, K>::BUF];
+    constexpr int BUF = GeoK<N, W, B, K>::BUF;
+    __shared__ __align__(16) uint32_t sbuf[MODE == -2 ? 4 : BUF];
+    uint32_t *const buf = MODE == -2 ? g_mix32 : sbuf;
     __shared__ int s_task;
     (void)polys;
     (void)nwords;
@@ -218,7 +232,7 @@ k_batch32xk(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
         if constexpr (SPLIT && kSplit32<N>) {
             using G = typename SplitGeo32xK<N, K>::G;
             static_assert(G::NT == T, "jump geometry must use the kernel's threads");
-            static_assert(G::template bytes<uint32_t>(N / 32 + 1) <= sizeof(buf),
+            static_assert(G::template bytes<uint32_t>(N / 32 + 1) <= sizeof(uint32_t) * BUF,
                           "jump buffers must fit the generation buffer");
             if (TK.j0 >= 0) {
                 for (int k = threadIdx.x; k < N; k += T) buf[k] = src[k];
@@ -255,12 +269,12 @@ k_batch32xk(const DevParams32 *__restrict__ params, uint32_t *__restrict__ state
                 C::run(buf, L, L.otab(MODE < 0 ? 0 : MODE), I.count, (typename C::OT *)o);
             } else {
                 switch (I.kind) {
-                case 0: CoreK<N, W, B, 0, K>::run(buf, L, L.tmp, I.count, (uint32_t *)o); break;
-                case 1: CoreK<N, W, B, 1, K>::run(buf, L, L.flt, I.count, (float *)o); break;
-                case 2: CoreK<N, W, B, 2, K>::run(buf, L, L.flt, I.count, (float *)o); break;
-                case 3: CoreK<N, W, B, 3, K>::run(buf, L, L.flt, I.count, (float *)o); break;
-                case 4: CoreK<N, W, B, 4, K>::run(buf, L, L.flt, I.count, (float *)o); break;
-                default: CoreK<N, W, B, -1, K>::run(buf, L, L.tmp, I.count, nullptr); break;
+                case 0: mixk32<N, W, B, 0, K>(L, I.count, o); break;
+                case 1: mixk32<N, W, B, 1, K>(L, I.count, o); break;
+                case 2: mixk32<N, W, B, 2, K>(L, I.count, o); break;
+                case 3: mixk32<N, W, B, 3, K>(L, I.count, o); break;
+                case 4: mixk32<N, W, B, 4, K>(L, I.count, o); break;
+                default: mixk32<N, W, B, -1, K>(L, I.count, nullptr); break;
                 }
             }
         }
@@ -461,7 +475,9 @@ static cudaError_t mode32xk(const BatchLaunch &b, const DevParams32 *p, uint32_t
     case 2: return go<uint32_t>(k_batch32xk<N, W, B, 2, SPLIT, K>, T, b, p, st, s);
     case 3: return go<uint32_t>(k_batch32xk<N, W, B, 3, SPLIT, K>, T, b, p, st, s);
     case 4: return go<uint32_t>(k_batch32xk<N, W, B, 4, SPLIT, K>, T, b, p, st, s);
-    default: return go<uint32_t>(k_batch32xk<N, W, B, -2, SPLIT, K>, T, b, p, st, s);
+    default:
+        return go<uint32_t>(k_batch32xk<N, W, B, -2, SPLIT, K>, T, b, p, st, s,
+                            sizeof(uint32_t) * GeoK<N, W, B, K>::BUF);
     }
 }
 

@@ -27,10 +27,16 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     o.jump_min = jumpMinSkip(P);
     o.max_gen_skip = kMaxGenSkip;
     o.chunk_tune = force_chunk ? force_chunk : P.tune.split_chunk;
-    // Plans whose generated values mix kinds (a generated skip counts as
-    // kind -1) run on the one-word core, whose per-kind loops are out of line
-    // at no cost.  The same rule as planCore's mode, decided up front because
-    // the chunk length depends on the core's resident CTAs.
+    // Whether the generated values mix kinds (a generated skip counts as kind
+    // -1): the same rule as planCore's mode, decided up front because the
+    // chunk length depends on the core's resident CTAs.  32-bit plans of mixed
+    // kinds run on any core (each kind's loop out of line), except that
+    // tasks that jump twice inside the kernel (a run start, then a chunk
+    // offset) keep a mixed plan on the one-word core, whose CTAs jump with
+    // twice the threads (on the two-word core such jumps drew out the tail
+    // of mixed serving batches: 3.5 against 4.2 M requests/s); the 64-bit
+    // two-word kernel has one kind per launch, so mixed 64-bit plans take the
+    // one-word core.
     int kinds = -3;
     auto addKind = [&kinds](int k) { kinds = (kinds == -3 || kinds == k) ? k : -2; };
     auto jumped = [&o](uint64_t v) { return o.can_jump && v >= o.jump_min; };
@@ -44,7 +50,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (it.count) addKind(it.kind);
         }
     }
-    int core = force_core ? force_core : kinds == -2 ? 1 : P.tune.core;
+    int core = force_core ? force_core : (kinds == -2 && T::kBits == 64) ? 1 : P.tune.core;
     // 64-bit cores: two words per thread (knob 2 or 4) or one; the two-word
     // kernel has no jump code, so plans with in-kernel jumps (jump_parts =
     // -1) take the one-word core
@@ -61,6 +67,12 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     std::string msg;
     int rc = planCore(items, nitems, o, &R, &msg);
     if (rc) return setErr(rc, "%s", msg.c_str());
+    if (T::kBits == 32 && kinds == -2 && kernel_jumps && !force_core && core != 1)
+        for (const PlanTask &pt : R.tasks)
+            if (pt.run && pt.off) {
+                core = 1;
+                break;
+            }
     const uint64_t out_bytes = R.out_bytes;
     const int64_t chunk = R.chunk;
     const bool cut = chunk > 0;
@@ -231,7 +243,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->out_bytes = out_bytes;
     pl->grid = (int)P.tune.batch_grid;
     pl->split = split;
-    pl->core = pl->mode == -2 ? 1 : core;
+    pl->core = (pl->mode == -2 && T::kBits == 64) ? 1 : core;
     pl->chunk = cut ? chunk : 0;
     pl->nstage = (int)stage_streams.size();
     pl->npre = npre;

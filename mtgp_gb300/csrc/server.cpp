@@ -35,7 +35,7 @@
 // it on the GPU and retires it (latencies, arena space).  So the host work
 // of up to `slots` batches runs in parallel, and the lock they share is held
 // for a few word writes per request.  A batch is admitted (up to max_batch
-// requests and half the arena; under a backlog, half of what waits) when a
+// requests and half the arena; under a backlog, a quarter of what waits) when a
 // slot is free and no other batch is being planned (low load: a lone
 // request goes straight to the GPU; under load the next batch collects what
 // arrives while one is planned), or when a quarter of a full batch is

@@ -168,6 +168,6 @@ def test_batch_cap(probe):
     cap = probe.probe_batch_cap
     assert cap(5, 8192, 0) == 8192            # no backlog: max_batch
     assert cap(100000, 8192, 1) == 8192       # a burst: full batches
-    assert cap(6000, 8192, 1) == 3000         # near capacity: half of what waits
-    assert cap(3000, 8192, 1) == 2048         # at least a quarter of max_batch
+    assert cap(20000, 8192, 1) == 5000        # near capacity: a quarter of what waits
+    assert cap(6000, 8192, 1) == 2048         # at least a quarter of max_batch
     assert cap(1, 1, 1) == 1 and cap(0, 2, 1) == 1  # never zero
