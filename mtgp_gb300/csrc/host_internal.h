@@ -1180,7 +1180,11 @@ struct mtgp_gpu_plan {
     // sum of its jump's parts (nparts descriptors in the blob), made before
     // every launch into slots that are zero (zeroed at allocation, and by the
     // batched kernel as each task reads its slot)
-    int npre = 0, nparts = 0;
+    // A task that jumps twice takes its window from a second launch of parts
+    // (nparts_b, after the first nparts), which jump the run starts made by
+    // the first launch in nmid middle slots (after the npre tasks' slots;
+    // cleared after each launch) by the chunk offsets.
+    int npre = 0, nparts = 0, nmid = 0, nparts_b = 0;
     const JumpPart *d_parts = nullptr;
     void *d_prewin = nullptr;
     size_t cap_prewin = 0;

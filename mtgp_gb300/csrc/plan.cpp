@@ -29,14 +29,13 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     o.chunk_tune = force_chunk ? force_chunk : P.tune.split_chunk;
     // Whether the generated values mix kinds (a generated skip counts as kind
     // -1): the same rule as planCore's mode, decided up front because the
-    // chunk length depends on the core's resident CTAs.  32-bit plans of mixed
-    // kinds run on any core (each kind's loop out of line), except that
-    // tasks that jump twice inside the kernel (a run start, then a chunk
-    // offset) keep a mixed plan on the one-word core, whose CTAs jump with
-    // twice the threads (on the two-word core such jumps drew out the tail
-    // of mixed serving batches: 3.5 against 4.2 M requests/s); the 64-bit
-    // two-word kernel has one kind per launch, so mixed 64-bit plans take the
-    // one-word core.
+    // chunk length depends on the core's resident CTAs.  Plans of mixed kinds
+    // take the one-word core unless a core is forced (the autotuner's
+    // candidates): the 32-bit two- and four-word kernels run mixed kinds too
+    // (each kind's loop out of line), 5-7 % faster on long steady batches,
+    // but serving batches of many short requests had longer tails on them
+    // (p99 at 0.9 load 5-7 ms against 2.5 ms); the 64-bit two-word kernel has
+    // one kind per launch.
     int kinds = -3;
     auto addKind = [&kinds](int k) { kinds = (kinds == -3 || kinds == k) ? k : -2; };
     auto jumped = [&o](uint64_t v) { return o.can_jump && v >= o.jump_min; };
@@ -50,7 +49,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (it.count) addKind(it.kind);
         }
     }
-    int core = force_core ? force_core : (kinds == -2 && T::kBits == 64) ? 1 : P.tune.core;
+    int core = force_core ? force_core : kinds == -2 ? 1 : P.tune.core;
     // 64-bit cores: two words per thread (knob 2 or 4) or one; the two-word
     // kernel has no jump code, so plans with in-kernel jumps (jump_parts =
     // -1) take the one-word core
@@ -67,12 +66,6 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     std::string msg;
     int rc = planCore(items, nitems, o, &R, &msg);
     if (rc) return setErr(rc, "%s", msg.c_str());
-    if (T::kBits == 32 && kinds == -2 && kernel_jumps && !force_core && core != 1)
-        for (const PlanTask &pt : R.tasks)
-            if (pt.run && pt.off) {
-                core = 1;
-                break;
-            }
     const uint64_t out_bytes = R.out_bytes;
     const int64_t chunk = R.chunk;
     const bool cut = chunk > 0;
@@ -116,6 +109,10 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         *idx = hit->second;
         return MTGP_OK;
     };
+    // Where neither the kernel nor jumps ahead of the launch (jump_parts < 0)
+    // can apply a run start and a chunk offset one after the other, the two
+    // make one polynomial.
+    const bool combined = !kernel_jumps && P.tune.jump_parts < 0;
     // every parameter set that jumps gets its tables in one batch, and the
     // chunk offsets not yet cached (with the run start where the two make
     // one polynomial) go to the GPU together, for later plans
@@ -126,7 +123,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             if (!pt.run && !pt.off) continue;
             const int k = P.hpidx[pt.stream];
             if (std::find(sets.begin(), sets.end(), k) == sets.end()) sets.push_back(k);
-            const uint64_t e = pt.run && !kernel_jumps ? pt.run + pt.off : pt.off;
+            const uint64_t e = pt.run && combined ? pt.run + pt.off : pt.off;
             if (pt.off && __builtin_popcountll(e) >= 2) offs.emplace_back(k, e);
         }
         {
@@ -150,7 +147,7 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         // X^run then X^off: the run starts (a requested skip) and the chunk
         // offsets (shared by every long request) are each few, so few
         // distinct polynomials are needed
-        if (pt.run && pt.off && !kernel_jumps) {
+        if (pt.run && pt.off && combined) {
             rc = polyIndex(t.pidx, pt.run + pt.off, &t.j0, true);
         } else if (pt.run && pt.off) {
             rc = polyIndex(t.pidx, pt.run, &t.j0, true);
@@ -190,26 +187,51 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     // ahead of the launch by jump parts (jumpParts() CTAs per jump, all
     // SMs at once), so no jump runs inside the persistent kernel; a chain of
     // two (a run start, then a chunk offset) still jumps inside it.
+    // A task that jumps twice (a run start, then a chunk offset) is jumped
+    // ahead in two launches: the run start once per run, from the stream's
+    // window into a middle slot (after the tasks' slots), with the single
+    // jumps; then each chunk offset from its run's middle slot (their source
+    // offsets are relative to the slots).
     static thread_local std::vector<JumpPart> jparts;
+    static thread_local std::vector<JumpPart> jparts_b;
     jparts.clear();
-    int npre = 0;
+    jparts_b.clear();
+    int npre = 0, nmid = 0;
     if (P.tune.jump_parts >= 0 && npolys > 0) {
         const int tch = T::jumpChunks(P.sh.mexp, (int)pw);
         const int parts = jumpParts(P.tune, tch);
-        for (BatchTask &t : tasks) {
-            if (t.j0 < 0 || t.j1 >= 0) continue;
+        auto addParts = [&](std::vector<JumpPart> &v, uint64_t src, int32_t poly, int32_t dst,
+                            int32_t pidx) {
             for (int q = 0; q < parts; q++) {
                 JumpPart d{};
-                d.src = (uint64_t)t.stream * (uint64_t)P.stride;
-                d.poly = t.j0;
-                d.dst = npre;
-                d.pidx = t.pidx;
+                d.src = src;
+                d.poly = poly;
+                d.dst = dst;
+                d.pidx = pidx;
                 d.ch0 = (int16_t)(q * tch / parts);
                 d.ch1 = (int16_t)((q + 1) * tch / parts);
-                jparts.push_back(d);
+                v.push_back(d);
             }
-            t.pre = ++npre;
-            t.j0 = -1;
+        };
+        for (BatchTask &t : tasks)
+            if (t.j0 >= 0) t.pre = ++npre;
+        std::map<std::pair<int32_t, uint64_t>, int32_t> mid;  // (stream, run) -> middle slot
+        for (size_t q = 0; q < tasks.size(); q++) {
+            BatchTask &t = tasks[q];
+            if (t.j0 < 0) continue;
+            const uint64_t win = (uint64_t)t.stream * (uint64_t)P.stride;
+            if (t.j1 < 0) {
+                addParts(jparts, win, t.j0, t.pre - 1, t.pidx);
+            } else {
+                auto it = mid.find({t.stream, R.tasks[q].run});
+                if (it == mid.end()) {
+                    it = mid.emplace(std::make_pair(t.stream, R.tasks[q].run), npre + nmid++).first;
+                    addParts(jparts, win, t.j0, it->second, t.pidx);
+                }
+                addParts(jparts_b, (uint64_t)it->second * (uint64_t)P.stride, t.j1, t.pre - 1,
+                         t.pidx);
+            }
+            t.j0 = t.j1 = -1;
         }
     }
     // jump_overlap: the tasks that start from a pre-jumped window go last,
@@ -243,11 +265,13 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->out_bytes = out_bytes;
     pl->grid = (int)P.tune.batch_grid;
     pl->split = split;
-    pl->core = (pl->mode == -2 && T::kBits == 64) ? 1 : core;
+    pl->core = core;
     pl->chunk = cut ? chunk : 0;
     pl->nstage = (int)stage_streams.size();
     pl->npre = npre;
+    pl->nmid = nmid;
     pl->nparts = (int)jparts.size();
+    pl->nparts_b = (int)jparts_b.size();
     pl->overlap = nmain < (int)tasks.size();
     pl->nmain = nmain;
     auto align = [](size_t n) { return (n + 255) & ~size_t(255); };
@@ -255,7 +279,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     const size_t off_polys = off_items + align(sizeof(BatchItem) * bitems.size());
     const size_t off_ops = off_polys + align(sizeof(uint32_t) * pw * npolys);
     const size_t off_parts = off_ops + align(sizeof(PowOp) * (size_t)sch.steps());
-    const size_t off_ss = off_parts + align(sizeof(JumpPart) * jparts.size());
+    const size_t off_ss =
+        off_parts + align(sizeof(JumpPart) * (jparts.size() + jparts_b.size()));
     const size_t bytes = off_ss + sizeof(int32_t) * stage_streams.size();
     cudaError_t e = cudaSuccess;
     if (!pl->d_counter) e = devMalloc(&pl->d_counter, 2 * sizeof(unsigned));
@@ -296,7 +321,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
         e = growDev(&pl->d_stage, &pl->cap_stage, sizeof(W) * (size_t)P.stride * pl->nstage);
     if (e == cudaSuccess && pl->npre) {
         const size_t before = pl->cap_prewin;
-        e = growDev(&pl->d_prewin, &pl->cap_prewin, sizeof(W) * (size_t)P.stride * pl->npre);
+        e = growDev(&pl->d_prewin, &pl->cap_prewin,
+                    sizeof(W) * (size_t)P.stride * (pl->npre + pl->nmid));
         if (pl->cap_prewin != before) pl->prewin_fresh = true;
     }
     if (e != cudaSuccess) {
@@ -306,7 +332,9 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
             pl->ntasks = 0;
             pl->nstage = 0;
             pl->npre = 0;
+            pl->nmid = 0;
             pl->nparts = 0;
+            pl->nparts_b = 0;
             pl->out_bytes = 0;
             pl->dirty = false;
         }
@@ -330,6 +358,9 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
     pl->d_powops = reinterpret_cast<const PowOp *>(pl->d_blob + off_ops);
     if (!jparts.empty())
         std::memcpy(h + off_parts, jparts.data(), sizeof(JumpPart) * jparts.size());
+    if (!jparts_b.empty())
+        std::memcpy(h + off_parts + sizeof(JumpPart) * jparts.size(), jparts_b.data(),
+                    sizeof(JumpPart) * jparts_b.size());
     pl->d_parts = reinterpret_cast<const JumpPart *>(pl->d_blob + off_parts);
     if (!stage_streams.empty())
         std::memcpy(h + off_ss, stage_streams.data(), sizeof(int32_t) * stage_streams.size());
@@ -399,6 +430,14 @@ int launchPlan(mtgp_gpu_plan *pl, void *out, void *s) {
         CK(T::parts(P.sh.mexp, P.d_params, P.d_states, pl->d_polys, P.polyWords(), pre, P.stride,
                     pl->d_parts, pl->nparts, js),
            "jumps ahead of the launch");
+        if (pl->nparts_b) {  // chunk offsets from the run starts in the middle slots
+            CK(T::parts(P.sh.mexp, P.d_params, pre, pl->d_polys, P.polyWords(), pre, P.stride,
+                        pl->d_parts + pl->nparts, pl->nparts_b, js),
+               "jumps ahead of the launch");
+            CK(cudaMemsetAsync(pre + (size_t)pl->npre * P.stride, 0,
+                               sizeof(W) * (size_t)P.stride * pl->nmid, js),
+               "clear the middle slots");
+        }
     }
     BatchLaunch b{};
     b.mexp = P.sh.mexp;
@@ -524,6 +563,7 @@ int mtgp_gpu_plan_describe(const mtgp_gpu_plan_t *pl, int64_t *values, int n) {
     if (!pl || (n > 0 && !values)) return setErr(MTGP_ERR_INVALID, "null plan or values");
     const int64_t v[8] = {pl->ntasks, pl->chunk, pl->core, pl->grid,
                           pl->ntasks ? 1 + (pl->nstage > 0) + (pl->nparts > 0) +
+                                           (pl->nparts_b > 0) +
                                            (pl->overlap && pl->nmain > 0)
                                      : 0,
                           pl->split ? 1 : 0, pl->npre, pl->overlap ? 1 : 0};

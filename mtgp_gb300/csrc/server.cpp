@@ -35,11 +35,15 @@
 // it on the GPU and retires it (latencies, arena space).  So the host work
 // of up to `slots` batches runs in parallel, and the lock they share is held
 // for a few word writes per request.  A batch is admitted (up to max_batch
-// requests and half the arena; under a backlog, a quarter of what waits) when a
-// slot is free and no other batch is being planned (low load: a lone
-// request goes straight to the GPU; under load the next batch collects what
-// arrives while one is planned), or when a quarter of a full batch is
-// waiting: only then are several batches planned at once.
+// requests and an eighth of the arena; under a backlog, a quarter of what
+// waits) when a slot is free and no other batch is being planned (low load:
+// a lone request goes straight to the GPU; under load the next batch
+// collects what arrives while one is planned), or when a quarter of a full
+// batch is waiting: only then are several batches planned at once.  Batches
+// of an eighth of the arena keep a steady load at 0.9 of the saturation
+// rate as fast as a burst's (with half the arena a burst ran 10 % faster,
+// and a steady load near that rate tipped into large batches and 5-7 ms
+// latency).
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -108,9 +112,10 @@ struct mtgp_server {
     int nplanning = 0;  // slots whose batch is handed over and not yet launched
     uint64_t next_place = 1;  // number of the batch whose turn it is to take arena space
     // arena bytes of admitted batches not yet placed, and of results kept in
-    // the arena: admission keeps ahead <= arena size - kept, so every batch
-    // admitted can be placed once the batches on the GPU are done, and a
-    // request that cannot stays pending (and cancellable)
+    // the arena (counted from admission: they outlive their batch's block):
+    // admission keeps ahead <= arena size - kept, so every batch admitted
+    // fits in the arena once the batches on the GPU are done, and a request
+    // that does not stays pending (and cancellable)
     uint64_t ahead = 0, kept_bytes = 0;
     uint64_t budget = 0;  // the arena's size
     std::vector<uint64_t> failed;  // numbers of batches that failed to launch (rare)
@@ -274,7 +279,7 @@ void mtgp_server::loop() {
             const int cap = mtgp::batchCap(pending.size(), max_batch, pipe);
             fs->block_bytes = mtgp::admitBatch(
                 pending, mark, cap, kJumpSkip, arena.size() - kept_bytes - ahead,
-                arena.size() / 2,
+                arena.size() / 8,
                 [&](const Req &r) {
                     const uint64_t l = order.latest(r);
                     return !pipe && l && live(l);
@@ -287,6 +292,8 @@ void mtgp_server::loop() {
                 fs->reqs.swap(take);
                 fs->seq = seq;
                 ahead += fs->block_bytes;
+                for (const Req &r : fs->reqs)
+                    if (r.keep) kept_bytes += Arena::round(r.bytes);
                 fs->busy = fs->assigned = fs->planning = true;
                 nplanning++;
                 fs->cv.notify_one();
@@ -374,11 +381,11 @@ void mtgp_server::retireBatch(Slot &sl, int st) {
         const Req &r = sl.reqs[k];
         latency[r.ticket - 1] = sl.lat[k];
         status[r.ticket - 1] = st;
+        if (r.keep && st) kept_bytes -= Arena::round(r.bytes);  // nothing to keep
         if (!st && r.keep && r.bytes) {
             kept[r.ticket] = {r.off, r.bytes};
-            kept_bytes += mtgp::Arena::round(r.bytes);
             if (r.off > at) arena.release(at, r.off - at);
-            at = r.off + mtgp::Arena::round(r.bytes);
+            at = r.off + Arena::round(r.bytes);
         }
         completed++;
         if (!st) bytes_done += r.bytes;

@@ -8,7 +8,7 @@
 using namespace mtgp;
 
 // All requests are pending at the start.  Each round does the first of:
-//   - admit one batch (at most max_batch requests and budget / 2 bytes,
+//   - admit one batch (at most max_batch requests and budget / 8 bytes,
 //     unless one request; all admitted batches not yet placed at most the
 //     budget) if fewer than `slots` batches are admitted and not retired;
 //     a stream with a batch not yet retired joins only while at least
@@ -62,7 +62,7 @@ extern "C" int probe_serve(int nreq, const int32_t *pool, const uint32_t *stream
             Batch b;
             const bool pipe = (int)pending.size() >= pipe_backlog;
             b.bytes = admitBatch(
-                pending, mark, max_batch, uint64_t(1) << 17, budget - ahead, budget / 2,
+                pending, mark, max_batch, uint64_t(1) << 17, budget - ahead, budget / 8,
                 [&](const ServeReq &r) {
                     const uint64_t l = order.latest(r);
                     return !pipe && l && !all[l - 1].retired;

@@ -234,6 +234,53 @@ def test_autotune_leaves_pool_and_picks_exact_plan(gpu, orc):
         assert np.array_equal(got[a:a + int(counts[j])], o.fill(0, int(counts[j]))), j
 
 
+@pytest.mark.parametrize("bits,table", [(32, "mtgp32_fast_11213"), (64, "mtgp64dc_fast_11213"),
+                                        (32, "mtgp32_fast_44497")])
+@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("parts", [0, -1])
+def test_batch_skip_then_split_chunks(gpu, orc, bits, table, mixed, parts):
+    """Long requests that start after a long skip and are split into chunks:
+    each chunk's start is the run start (a jump by the skip) then the chunk
+    offset (a second jump).  Ahead of the launch (parts 0) the run starts
+    are jumped once per run into middle slots and the chunk offsets from
+    there, by a second launch of jump parts; inside the kernel (parts -1,
+    where the exponent has it) the two jumps follow each other.  Bit-exact
+    outputs and final states, across two launches of the same plan."""
+    from mtgp_gb300.api import Pool, work_items
+    tbl = load_table(table)
+    if parts < 0 and tbl[0].mexp == 44497:
+        pytest.skip("MEXP 44497 jumps only ahead of the launch")
+    rng = np.random.default_rng(bits + 2 * mixed + tbl[0].mexp)
+    nstreams = 12
+    plist = [tbl[i] for i in range(3)]
+    pidx = np.arange(nstreams) % 3
+    seeds = np.arange(nstreams) + 11
+    pool = Pool.create(plist, seeds, pidx)
+    counts = rng.integers(2000, 9000, nstreams)
+    skips = np.array([(1 << 17) + 12345, 1 << 20, 0, (1 << 18) + 3] * 3, np.uint64)
+    kinds = rng.integers(0, 5, nstreams) if mixed else np.zeros(nstreams, np.int64)
+    esz = bits // 8
+    offs = np.concatenate([[0], np.cumsum(counts)[:-1]]) * esz
+    pool.set_tuning("split_chunk", 1500)
+    pool.set_tuning("jump_parts", parts)
+    plan = pool.plan(work_items(range(nstreams), kinds, counts, offs, skips))
+    desc = plan.describe()
+    assert (desc["prejumps"] > nstreams and not desc["jumps"]) if parts == 0 else desc["jumps"]
+    out = torch.zeros(int(sum(counts)) * esz // 4 + 16, dtype=torch.int32, device="cuda")
+    gens = {s: orc.gen(plist[pidx[s]], seed=int(seeds[s])) for s in range(nstreams)}
+    for rep in range(2):
+        plan.launch(out)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().view(np.uint8)
+        for k in range(nstreams):
+            gens[k].skip(int(skips[k]))
+            ref = np_bits(gens[k].fill(int(kinds[k]), int(counts[k])), bits).view(np.uint8)
+            assert np.array_equal(got[offs[k]:offs[k] + ref.size], ref), (rep, k)
+        w = pool.windows()
+        for s in range(nstreams):
+            assert np.array_equal(w[s], gens[s].window()), (rep, s)
+
+
 @pytest.mark.parametrize("bits,core", [(32, 4), (32, 2), (64, 2), (64, 1)])
 @pytest.mark.parametrize("kind", [0, 1, 2, 3, 4, -1])
 def test_batch_vector_cores_one_kind(gpu, orc, bits, core, kind):

@@ -3,7 +3,7 @@
 request is admitted once; a stream's requests are admitted in submission
 order; a batch holding a stream whose earlier batch is still in flight is
 ordered after that batch; a long skip only opens a stream's part of a batch;
-batches respect max_batch and half the budget; blocks are placed in
+batches respect max_batch and an eighth of the budget; blocks are placed in
 admission order; in-flight outputs never overlap in the arena nor exceed the
 budget; all space returns."""
 import ctypes
@@ -111,9 +111,9 @@ def test_admission_invariants(probe, seed, pipe_backlog):
         sp = sorted(spans[b])
         assert all(sp[i][1] <= sp[i + 1][0] for i in range(len(sp) - 1))
         assert all(x1 <= budget for _, x1 in sp)
-        # at most half the budget, unless the batch is one request
+        # at most an eighth of the budget, unless the batch is one request
         size = sum(x1 - x0 for x0, x1 in sp)
-        assert size <= budget // 2 or len(sp) == 1
+        assert size <= budget // 8 or len(sp) == 1
     # batches in the arena at the same time share no bytes
     for a in range(nb):
         for b in range(a + 1, nb):
@@ -125,8 +125,8 @@ def test_admission_invariants(probe, seed, pipe_backlog):
 
 def test_first_come_first_served(probe):
     # a batch whose block does not fit holds back later ones (no overtaking by
-    # small requests) until space returns; a batch takes at most half the
-    # budget unless it is one request
+    # small requests) until space returns; a batch takes at most an eighth of
+    # the budget unless it is one request
     r = simulate(probe, [0, 0, 0], [0, 1, 2], [0, 0, 0], [700_000, 700_000, 1000], (3, 1),
                  1 << 20, 8, 4, 0)
     assert r["rc"] == 0
