@@ -495,7 +495,8 @@ int mtgp32_gpu_batch_noalloc(const mtgp32_params_fast_t *params, int nparams,
  * one launch per request).  A server owns a device output arena of
  * `budget_bytes` (the memory budget) and a scheduler thread that admits
  * pending requests first-come-first-served into batches of at most
- * `max_batch` requests (and an eighth of the budget), keeps up to `slots` (at most
+ * `max_batch` requests (and an eighth of the budget, up to half under a
+ * backlog), keeps up to `slots` (at most
  * 256) batches in flight on their own CUDA streams, and copies each result
  * to its destination when the batch completes.  A batch's outputs take one
  * block of the arena, placed in admission order; results kept in the arena

@@ -35,15 +35,11 @@
 // it on the GPU and retires it (latencies, arena space).  So the host work
 // of up to `slots` batches runs in parallel, and the lock they share is held
 // for a few word writes per request.  A batch is admitted (up to max_batch
-// requests and an eighth of the arena; under a backlog, a quarter of what
-// waits) when a slot is free and no other batch is being planned (low load:
+// requests, under a backlog a quarter of what waits, and batchBytes of
+// output) when a slot is free and no other batch is being planned (low load:
 // a lone request goes straight to the GPU; under load the next batch
 // collects what arrives while one is planned), or when a quarter of a full
-// batch is waiting: only then are several batches planned at once.  Batches
-// of an eighth of the arena keep a steady load at 0.9 of the saturation
-// rate as fast as a burst's (with half the arena a burst ran 10 % faster,
-// and a steady load near that rate tipped into large batches and 5-7 ms
-// latency).
+// batch is waiting: only then are several batches planned at once.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -118,6 +114,7 @@ struct mtgp_server {
     // that does not stays pending (and cancellable)
     uint64_t ahead = 0, kept_bytes = 0;
     uint64_t budget = 0;  // the arena's size
+    uint64_t pending_bytes = 0;  // output bytes of the pending requests (rounded)
     std::vector<uint64_t> failed;  // numbers of batches that failed to launch (rare)
     // set when admission may take more: a submission, a retired batch or
     // released space since the scheduler's last admission pass
@@ -279,12 +276,13 @@ void mtgp_server::loop() {
             const int cap = mtgp::batchCap(pending.size(), max_batch, pipe);
             fs->block_bytes = mtgp::admitBatch(
                 pending, mark, cap, kJumpSkip, arena.size() - kept_bytes - ahead,
-                arena.size() / 8,
+                mtgp::batchBytes(pending_bytes, arena.size()),
                 [&](const Req &r) {
                     const uint64_t l = order.latest(r);
                     return !pipe && l && live(l);
                 },
                 &take, 4 * (size_t)max_batch);
+            pending_bytes -= fs->block_bytes;
             if (!take.empty()) {
                 const uint64_t seq = ++batches;
                 // the batches still in flight that hold some of its streams
@@ -506,6 +504,7 @@ void mtgp_server::pushLocked(Req &r) {
     latency.push_back(-1.0);
     status.push_back(1);
     pending.push_back(r);
+    pending_bytes += Arena::round(r.bytes);
     dirty = true;
     if (sched_waiting) cv.notify_one();
 }
@@ -550,6 +549,7 @@ int mtgp_server_cancel(mtgp_server_t *s, uint64_t ticket) {
         s->latency[ticket - 1] = 0;
         s->status[ticket - 1] = MTGP_ERR_BUSY;  // cancelled before it ran
         s->completed++;
+        s->pending_bytes -= mtgp::Arena::round(it->bytes);
         s->pending.erase(it);
         s->cv_done.notify_all();
         return MTGP_OK;

@@ -154,6 +154,16 @@ inline int batchCap(size_t pending, int max_batch, bool backlog) {
     return std::min(max_batch, std::max({1, max_batch / 4, want}));
 }
 
+// Output bytes the next batch may take: pending_bytes / 8, at least an
+// eighth and at most half of the arena.  Under a burst the batches are large
+// (fewer chains of batches on the GPU); a steady load keeps batches of an
+// eighth of the arena, small enough that it sustains 0.9 of a burst's rate
+// at low latency (a fixed half of the arena tipped such a load into large
+// batches and 5-7 ms latency; a fixed eighth ran a burst 5 % slower).
+inline uint64_t batchBytes(uint64_t pending_bytes, uint64_t arena) {
+    return std::min(arena / 2, std::max(arena / 8, pending_bytes / 8));
+}
+
 // The order of batches on the GPU: a batch that holds requests of a stream
 // must run after that stream's earlier batches, which read and write the
 // stream's window.  Each stream remembers its latest batch by a caller-chosen

@@ -125,3 +125,8 @@ extern "C" int probe_serve(int nreq, const int32_t *pool, const uint32_t *stream
 extern "C" int probe_batch_cap(uint64_t pending, int max_batch, int backlog) {
     return batchCap((size_t)pending, max_batch, backlog != 0);
 }
+
+// The next batch's byte cap (batchBytes).
+extern "C" uint64_t probe_batch_bytes(uint64_t pending_bytes, uint64_t arena) {
+    return batchBytes(pending_bytes, arena);
+}

@@ -25,6 +25,8 @@ def probe(tmp_path_factory):
     L = ctypes.CDLL(so)
     vp, ci = ctypes.c_void_p, ctypes.c_int
     L.probe_batch_cap.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
+    L.probe_batch_bytes.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+    L.probe_batch_bytes.restype = ctypes.c_uint64
     L.probe_serve.argtypes = [ci, vp, vp, vp, vp, ci, ci, ctypes.c_uint64, ci, ci, ci, vp,
                               ci, vp, vp, vp, vp, vp, vp, vp, vp]
     return L
@@ -171,3 +173,11 @@ def test_batch_cap(probe):
     assert cap(20000, 8192, 1) == 5000        # near capacity: a quarter of what waits
     assert cap(6000, 8192, 1) == 2048         # at least a quarter of max_batch
     assert cap(1, 1, 1) == 1 and cap(0, 2, 1) == 1  # never zero
+
+
+def test_batch_bytes(probe):
+    nb = probe.probe_batch_bytes
+    gb = 1 << 30
+    assert nb(0, 8 * gb) == gb                # a light load: an eighth of the arena
+    assert nb(16 * gb, 8 * gb) == 2 * gb      # a backlog: an eighth of what waits
+    assert nb(100 * gb, 8 * gb) == 4 * gb     # a burst: at most half the arena
