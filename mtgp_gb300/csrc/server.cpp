@@ -17,7 +17,8 @@
 //     those batches: an event wait per earlier batch on the new batch's
 //     CUDA stream of that pool, made once they are launched;
 //   - a batch's outputs take one block of the device output arena (the
-//     memory budget), placed in admission order once the batch is planned;
+//     memory budget), placed in admission order (at admission if there is
+//     room, else once the batch is planned);
 //   - a request's skip is done by generation when short and by a GF(2) jump
 //     when long (mtgp_work_item_t);
 //   - when a batch completes, results are copied to the callers'
@@ -152,6 +153,7 @@ struct mtgp_server {
     int planBatch(Slot &sl, double *plan_s);
     int launchBatch(Slot &sl);
     int orderBatch(Slot &sl, std::unique_lock<std::mutex> &lk, int rc);
+    bool placeNow(Slot &sl);
     void retireBatch(Slot &sl, int st);
 };
 
@@ -185,22 +187,39 @@ int mtgp_server::planBatch(Slot &sl, double *plan_s) {
     return rc;
 }
 
-// Take the batch's arena block in admission order (waiting for space), then
-// order its CUDA stream after the batches that hold its streams (waiting for
-// their launches).  With rc set (planning failed) only the turn is taken.
-// Called and returns with the lock held.
-int mtgp_server::orderBatch(Slot &sl, std::unique_lock<std::mutex> &lk, int rc) {
-    cv_turn.wait(lk, [&] {
-        if (stop.load()) return true;
-        if (next_place != sl.seq) return false;
-        if (rc) return true;
-        sl.has_block = arena.alloc(sl.block_bytes, &sl.block);
-        return sl.has_block;
-    });
-    if (stop.load() && next_place != sl.seq) return mtgp::recordError(MTGP_ERR_BUSY, "stopping");
+// Place a batch's block now if it is its turn and the arena has room (with
+// the lock held; the scheduler tries it at admission, so that a batch whose
+// planning is slow does not hold back the placement of the next ones).
+bool mtgp_server::placeNow(Slot &sl) {
+    if (sl.has_block || next_place != sl.seq || !arena.alloc(sl.block_bytes, &sl.block))
+        return false;
+    sl.has_block = true;
     next_place++;
     ahead -= sl.block_bytes;
     cv_turn.notify_all();
+    return true;
+}
+
+// Take the batch's arena block in admission order (waiting for space) unless
+// it was placed at admission, then order its CUDA stream after the batches
+// that hold its streams (waiting for their launches).  With rc set (planning
+// failed) only the turn is taken.  Called and returns with the lock held.
+int mtgp_server::orderBatch(Slot &sl, std::unique_lock<std::mutex> &lk, int rc) {
+    if (!sl.has_block) {
+        cv_turn.wait(lk, [&] {
+            if (stop.load()) return true;
+            if (next_place != sl.seq) return false;
+            return rc != MTGP_OK || placeNow(sl);
+        });
+        if (!sl.has_block) {  // planning failed, or stopping
+            if (next_place == sl.seq) {
+                next_place++;
+                ahead -= sl.block_bytes;
+                cv_turn.notify_all();
+            }
+            if (!rc) rc = mtgp::recordError(MTGP_ERR_BUSY, "stopping");
+        }
+    }
     if (!rc)
         for (Req &r : sl.reqs) r.off += sl.block;
     for (int p = 0; p < 2; p++)
@@ -290,6 +309,7 @@ void mtgp_server::loop() {
                 fs->reqs.swap(take);
                 fs->seq = seq;
                 ahead += fs->block_bytes;
+                placeNow(*fs);
                 for (const Req &r : fs->reqs)
                     if (r.keep) kept_bytes += Arena::round(r.bytes);
                 fs->busy = fs->assigned = fs->planning = true;
