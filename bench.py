@@ -705,8 +705,10 @@ def main():
     ap.add_argument("--serve-burst", type=int, default=100000,
                     help="requests of the burst that finds the saturation rate")
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--serve-slots", type=int, default=8,
-                    help="batches the server keeps in flight (CUDA streams)")
+    ap.add_argument("--serve-slots", type=int, default=4,
+                    help="batches the server keeps in flight (measured: 4 slots "
+                         "4.3-4.4 M req/s, 8 slots 4.1-4.2, 16 slots 3.9; p99 at "
+                         "0.9 load 2.3-2.7 ms for each)")
     ap.add_argument("--serve-sample", type=int, default=10,
                     help="requests of each output type checked per timed serving trace")
     ap.add_argument("--uniform", type=int, default=0,
