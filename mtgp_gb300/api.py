@@ -388,7 +388,7 @@ class Server:
     returns.  Without `dst` the result stays in the server's device arena:
     `result(ticket)` is a zero-copy view of it until `release(ticket)`."""
 
-    def __init__(self, pool32=None, pool64=None, budget_bytes=1 << 30, slots=8, max_batch=4096):
+    def __init__(self, pool32=None, pool64=None, budget_bytes=1 << 30, slots=4, max_batch=4096):
         self.pools = (pool32, pool64)  # keep the pools alive
         h = ctypes.c_void_p()
         check(lib().mtgp_server_create(ctypes.byref(h), pool32.h if pool32 else None,
