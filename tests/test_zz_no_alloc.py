@@ -9,7 +9,8 @@ call's output and advanced windows bit-exactly against the pool entry point
 (mtgp32_gpu_pool_submit) run on the same windows and items: batches of one
 output kind (the two-word core), batches that mix kinds and advance-only
 items (the one-word core), another exponent, and the default parameter
-index.  The file is named so that pytest collects it last.
+index; and batches with advance-only items directly against the oracle.
+The file is named so that pytest collects it last.
 """
 import ctypes
 
@@ -71,6 +72,54 @@ def _compare(table, nparams, nstreams, kinds, use_pidx, seed0):
         assert torch.equal(got, ref), call
         w = dev_win.cpu().numpy().view(np.uint32)[:, :size]
         assert np.array_equal(w, pool.windows()), call
+
+
+def test_noalloc_vs_oracle(gpu, orc):
+    """The entry point against the oracle directly: three parameter sets, a
+    few streams, items of every output kind and advance-only items (the
+    entry point takes no skips), in stream order, over two calls."""
+    from mtgp_gb300._lib import check, lib
+    from mtgp_gb300.api import Pool, work_items
+    tbl = load_table("mtgp32_fast_11213")
+    mexp = tbl[0].mexp
+    size, stride = mexp // 32 + 1, _stride(mexp)
+    nparams, nstreams = 3, 6
+    plist = [tbl[i] for i in range(nparams)]
+    pidx = (np.arange(nstreams) % nparams).astype(np.int32)
+    seeds = np.arange(nstreams) + 77
+    pool = Pool.create(plist, seeds, pidx)
+    win = np.zeros((nstreams, stride), dtype=np.uint32)
+    win[:, :size] = pool.windows()
+    dev_win = torch.from_numpy(win.view(np.int32)).cuda()
+    parr = (MTGP32Params * nparams)(*plist)
+    gens = [orc.gen(plist[pidx[s]], seed=int(seeds[s])) for s in range(nstreams)]
+    rng = np.random.default_rng(78)
+    for call in range(2):
+        n = 24
+        streams = rng.integers(0, nstreams, n)
+        kinds = rng.integers(-1, 5, n)
+        counts = rng.integers(1, 7000, n)
+        sizes = np.where(kinds >= 0, counts, 0)
+        offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]) * 4
+        items = work_items(streams, kinds, counts, offs)
+        got = torch.zeros(int(sizes.sum()) + 8, dtype=torch.int32, device="cuda")
+        check(lib().mtgp32_gpu_batch_noalloc(
+            parr, nparams, pidx.ctypes.data_as(ctypes.c_void_p),
+            ctypes.c_void_p(dev_win.data_ptr()), nstreams, items, n,
+            ctypes.c_void_p(got.data_ptr()),
+            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        torch.cuda.synchronize()
+        out = got.cpu().numpy().view(np.uint8)
+        for k in range(n):
+            g = gens[streams[k]]
+            if kinds[k] < 0:
+                g.skip(int(counts[k]))
+                continue
+            ref = np.ascontiguousarray(g.fill(int(kinds[k]), int(counts[k]))).view(np.uint8)
+            assert np.array_equal(out[offs[k]:offs[k] + ref.size], ref), (call, k)
+        w = dev_win.cpu().numpy().view(np.uint32)[:, :size]
+        for s in range(nstreams):
+            assert np.array_equal(w[s], gens[s].window()), (call, s)
 
 
 @pytest.mark.parametrize("kinds", [[0], [3], [0, 1, 2, 3, 4], [-1, 0, 2]],
