@@ -208,8 +208,8 @@ int makePlan(Pool<T> &P, const mtgp_work_item_t *items, int nitems, mtgp_gpu_pla
                 d.poly = poly;
                 d.dst = dst;
                 d.pidx = pidx;
-                d.ch0 = (int16_t)(q * tch / parts);
-                d.ch1 = (int16_t)((q + 1) * tch / parts);
+                d.ch0 = (int16_t)partChunk(q, tch, parts);
+                d.ch1 = (int16_t)partChunk(q + 1, tch, parts);
                 v.push_back(d);
             }
         };

@@ -179,8 +179,8 @@ int fillSingle(Obj *h, int kind, void *out, size_t n, void *s) {
                 d.poly = c - 1;
                 d.dst = c;
                 d.pidx = P.hpidx[0];
-                d.ch0 = (int16_t)(q * tchunks / parts);
-                d.ch1 = (int16_t)((q + 1) * tchunks / parts);
+                d.ch0 = (int16_t)partChunk(q, tchunks, parts);
+                d.ch1 = (int16_t)partChunk(q + 1, tchunks, parts);
             }
         CK(cudaMemcpyAsync(L.d_desc, L.h_desc, bytes, cudaMemcpyHostToDevice, S(s)),
            "upload fill descriptors");
