@@ -126,15 +126,6 @@ constexpr int kJumpParts = 4;
 
 // CTAs per jump made ahead of a batched launch, for a jump of tchunks tap
 // chunks (tuning knob jump_parts).
-// First tap chunk of part q of a jump split into `parts` over `tchunks`
-// chunks (part q covers [partChunk(q), partChunk(q + 1))).  A part generates
-// the sequence up to its last chunk and correlates only its own, so the
-// later parts are the longer ones: the rounding gives the extra chunks to
-// the earlier parts (11 chunks in 4 parts: 3, 3, 3, 2 rather than 2, 3, 3, 3).
-inline int partChunk(int q, int tchunks, int parts) {
-    return (q * tchunks + parts - 1) / parts;
-}
-
 inline int jumpParts(const Tuning &t, int tchunks) {
     const int64_t p = t.jump_parts > 0 ? t.jump_parts : kJumpParts;
     return (int)std::min<int64_t>(p, tchunks);

@@ -33,6 +33,16 @@
 
 namespace mtgp {
 
+// First tap chunk of part q of a jump split into `parts` over `tchunks`
+// chunks (part q covers [partChunk(q), partChunk(q + 1))).  A part generates
+// the sequence up to its last chunk and correlates only its own, so the
+// later parts are the longer ones: the rounding gives the extra chunks to
+// the earlier parts (11 chunks in 4 parts: 3, 3, 3, 2 rather than 2, 3, 3, 3).
+inline int partChunk(int q, int tchunks, int parts) {
+    const int rem = tchunks % parts;
+    return q * (tchunks / parts) + (q < rem ? q : rem);
+}
+
 struct PlanOptions {
     int nstreams = 0;
     size_t word_bytes = 4;          // bytes of one output value

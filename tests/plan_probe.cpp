@@ -45,3 +45,8 @@ extern "C" int probe_plan(const mtgp_work_item_t *items, int nitems, int nstream
     std::memcpy(stage, r.stage_streams.data(), sizeof(int32_t) * r.stage_streams.size());
     return 0;
 }
+
+// The tap-chunk ranges of a jump's parts (partChunk): bounds[0..parts].
+extern "C" void probe_part_chunks(int tchunks, int parts, int32_t *bounds) {
+    for (int q = 0; q <= parts; q++) bounds[q] = partChunk(q, tchunks, parts);
+}

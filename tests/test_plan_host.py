@@ -202,3 +202,21 @@ def test_plan_automatic_chunk(probe):
     rc, res = plan(probe, items + [(4, 0, 5_000_000, 4_800_000, 0)], 5, resident=64)
     assert rc == 0 and res[3] == 1 << 17
     check(items + [(4, 0, 5_000_000, 4_800_000, 0)], res, 5, 4, True, 0)
+
+
+def test_jump_part_chunks(probe):
+    """Every tap chunk of a jump goes to exactly one part, no part is empty,
+    and the earlier parts (which generate less of the sequence) take the
+    extra chunks."""
+    import ctypes
+    probe.probe_part_chunks.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    for tch in range(1, 64):
+        for parts in range(1, tch + 1):
+            b = np.zeros(parts + 1, np.int32)
+            probe.probe_part_chunks(tch, parts, b.ctypes.data_as(ctypes.c_void_p))
+            sizes = np.diff(b)
+            assert b[0] == 0 and b[-1] == tch and (sizes > 0).all(), (tch, parts, b)
+            assert (np.diff(sizes) <= 0).all(), (tch, parts, sizes)
+    b = np.zeros(5, np.int32)
+    probe.probe_part_chunks(11, 4, b.ctypes.data_as(ctypes.c_void_p))
+    assert b.tolist() == [0, 3, 6, 9, 11]
