@@ -557,10 +557,11 @@ int mtgp_server_results(mtgp_server_t *s, double *latency, int *status,
 int mtgp_server_stats(mtgp_server_t *s, uint64_t *completed, uint64_t *bytes,
                       uint64_t *batches);
 /* Host time spent so far, in seconds: [0] admitting requests (the
- * scheduler thread), [1] planning and launching batches and [2] retiring
- * them (summed over the slots' worker threads, which run in parallel),
- * [3] the scheduler waiting for work, [4] the planning part of [1] (the
- * first n of these five). */
+ * scheduler thread), [1] planning and launching batches (with the waits for
+ * arena space and for the launches of earlier batches of the same streams)
+ * and [2] retiring them (summed over the slots' worker threads, which run
+ * in parallel), [3] the scheduler waiting for work, [4] the planning part of
+ * [1] (the first n of these five). */
 int mtgp_server_profile(mtgp_server_t *s, double *seconds, int n);
 /* Submit n requests at their arrival times (seconds after the call starts),
  * then drain; wall_s receives the elapsed time. */
